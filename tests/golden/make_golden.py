@@ -1,0 +1,91 @@
+"""Generate the golden vectors the oracle and the CUDA path are pinned to.
+
+Run in a checkout next to the reference (it executes the reference's own
+z06 Python on CPU through ``oracle/refrun``):
+
+    python tests/golden/make_golden.py [case ...]
+
+Each case builds a synthetic mesh with this package's generator, writes it
+as a Gmsh v2 file plus the SFC ordering the reference reads from its cache,
+runs the reference in a subprocess and stores a compressed ``.npz`` here.
+Small meshes keep every intermediate; the 2D benchmark mesh keeps hashes of
+its integer arrays and the vectors that are not reproducible from a seed.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from dg_nn_public_gb300 import mesh as dgmesh  # noqa: E402
+from dg_nn_public_gb300 import sfc as dgsfc  # noqa: E402
+
+# name: (kind, n, options)
+CASES = {
+    "tri3_sinh": ("tri", 3, dict(problem="sinh2d", gmres_its=90)),
+    "tri4_sin": ("tri", 4, dict(problem="sin", gmres_its=90)),
+    "tet2_sin": ("tet", 2, dict(problem="sin", gmres_its=90)),
+    "tet3_v22": ("tet", 3, dict(problem="sin", pre_smooth_its=2, post_smooth_its=2, gmres_its=120)),
+    "tri32_c1": ("tri", 32, dict(problem="sin", gmres_its=400, full=False)),
+}
+
+FULL_KEYS_SKIP = ()
+REDUCED_KEEP = ("apply_r", "smooth_x", "rhs", "RARvalues", "mg_e", "pc_x", "x_solution", "its",
+                "res_hist", "l2err", "linferr", "ncolor", "nlevel", "nodes_per_level",
+                "t_apply", "t_solve", "t_rar", "t_mesh_setup", "t_rhs", "t_precond", "threads")
+HASHED = ("x_ref_in", "nbf", "alnmt", "glb_bcface_type", "fina", "cola", "whichc", "sfc")
+
+
+def array_digest(a) -> str:
+    a = np.ascontiguousarray(a)
+    h = hashlib.sha256()
+    h.update(str(a.dtype.str).encode())
+    h.update(str(a.shape).encode())
+    h.update(a.tobytes())
+    return h.hexdigest()
+
+
+def run_case(name: str) -> str:
+    kind, n, opts = CASES[name]
+    opts = dict(opts)
+    full = opts.pop("full", True)
+    g = dgmesh.unit_square_tri_mesh(n) if kind == "tri" else dgmesh.unit_cube_kuhn_mesh(n)
+    m = dgmesh.ingest(g)
+    order = dgsfc.hilbert_sfc_order(m.cg_coords)
+    work = tempfile.mkdtemp(prefix="golden_")
+    mp = os.path.join(work, "mesh.msh")
+    dgmesh.write_gmsh22(mp, g)
+    sp = os.path.join(work, "sfc.npy")
+    np.save(sp, order)
+    op = os.path.join(work, "opts.json")
+    with open(op, "w") as fh:
+        json.dump(opts, fh)
+    raw = os.path.join(work, "out.npz")
+    subprocess.run([sys.executable, "-m", "oracle.refrun.run_reference", mp, sp, raw, op],
+                   cwd=REPO, check=True, stdout=subprocess.DEVNULL)
+    d = dict(np.load(raw))
+    meta = dict(kind=kind, n=n, seed=0, opts=opts, full=full)
+    if full:
+        keep = {k: v for k, v in d.items()}
+    else:
+        keep = {k: d[k] for k in REDUCED_KEEP if k in d}
+        meta["digests"] = {k: array_digest(d[k]) for k in HASHED if k in d}
+    keep["meta_json"] = np.asarray(json.dumps(meta))
+    out = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(out, **keep)
+    return out
+
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(CASES)
+    for nm in names:
+        print("generated", run_case(nm))

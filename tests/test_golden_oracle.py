@@ -1,0 +1,113 @@
+"""Pin the CPU oracle and the mesh/element setup to the reference's own outputs.
+
+The golden vectors come from running the reference's z06 Python on CPU
+(tests/golden/make_golden.py).  Integer arrays must match exactly; floating
+point stages within a few units of roundoff of the FP64 reference.
+"""
+import numpy as np
+import pytest
+
+from dg_nn_public_gb300 import element
+from oracle.dg_oracle import OracleDG, upsample_index
+from golden_util import SMALL_CASES, load, rebuild, rel
+
+FP_TOL = 5e-13      # relative (max-abs) tolerance for single FP64 stages
+SOL_TOL = 1e-11     # relative tolerance on the GMRES solution
+
+
+@pytest.fixture(scope="module", params=SMALL_CASES)
+def case(request):
+    d, meta = load(request.param)
+    g, m, el, order = rebuild(meta)
+    opts = meta["opts"]
+    O = OracleDG(m, el, element.drst_duv(m.ndim), eta_e=opts.get("eta_e", 90.0),
+                 pre_smooth_its=opts.get("pre_smooth_its", 3),
+                 post_smooth_its=opts.get("post_smooth_its", 3))
+    return d, meta, m, el, order, O
+
+
+def test_mesh_ingest_bit_exact(case):
+    d, meta, m, el, order, O = case
+    assert np.array_equal(m.x_ref_in, d["x_ref_in"])
+    assert np.array_equal(m.nbf, d["nbf"])
+    assert np.array_equal(m.alnmt, d["alnmt"])
+    assert np.array_equal(m.glb_bcface_type, d["glb_bcface_type"])
+    assert np.array_equal(m.cg_ndglno, d["cg_ndglno"])
+    assert np.array_equal(np.asarray(m.bc_node_list), d["bc_node_list"])
+    assert np.array_equal(order, d["sfc"])
+
+
+def test_element_tables(case):
+    d, meta, m, el, order, O = case
+    for k in ("n", "nlx", "weight", "sn", "snlx", "sweight"):
+        a, b = getattr(el, k), d["el_" + k]
+        assert a.shape == b.shape
+        assert np.abs(a - b).max() < 1e-13, k
+    assert np.array_equal(el.gi_align, d["el_gi_align"])
+
+
+def test_operator_stages(case):
+    d, meta, m, el, order, O = case
+    assert rel(O.residual(d["apply_x"], d["apply_b"]), d["apply_r"]) < FP_TOL
+    K, dK = O.bdiag()
+    assert rel(K, d["bdiagK"]) < FP_TOL
+    assert rel(dK, d["diagK"]) < FP_TOL
+    rs, xs = O.smooth(d["apply_x"], d["apply_b"], K, dK)
+    assert rel(rs, d["smooth_r"]) < FP_TOL
+    assert rel(xs, d["smooth_x"]) < FP_TOL
+    assert rel(O.rhs(d["f"], d["g"]), d["rhs"]) < FP_TOL
+
+
+def test_p1cg_structures_exact(case):
+    d, meta, m, el, order, O = case
+    pc = O.p1cg()
+    assert np.array_equal(pc["fina"], d["fina"])
+    assert np.array_equal(pc["cola"], d["cola"])
+    assert np.array_equal(pc["whichc"], d["whichc"])
+    assert pc["ncolor"] == int(d["ncolor"])
+    # I_cf rows: the DG copies of each vertex with weight 1/#copies
+    crow, col, val = d["I_cf_crow"], d["I_cf_col"], d["I_cf_val"]
+    p1 = m.p1cg.ravel()
+    for i in range(m.cg_nonods):
+        cols = np.sort(col[crow[i]:crow[i + 1]])
+        assert np.array_equal(cols, np.nonzero(p1 == i)[0])
+        assert np.allclose(val[crow[i]:crow[i + 1]], 1.0 / cols.size, rtol=0, atol=1e-16)
+
+
+def test_sfc_hierarchy_and_vcycle(case):
+    d, meta, m, el, order, O = case
+    ctx = O.setup(order)
+    assert rel(ctx["rar"], d["RARvalues"]) < FP_TOL
+    assert ctx["nlevel"] == int(d["nlevel"])
+    assert list(ctx["sizes"]) == list(d["nodes_per_level"])
+    for lev in range(ctx["nlevel"] - 1):
+        A, dg = ctx["levels"][lev]
+        assert np.array_equal(A.indptr, d["lev%d_crow" % lev])
+        assert np.array_equal(A.indices, d["lev%d_col" % lev])
+        assert rel(A.data, d["lev%d_val" % lev]) < FP_TOL
+        assert rel(dg, d["lev%d_diag" % lev]) < FP_TOL
+    assert rel(O.mg_on_p1cg(d["mg_r"], ctx["levels"], ctx["sizes"]), d["mg_e"]) < FP_TOL
+    assert rel(O.precond(d["pc_r"], ctx), d["pc_x"]) < FP_TOL
+
+
+def test_gmres_solution(case):
+    d, meta, m, el, order, O = case
+    ctx = O.setup(order)
+    opts = meta["opts"]
+    tol = opts.get("rtol", 1e-10) * np.linalg.norm(d["rhs"])
+    x, its, hist = O.gmres(d["rhs"], ctx, tol, m=opts.get("gmres_m", 30),
+                           max_its=opts.get("gmres_its", 400))
+    assert its == int(d["its"])
+    assert rel(x, d["x_solution"]) < SOL_TOL
+    l2, linf = O.l2_error(x, d["u_exact"])
+    assert abs(l2 - float(d["l2err"])) <= 1e-10 * abs(float(d["l2err"]))
+
+
+def test_upsample_index_matches_torch():
+    torch = pytest.importorskip("torch")
+    for nf in list(range(2, 80)) + [1157, 2315, 4631, 9261, 68921, 137841]:
+        nc = (nf - 1) // 2 + 1
+        up = torch.nn.Upsample(scale_factor=nf / nc)
+        src = torch.arange(nc, dtype=torch.float64).view(1, 1, -1)
+        got = up(src).view(-1).numpy().astype(np.int64)
+        assert np.array_equal(got, upsample_index(nf, nc)), nf
