@@ -1,0 +1,383 @@
+"""Benchmark: solved DOF/s of the 3D P3 SIP-DG Poisson solve on one GB300.
+
+Workload (default): unit cube, 20^3 cells, Kuhn 6-tet split (48,000 P3
+tetrahedra, 960,000 DOFs), interior vertices jittered +-0.15h (seed 0),
+manufactured u = sin(pi x) sin(pi y) sin(pi z), Dirichlet on all faces,
+penalty eta = 90, DG->CG + SFC multigrid V(2,2) preconditioned GMRES(30)
+to ||b - A x|| <= 1e-10 ||b||, FP64.
+
+A step is one solve: right-hand-side assembly + GMRES from x0 = 0 with the
+mesh and operator resident on the device.  ``value`` is DOFs * steps / time
+of the timed steps (CUDA events on the launching stream); ``e2e`` repeats
+the measurement through DGSolver.solve() with the source on pinned host
+memory and the solution copied back each step.  Setup (mesh, operator
+blocks, colour-probe Galerkin operator, SFC levels) is timed separately.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With torchrun (N > 1) every rank solves its own replica (the solve does not
+shard); the timed region is bracketed by barriers and the max over ranks is
+used.  ``--impl reference`` times the CPU restatement of the reference's
+algorithm (oracle/) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solved DOF/s to 1e-10 rel. residual, mixed/batched vs FP64 GPU; p50/p99 latency"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+# GMRES iterations of the FP64 solve per mesh size (cells per side), as
+# measured on the GPU path; the CPU restatement runs the same algorithm.
+REFERENCE_ITS = {20: 120}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=20, help="cells per cube side")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--smooth", type=int, default=2, help="V(s,s) smoothing steps")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(args):
+    from dg_nn_public_gb300 import element, mesh, sfc
+    m = mesh.build_mesh("tet", args.n, seed=args.seed)
+    order = sfc.hilbert_sfc_order(m.cg_coords)
+    el = element.p3_element(3)
+    X = m.x_ref_in
+    f = 3 * np.pi ** 2 * np.prod([np.sin(np.pi * X[:, d]) for d in range(3)], axis=0)
+    u = np.prod([np.sin(np.pi * X[:, d]) for d in range(3)], axis=0)
+    return m, order, el, f.reshape(-1), u.reshape(-1)
+
+
+def config_block(args, m, extra=None):
+    d = {"workload": "3D P3 SIP-DG Poisson, Kuhn cube %d^3 (%d tets, %d DOFs), jitter 0.15h seed %d, "
+                     "SFC-MG V(%d,%d) + GMRES(30), rtol 1e-10, FP64"
+                     % (args.n, m.nele, m.nele * m.nloc, args.seed, args.smooth, args.smooth),
+         "nele": int(m.nele), "dofs": int(m.nele * m.nloc), "eta_e": 90.0, "gmres_m": 30,
+         "smoothing": "V(%d,%d)" % (args.smooth, args.smooth),
+         "l2_policy": "inputs larger than L2: the FP64 operator blocks (%.0f MB) stream from HBM every apply"
+                      % (m.nele * 5 * 400 * 8 / 1e6)}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def apply_bytes(m):
+    """Algorithmic bytes of one stored-block FP64 apply y = A x."""
+    N = m.nloc
+    s_int = int((m.glb_bcface_type < 0).sum())
+    return m.nele * N * N * 8 + s_int * N * N * 8 + 2 * m.nele * N * 8 + s_int * 4, s_int
+
+
+class CpuBaseline:
+    """The CPU restatement of the reference's algorithm (oracle/) set up on
+    this workload; step() times one preconditioned Arnoldi step (operator
+    apply, DG->CG SFC-MG preconditioner, MGS orthogonalisation against the
+    average basis size of a GMRES(30) cycle)."""
+
+    def __init__(self, m, order, el, rar=None, smooth=2):
+        from dg_nn_public_gb300 import element
+        from oracle.dg_oracle import OracleDG
+        t0 = time.perf_counter()
+        O = OracleDG(m, el, element.drst_duv(3), pre_smooth_its=smooth, post_smooth_its=smooth)
+        K, dK = O.bdiag()
+        pc = O.p1cg()
+        rar = O.rar(pc) if rar is None else rar
+        levels, sizes, nl = O.sfc_levels(pc, rar, order)
+        self.ctx = dict(bdiagK=K, diagK=dK, pc=pc, levels=levels, sizes=sizes,
+                        sfc=np.asarray(order).reshape(-1))
+        self.t_setup = time.perf_counter() - t0
+        self.O, self.m = O, m
+        rng = np.random.default_rng(0)
+        v = rng.standard_normal(m.nele * m.nloc)
+        self.v = v / np.linalg.norm(v)
+        self.V = np.stack([self.v] * 15)
+
+    def step(self):
+        t0 = time.perf_counter()
+        w = self.O.apply_Ax(self.v)
+        z = self.O.precond(w, self.ctx).reshape(-1)
+        for i in range(self.V.shape[0]):
+            h = z @ self.V[i]
+            z = z - h * self.V[i]
+        return time.perf_counter() - t0
+
+    def solve_rate(self, t_step, its):
+        """DOF/s of a whole solve: its Arnoldi steps plus two operator
+        applies per restart cycle (an Arnoldi step costs ~8 applies)."""
+        cycles = max(1, -(-its // 30))
+        t_solve = t_step * its + cycles * 2 * (t_step / 8.0)
+        return (self.m.nele * self.m.nloc) / t_solve
+
+    @staticmethod
+    def sample_text(its):
+        return ("one preconditioned Arnoldi step of this solve (operator apply + DG->CG SFC-MG "
+                "preconditioner + orthogonalisation) on the numpy restatement of the reference, "
+                "extrapolated by the solve's %d iterations" % its)
+
+
+def cpu_baseline_sample(m, order, el, its, rar=None, smooth=2, reps=1):
+    cb = CpuBaseline(m, order, el, rar=rar, smooth=smooth)
+    t = min(cb.step() for _ in range(reps))
+    return {"value": cb.solve_rate(t, its), "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
+            "t_arnoldi_step_s": t, "t_setup_s": cb.t_setup, "sample": CpuBaseline.sample_text(its)}
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    from dg_nn_public_gb300 import _capi, build
+    if rank == 0 or ws == 1:
+        build.build()
+    if ws > 1:
+        torch.distributed.barrier()
+    from dg_nn_public_gb300.solver import DGSolver, SolverConfig
+
+    m, order, el, f, u = workload(args)
+    cfg = SolverConfig(pre_smooth_its=args.smooth, post_smooth_its=args.smooth, device=local)
+    t0 = time.perf_counter()
+    s = DGSolver(m, order, cfg, el)
+    s.build_operator()
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    dofs = m.nele * m.nloc
+    dev = "cuda:%d" % local
+    f_dev = torch.tensor(f, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        b = s.rhs(f_dev)
+        x = torch.zeros_like(b)
+        tol = 1e-10 * float(torch.linalg.norm(b))
+        its, res = s.gmres(x, b, tol)
+        return x, its, res, tol
+
+    for _ in range(args.warmup):
+        x, its, res, tol = step()
+    clocks = ClockSampler(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = _capi.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    its_list = []
+    for _ in range(args.steps):
+        x, its, res, tol = step()
+        its_list.append(its)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    launches = _capi.launch_count() - l0
+    clk = clocks.stop()
+    t_ms = ev0.elapsed_time(ev1)
+    tmax = torch.tensor([t_ms], device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+    t_ms = float(tmax.item())
+    value = ws * dofs * args.steps / (t_ms / 1e3)
+
+    # accuracy of the last solve (independent FP64 residual + manufactured error)
+    b = s.rhs(f_dev)
+    rel_res = float(torch.linalg.norm(s.residual(x, b)) / torch.linalg.norm(b))
+    err_inf = float(np.abs(x.cpu().numpy() - u).max())
+
+    # end to end through the public solve() with pinned host buffers
+    f_host = torch.tensor(f, dtype=torch.float64).pin_memory()
+    x_host = torch.empty(dofs, dtype=torch.float64).pin_memory()
+    for _ in range(1):
+        s.solve(f_host, out=x_host)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.solve(f_host, out=x_host)
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    te = torch.tensor([t_e2e], device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
+    e2e_value = ws * dofs * args.steps / float(te.item())
+
+    # roofline of the dominant kernel: the stored-block FP64 apply, timed alone
+    xa = torch.randn(dofs, dtype=torch.float64, device=dev)
+    ya = torch.empty_like(xa)
+    for _ in range(3):
+        s.apply(xa, ya)
+    reps = 20
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        s.apply(xa, ya)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_apply = e0.elapsed_time(e1) / reps / 1e3
+    nbytes, s_int = apply_bytes(m)
+    peaks, kind = load_peaks()
+    peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
+    achieved = nbytes / t_apply / 1e9
+    flops = 2.0 * m.nloc * m.nloc * (m.nele + s_int)
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "apply_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as fh:
+            traffic = json.load(fh).get("bytes_per_launch")
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_block(args, m, {"parallelism": "replicas" if ws > 1 else "single GPU",
+                                         "precision": "fp64"}),
+        "its": its_list, "rel_residual": rel_res, "max_nodal_error_vs_exact": err_inf,
+        "setup_s": t_setup,
+        "e2e": {"value": e2e_value, "unit": "DOF/s", "h2d_bytes_per_step": dofs * 8,
+                "d2h_bytes_per_step": dofs * 8, "api": "DGSolver.solve (pinned host f -> x)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": kind,
+                     "kernel": "residual_kernel<20,4,8> (stored-block FP64 apply)",
+                     "bytes_per_launch": nbytes, "launch_ms": t_apply * 1e3,
+                     "fp64_tflops": flops / t_apply / 1e12},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            out["cpu_baseline"] = cpu_baseline_sample(m, order, el, int(np.median(its_list)),
+                                                      rar=s.rar_values().cpu().numpy(), smooth=args.smooth)
+        except Exception as exc:  # reported, not fatal
+            out["cpu_baseline"] = {"value": None, "error": repr(exc)}
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    m, order, el, f, u = workload(args)
+    # iteration count of this solve: the CPU restatement follows the same
+    # algorithm, which matches the GPU path iteration for iteration on every
+    # pinned case; the count for this workload is measured by the GPU arm
+    its = int(os.environ.get("DG_BENCH_ITS", "0")) or REFERENCE_ITS.get(args.n, 60)
+    cb = CpuBaseline(m, order, el, smooth=args.smooth)
+    ts = []
+    for k in range(args.warmup + args.steps):
+        t = cb.step()
+        if k >= args.warmup:
+            ts.append(t)
+    v = cb.solve_rate(float(np.median(ts)), its)
+    dofs = m.nele * m.nloc
+    out = {"metric": METRIC, "impl": "reference", "value": v, "unit": "DOF/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dofs / v * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": config_block(args, m, {"precision": "fp64"}),
+           "cpu_baseline": {"value": v, "unit": "DOF/s", "cores": os.cpu_count(), "kind": "port",
+                            "sample": CpuBaseline.sample_text(its), "setup_s": cb.t_setup},
+           "e2e": {"value": v, "unit": "DOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

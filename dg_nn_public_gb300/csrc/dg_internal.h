@@ -1,0 +1,37 @@
+// Internal declarations shared by the translation units of libdgsip.
+#pragma once
+#include <array>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/dgsip.h"
+
+namespace dg {
+
+int set_thread_error(int code, const std::string& msg);
+extern thread_local std::string g_thread_error;
+
+struct SfcHierarchy {
+  int32_t nlevel = 0;
+  std::vector<int64_t> sizes;     // nodes per level
+  std::vector<int64_t> start;     // stacked first node of each level (nlevel+1)
+  std::vector<int64_t> row_ptr;   // stacked CSR rows (total+1), into col/val
+  std::vector<int64_t> col;       // level-local column index
+  std::vector<double> val;
+};
+
+int p1cg_sparsity(int64_t nele, int ncorner, const int64_t* p1cg, int64_t n,
+                  std::vector<int64_t>& fina, std::vector<int64_t>& cola);
+int color2(int64_t n, const int64_t* fina, const int64_t* cola, std::vector<int64_t>& whichc,
+           int32_t& ncolor);
+void sparse_idx_for_color(int64_t n, const int64_t* fina, const int64_t* cola,
+                          const std::vector<int64_t>& whichc, int32_t ncolor,
+                          std::vector<std::vector<int64_t>>& spidx,
+                          std::vector<std::vector<int64_t>>& colidx);
+int32_t nlevel_sfc(int64_t nonods);
+int sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double* a,
+               const int64_t* sfc_order, SfcHierarchy& h);
+int face_connectivity(int ndim, int64_t nele, const int64_t* corners, int64_t* nbf, int64_t* alnmt);
+
+}  // namespace dg

@@ -1,0 +1,367 @@
+// Device kernels of libdgsip (FP64 path).
+//
+// Operator storage.  The SIP-DG operator is kept as dense element blocks:
+// for element e, block 0 is the element's own block A_ee (volume term plus
+// the own-side terms of its interior and Dirichlet faces -- exactly the
+// reference's bdiagK) and block 1+f is the coupling A_{e,nb(e,f)} to the
+// face-f neighbour (zero for boundary faces).  Blocks are stored
+// column-major, blk[((e*(F+1)+b)*N + n)*N + m] = A_b(m, n), so that the
+// threads of an element (one per row m) read a column with one coalesced
+// 8*N-byte access.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dg {
+
+struct Tables {
+  const double* n;        // (N, VG)
+  const double* nlx;      // (D, N, VG)
+  const double* weight;   // (VG)
+  const double* sn;       // (F, N, SG)
+  const double* snlx;     // (F, D, N, SG)
+  const double* sweight;  // (SG)
+  const double* drst;     // (F, D, D-1)
+  const double* P;        // (N, D+1) P1 -> P3 element prolongator
+  const int* align;       // (D, SG)
+};
+
+struct BuildParams {
+  Tables T;
+  const double* x;        // (B, D, N)
+  const int* nbe;         // (B*F) neighbour element (interior faces) or -1
+  const int* nbface;      // (B*F) neighbour local face
+  const int* aln;         // (B*F)
+  const int* bct;         // (B*F)
+  const double* kappa;    // (B)
+  double* blk;            // (B, F+1, N, N)
+  double* detw;           // (B, VG) signed det * weight
+  double eta, mu;
+  int64_t B;
+  int* err;               // error word: 1 = non-positive Jacobian
+};
+
+// ---------------------------------------------------------------------------
+// small dense helpers
+template <int D>
+__device__ __forceinline__ double inv_det(const double* j, double* inv) {
+  // j[i*D+k] = d x_k / d l_i; inverse by cofactors like the reference
+  if constexpr (D == 3) {
+    double det = j[0] * (j[4] * j[8] - j[5] * j[7]) - j[1] * (j[3] * j[8] - j[5] * j[6]) +
+                 j[2] * (j[3] * j[7] - j[4] * j[6]);
+    inv[0] = (j[4] * j[8] - j[5] * j[7]) / det;
+    inv[1] = (j[2] * j[7] - j[1] * j[8]) / det;
+    inv[2] = (j[1] * j[5] - j[2] * j[4]) / det;
+    inv[3] = (j[5] * j[6] - j[3] * j[8]) / det;
+    inv[4] = (j[0] * j[8] - j[2] * j[6]) / det;
+    inv[5] = (j[2] * j[3] - j[0] * j[5]) / det;
+    inv[6] = (j[3] * j[7] - j[4] * j[6]) / det;
+    inv[7] = (j[1] * j[6] - j[0] * j[7]) / det;
+    inv[8] = (j[0] * j[4] - j[1] * j[3]) / det;
+    return det;
+  } else {
+    double det = j[0] * j[3] - j[1] * j[2];
+    inv[0] = j[3] / det;
+    inv[1] = -j[1] / det;
+    inv[2] = -j[2] / det;
+    inv[3] = j[0] / det;
+    return det;
+  }
+}
+
+// Jacobian at one point from derivative table d (D, N, npts) at column g.
+template <int D, int N>
+__device__ __forceinline__ void jacobian(const double* __restrict__ d, int npts, int g,
+                                         const double* xe, double* j) {
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      double s = 0.0;
+#pragma unroll 4
+      for (int n = 0; n < N; ++n) s += __ldg(d + (i * N + n) * npts + g) * xe[k * N + n];
+      j[i * D + k] = s;
+    }
+}
+
+// Face tangents, unit outward normal and area element at a face point.
+template <int D>
+__device__ __forceinline__ double face_normal(const double* j, const double* drst_f, double* nrm) {
+  if constexpr (D == 3) {
+    double t[2][3];
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        double s = 0.0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) s += j[i * 3 + c] * drst_f[i * 2 + k];
+        t[k][c] = s;
+      }
+    double cx = t[0][1] * t[1][2] - t[0][2] * t[1][1];
+    double cy = t[0][2] * t[1][0] - t[0][0] * t[1][2];
+    double cz = t[0][0] * t[1][1] - t[0][1] * t[1][0];
+    double sdet = sqrt(cx * cx + cy * cy + cz * cz);
+    nrm[0] = cx / sdet;
+    nrm[1] = cy / sdet;
+    nrm[2] = cz / sdet;
+    return sdet;
+  } else {
+    double t0 = j[0] * drst_f[0] + j[2] * drst_f[1];
+    double t1 = j[1] * drst_f[0] + j[3] * drst_f[1];
+    double sdet = sqrt(t0 * t0 + t1 * t1);
+    nrm[0] = t1 / sdet;
+    nrm[1] = -t0 / sdet;
+    return sdet;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stored-block assembly: one CTA per element, N*N threads.
+template <int D, int N, int F, int VG, int SG>
+struct BuildSmem {
+  double xe[D * N];
+  double xnb[F][D * N];
+  double ivj[VG][D * D];
+  double dtw[VG];
+  double nx[D][N][VG];
+  double nrm[F][SG][D];
+  double sw[F][SG];
+  double ivs[F][SG][D * D];
+  double ivsn[F][SG][D * D];
+  double gn[F][N][SG];
+  double gnb[F][N][SG];
+  double snb[F][N][SG];
+  double gam[F];
+  double kf[F];
+  int nbi[F], nbfc[F], aln[F], bct[F];
+};
+
+template <int D, int N, int F, int VG, int SG>
+__global__ void __launch_bounds__(N* N) build_blocks_kernel(BuildParams p) {
+  using S = BuildSmem<D, N, F, VG, SG>;
+  extern __shared__ double smem_raw[];
+  S& s = *reinterpret_cast<S*>(smem_raw);
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int NT = N * N;
+  const Tables& T = p.T;
+  for (int k = tid; k < D * N; k += NT) s.xe[k] = p.x[e * D * N + k];
+  if (tid < F) {
+    int64_t fi = e * F + tid;
+    s.nbi[tid] = p.nbe[fi];
+    s.nbfc[tid] = p.nbface[fi];
+    s.aln[tid] = p.aln[fi];
+    s.bct[tid] = p.bct[fi];
+  }
+  __syncthreads();
+  for (int k = tid; k < F * D * N; k += NT) {
+    int f = k / (D * N), r = k % (D * N);
+    int nb = s.nbi[f];
+    s.xnb[f][r] = nb >= 0 ? p.x[(int64_t)nb * D * N + r] : 0.0;
+  }
+  __syncthreads();
+  // volume Jacobians
+  for (int g = tid; g < VG; g += NT) {
+    double j[D * D];
+    jacobian<D, N>(T.nlx, VG, g, s.xe, j);
+    double det = inv_det<D>(j, s.ivj[g]);
+    s.dtw[g] = det * T.weight[g];
+    if (!(det > 0.0)) atomicExch(p.err, 1);
+    p.detw[e * VG + g] = det * T.weight[g];
+  }
+  // face Jacobians: own side and (interior faces) neighbour side
+  for (int k = tid; k < F * SG; k += NT) {
+    int f = k / SG, g = k % SG;
+    double j[D * D];
+    jacobian<D, N>(T.snlx + (size_t)f * D * N * SG, SG, g, s.xe, j);
+    inv_det<D>(j, s.ivs[f][g]);
+    double sdet = face_normal<D>(j, T.drst + f * D * (D - 1), s.nrm[f][g]);
+    s.sw[f][g] = sdet * T.sweight[g];
+    if (s.nbi[f] >= 0) {
+      int fn = s.nbfc[f];
+      jacobian<D, N>(T.snlx + (size_t)fn * D * N * SG, SG, g, s.xnb[f], j);
+      inv_det<D>(j, s.ivsn[f][g]);
+    }
+  }
+  __syncthreads();
+  // physical gradients at volume points
+  for (int k = tid; k < D * N * VG; k += NT) {
+    int i = k / (N * VG), r = k % (N * VG), n = r / VG, g = r % VG;
+    double v = 0.0;
+#pragma unroll
+    for (int jj = 0; jj < D; ++jj) v += s.ivj[g][i * D + jj] * __ldg(T.nlx + (jj * N + n) * VG + g);
+    s.nx[i][n][g] = v;
+  }
+  // grad(phi).n on the faces, own side and neighbour side at aligned points
+  for (int k = tid; k < F * N * SG; k += NT) {
+    int f = k / (N * SG), r = k % (N * SG), n = r / SG, g = r % SG;
+    const double* snlx_f = T.snlx + (size_t)f * D * N * SG;
+    double v = 0.0;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      double gi = 0.0;
+#pragma unroll
+      for (int jj = 0; jj < D; ++jj) gi += s.ivs[f][g][i * D + jj] * __ldg(snlx_f + (jj * N + n) * SG + g);
+      v += gi * s.nrm[f][g][i];
+    }
+    s.gn[f][n][g] = v;
+    double vb = 0.0, sb = 0.0;
+    if (s.nbi[f] >= 0) {
+      int fn = s.nbfc[f];
+      int a = T.align[s.aln[f] * SG + g];
+      const double* snlx_n = T.snlx + (size_t)fn * D * N * SG;
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        double gi = 0.0;
+#pragma unroll
+        for (int jj = 0; jj < D; ++jj) gi += s.ivsn[f][a][i * D + jj] * __ldg(snlx_n + (jj * N + n) * SG + a);
+        vb += gi * s.nrm[f][g][i];
+      }
+      sb = __ldg(T.sn + ((size_t)fn * N + n) * SG + a);
+    }
+    s.gnb[f][n][g] = vb;
+    s.snb[f][n][g] = sb;
+  }
+  if (tid < F) {
+    int f = tid;
+    double h = 0.0;
+    for (int g = 0; g < SG; ++g) h += s.sw[f][g];
+    if (D == 3) h = sqrt(h);
+    s.gam[f] = p.eta / h;
+    double ke = p.kappa[e];
+    if (s.bct[f] < 0) {
+      int nb = s.nbi[f];
+      s.kf[f] = p.mu * 0.5 * (ke + (nb >= 0 ? p.kappa[nb] : ke));
+    } else if (s.bct[f] == 0) {
+      s.kf[f] = p.mu * ke;
+    } else {
+      s.kf[f] = 0.0;
+    }
+  }
+  __syncthreads();
+  // entries: thread -> (m, n), m fastest
+  const int m = tid % N, n = tid / N;
+  double vol = 0.0;
+#pragma unroll 4
+  for (int g = 0; g < VG; ++g) {
+    double dd = 0.0;
+#pragma unroll
+    for (int i = 0; i < D; ++i) dd += s.nx[i][m][g] * s.nx[i][n][g];
+    vol += s.dtw[g] * dd;
+  }
+  double diag = p.mu * p.kappa[e] * vol;
+  double* out = p.blk + (size_t)e * (F + 1) * N * N;
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    const double* snf = T.sn + (size_t)f * N * SG;
+    double off = 0.0;
+    if (s.kf[f] != 0.0) {
+      const bool interior = s.bct[f] < 0;
+      const double a = interior ? 0.5 : 1.0;
+      double cs = 0.0, sc = 0.0, ss = 0.0, cnb = 0.0, snbv = 0.0, ssnb = 0.0;
+      for (int g = 0; g < SG; ++g) {
+        double w = s.sw[f][g];
+        double snm = __ldg(snf + m * SG + g), snn = __ldg(snf + n * SG + g);
+        cs += snm * s.gn[f][n][g] * w;
+        sc += s.gn[f][m][g] * snn * w;
+        ss += snm * snn * w;
+        if (interior) {
+          cnb += snm * s.gnb[f][n][g] * w;
+          snbv += s.gn[f][m][g] * s.snb[f][n][g] * w;
+          ssnb += snm * s.snb[f][n][g] * w;
+        }
+      }
+      diag += s.kf[f] * (-a * cs - a * sc + s.gam[f] * ss);
+      if (interior) off = s.kf[f] * (-0.5 * cnb + 0.5 * snbv - s.gam[f] * ssnb);
+    }
+    out[(size_t)(1 + f) * N * N + n * N + m] = off;
+  }
+  out[n * N + m] = diag;
+}
+
+// ---------------------------------------------------------------------------
+// Residual / smoother: EPB elements per CTA, one thread per (element, row).
+//   res = b - A x            (b = 0 when null; x = 0 when ZEROX)
+//   r  <- sgn * res          (when r != null)
+//   SMOOTH: c = 3 Jacobi sweeps on A_ee c = res; x_out = x + w c
+enum { RF_ZEROX = 1, RF_SMOOTH = 2, RF_NEG = 4 };
+
+template <int N, int F, int EPB>
+__global__ void __launch_bounds__(EPB* N) residual_kernel(const double* __restrict__ blk,
+                                                          const int* __restrict__ nbe,
+                                                          const double* __restrict__ x,
+                                                          const double* __restrict__ b,
+                                                          double* __restrict__ r,
+                                                          double* __restrict__ x_out, int64_t B,
+                                                          double w, int flags) {
+  __shared__ double xs[EPB][F + 1][N];
+  __shared__ double cs[EPB][N];
+  __shared__ int nbs[EPB][F];
+  const int le = threadIdx.x / N, m = threadIdx.x % N;
+  const int64_t e = (int64_t)blockIdx.x * EPB + le;
+  const bool valid = e < B;
+  const bool zerox = flags & RF_ZEROX;
+  if (valid && m < F) nbs[le][m] = nbe[e * F + m];
+  __syncthreads();
+  if (valid && !zerox) {
+    xs[le][0][m] = x[e * N + m];
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      int nb = nbs[le][f];
+      xs[le][1 + f][m] = nb >= 0 ? x[(int64_t)nb * N + m] : 0.0;
+    }
+  }
+  __syncthreads();
+  double acc = 0.0;
+  double aee[N];
+  const double* A = blk + (size_t)e * (F + 1) * N * N;
+  const bool smooth = flags & RF_SMOOTH;
+  if (valid) {
+    if (!zerox || smooth) {
+#pragma unroll
+      for (int n = 0; n < N; ++n) aee[n] = A[n * N + m];
+    }
+    if (!zerox) {
+#pragma unroll
+      for (int n = 0; n < N; ++n) acc += aee[n] * xs[le][0][n];
+#pragma unroll
+      for (int f = 0; f < F; ++f) {
+        if (nbs[le][f] >= 0) {
+          const double* Af = A + (size_t)(1 + f) * N * N;
+#pragma unroll
+          for (int n = 0; n < N; ++n) acc += Af[n * N + m] * xs[le][1 + f][n];
+        }
+      }
+    }
+  }
+  double res = 0.0;
+  if (valid) {
+    res = (b ? b[e * N + m] : 0.0) - acc;
+    if (r) r[e * N + m] = (flags & RF_NEG) ? -res : res;
+  }
+  if (smooth) {
+    // three point-Jacobi sweeps on the element block (volume_mf_diff.py:474-480)
+    double dgm = valid ? aee[0] : 1.0;
+#pragma unroll
+    for (int n = 0; n < N; ++n)
+      if (n == m) dgm = aee[n];
+    double c = 0.0;
+    cs[le][m] = 0.0;
+    for (int it = 0; it < 3; ++it) {
+      __syncthreads();
+      double s = 0.0;
+      if (valid) {
+#pragma unroll
+        for (int n = 0; n < N; ++n) s += aee[n] * cs[le][n];
+      }
+      double cn = c + w * (res - s) / dgm;
+      __syncthreads();
+      cs[le][m] = cn;
+      c = cn;
+    }
+    if (valid) x_out[e * N + m] = (zerox ? 0.0 : xs[le][0][m]) + w * c;
+  }
+}
+
+}  // namespace dg

@@ -1,0 +1,337 @@
+// Device kernels of libdgsip, part 2: right-hand side, DG<->CG transfers,
+// SFC-level multigrid and the Krylov vector kernels (FP64).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dg_kernels.cuh"
+
+namespace dg {
+
+// ---------------------------------------------------------------------------
+// boundary-face geometry for the right-hand side (Dirichlet / Neumann faces)
+struct BFaceParams {
+  Tables T;
+  const double* x;       // (B, D, N)
+  const int* elem;       // (nbf) element of each boundary face
+  const int* face;       // (nbf) local face index
+  double* sw;            // (nbf, SG) sdet * sweight
+  double* gn;            // (nbf, N, SG) grad(phi).n
+  double* gam;           // (nbf) eta / h
+  double eta;
+  int nbf;
+};
+
+template <int D, int N, int F, int SG>
+__global__ void bface_geom_kernel(BFaceParams p) {
+  const int k = blockIdx.x;       // boundary face
+  const int tid = threadIdx.x;
+  __shared__ double xe[D * N];
+  __shared__ double ivs[SG][D * D];
+  __shared__ double nrm[SG][D];
+  __shared__ double swl[SG];
+  const int e = p.elem[k], f = p.face[k];
+  for (int i = tid; i < D * N; i += blockDim.x) xe[i] = p.x[(int64_t)e * D * N + i];
+  __syncthreads();
+  const double* snlx_f = p.T.snlx + (size_t)f * D * N * SG;
+  for (int g = tid; g < SG; g += blockDim.x) {
+    double j[D * D];
+    jacobian<D, N>(snlx_f, SG, g, xe, j);
+    inv_det<D>(j, ivs[g]);
+    double sdet = face_normal<D>(j, p.T.drst + f * D * (D - 1), nrm[g]);
+    swl[g] = sdet * p.T.sweight[g];
+    p.sw[(int64_t)k * SG + g] = swl[g];
+  }
+  __syncthreads();
+  for (int i = tid; i < N * SG; i += blockDim.x) {
+    int n = i / SG, g = i % SG;
+    double v = 0.0;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double gi = 0.0;
+#pragma unroll
+      for (int b = 0; b < D; ++b) gi += ivs[g][a * D + b] * snlx_f[(b * N + n) * SG + g];
+      v += gi * nrm[g][a];
+    }
+    p.gn[((int64_t)k * N + n) * SG + g] = v;
+  }
+  if (tid == 0) {
+    double h = 0.0;
+    for (int g = 0; g < SG; ++g) h += swl[g];
+    if (D == 3) h = sqrt(h);
+    p.gam[k] = p.eta / h;
+  }
+}
+
+// b[e] = M_e f[e] (consistent mass, z06/volume_mf_diff.py:195-239)
+template <int N, int VG, int EPB>
+__global__ void rhs_mass_kernel(const double* __restrict__ nt, const double* __restrict__ detw,
+                                const double* __restrict__ f, double* __restrict__ b, int64_t B) {
+  __shared__ double fq[EPB][VG];
+  __shared__ double fs[EPB][N];
+  const int le = threadIdx.x / N, m = threadIdx.x % N;
+  const int64_t e = (int64_t)blockIdx.x * EPB + le;
+  const bool valid = e < B;
+  if (valid) fs[le][m] = f[e * N + m];
+  __syncthreads();
+  for (int g = m; g < VG; g += N) {
+    double s = 0.0;
+    if (valid)
+      for (int n = 0; n < N; ++n) s += nt[n * VG + g] * fs[le][n];
+    fq[le][g] = valid ? s * detw[e * VG + g] : 0.0;
+  }
+  __syncthreads();
+  if (!valid) return;
+  double acc = 0.0;
+  for (int g = 0; g < VG; ++g) acc += nt[m * VG + g] * fq[le][g];
+  b[e * N + m] = acc;
+}
+
+// Dirichlet lifting (mode 0) or Neumann flux (mode 1) of the boundary faces
+// with local face index fsel (z06/volume_mf_diff.py:242-359).  Faces of one
+// local index never share an element, so the updates do not collide.
+template <int N, int SG>
+__global__ void rhs_bface_kernel(const double* __restrict__ sn_tab, const int* __restrict__ elem,
+                                 const int* __restrict__ face, const int* __restrict__ type,
+                                 const double* __restrict__ sw, const double* __restrict__ gn,
+                                 const double* __restrict__ gam, const double* __restrict__ kappa,
+                                 const double* __restrict__ g, double* __restrict__ b, int nbf,
+                                 int fsel, int mode, double mu) {
+  const int k = blockIdx.x * (blockDim.x / N) + threadIdx.x / N;
+  const int m = threadIdx.x % N;
+  if (k >= nbf) return;
+  const int f = face[k];
+  if (f != fsel || type[k] != mode) return;
+  const int e = elem[k];
+  const double* snf = sn_tab + (size_t)f * N * SG;
+  double acc = 0.0;
+  for (int q = 0; q < SG; ++q) {
+    double gq = 0.0;
+    for (int n = 0; n < N; ++n) gq += snf[n * SG + q] * g[(int64_t)e * N + n];
+    double w = sw[(int64_t)k * SG + q];
+    if (mode == 0)
+      acc += (-gn[((int64_t)k * N + m) * SG + q] + gam[k] * snf[m * SG + q]) * gq * w;
+    else
+      acc += snf[m * SG + q] * gq * w;
+  }
+  if (mode == 0) acc *= mu * kappa[e];
+  b[(int64_t)e * N + m] += acc;
+}
+
+// ---------------------------------------------------------------------------
+// DG <-> CG P1 transfers (z06/volume_mf_diff.py:1961-1966, 2010-2013;
+// multigrid_linearelastic.py:286-297; sparsity.py:125-165)
+
+// out[pos(i)] = sum over DG copies (e, c) of vertex i of w_ec * sum_n P[n][c] r[e][n]
+template <int N, int NC>
+__global__ void restrict_cg_kernel(const double* __restrict__ r, const double* __restrict__ P,
+                                   const int* __restrict__ gptr, const int* __restrict__ gent,
+                                   const double* __restrict__ wdg, const int* __restrict__ pos,
+                                   double* __restrict__ out, int ncg) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncg) return;
+  double acc = 0.0;
+  for (int k = gptr[i]; k < gptr[i + 1]; ++k) {
+    const int ent = gent[k];
+    const int64_t e = ent / NC;
+    const int c = ent % NC;
+    double v = 0.0;
+#pragma unroll
+    for (int n = 0; n < N; ++n) v += P[n * NC + c] * r[e * N + n];
+    acc += wdg[ent] * v;
+  }
+  out[pos ? pos[i] : i] = acc;
+}
+
+// x[e][n] (+)= sum_c P[n][c] * w_ec * ecg[idx(p1cg[e][c])]; with whichc set,
+// ecg is the indicator of colour `color` (colour-probe prolongation).
+template <int N, int NC>
+__global__ void prolong_cg_kernel(double* __restrict__ x, const double* __restrict__ ecg,
+                                  const int* __restrict__ pos, const int* __restrict__ p1cg,
+                                  const double* __restrict__ wdg, const double* __restrict__ P,
+                                  const int* __restrict__ whichc, int color, int64_t B, int add) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * N) return;
+  const int64_t e = t / N;
+  const int n = t % N;
+  double v = 0.0;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const int vtx = p1cg[e * NC + c];
+    double ev;
+    if (whichc)
+      ev = whichc[vtx] == color ? 1.0 : 0.0;
+    else
+      ev = ecg[pos ? pos[vtx] : vtx];
+    v += P[n * NC + c] * (wdg[e * NC + c] * ev);
+  }
+  x[t] = add ? x[t] + v : v;
+}
+
+// value[spidx[k]] += rarm[colidx[k]] for the probe entries of one colour
+__global__ void rar_scatter_kernel(double* __restrict__ value, const double* __restrict__ rarm,
+                                   const int* __restrict__ spidx, const int* __restrict__ colidx,
+                                   int cnt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < cnt) value[spidx[k]] += rarm[colidx[k]];
+}
+
+// ---------------------------------------------------------------------------
+// SFC levels (multigrid_linearelastic.py:25-172)
+
+// rr = b - A e_in;  e_out = e_in + w * rr / diag   (mg_smooth_one_level)
+__global__ void lev_jacobi_kernel(const int* __restrict__ rowptr, const int* __restrict__ col,
+                                  const double* __restrict__ val, const double* __restrict__ diag,
+                                  const double* __restrict__ e_in, const double* __restrict__ b,
+                                  double* __restrict__ e_out, double* __restrict__ rr_out, int n,
+                                  double w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += val[k] * e_in[col[k]];
+  const double rr = b[i] - s;
+  e_out[i] = e_in[i] + rr / diag[i] * w;
+  if (rr_out) rr_out[i] = rr;
+}
+
+// pair sums with a zero pad (F.pad + Conv1d([1, 1], stride 2), :147-153)
+__global__ void lev_restrict_kernel(const double* __restrict__ rr, const double* __restrict__ e,
+                                    double* __restrict__ r_next, double* __restrict__ e_next,
+                                    int n, int nn) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nn) return;
+  const int a = 2 * i, b = 2 * i + 1;
+  r_next[i] = rr[a] + (b < n ? rr[b] : 0.0);
+  e_next[i] = e[a] + (b < n ? e[b] : 0.0);
+}
+
+// e_l[i] += e_next[up[i]]  (nn.Upsample nearest, :163-164)
+__global__ void lev_prolong_kernel(double* __restrict__ e, const double* __restrict__ e_next,
+                                   const int* __restrict__ up, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) e[i] += e_next[up[i]];
+}
+
+// coarsest level: one node, e = r / a (scipy spsolve on a 1x1 system, :157-160)
+__global__ void lev_coarse_kernel(const double* __restrict__ val, const double* __restrict__ r,
+                                  double* __restrict__ e) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) e[0] = r[0] / val[0];
+}
+
+// ---------------------------------------------------------------------------
+// Krylov vector kernels (deterministic fixed-grid reductions)
+constexpr int KMAXV = 32;     // maximum number of basis vectors in one pass
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// partial[blk][i] = sum over this block's slice of V[i] . z   (i < nv)
+template <int TB>
+__global__ void __launch_bounds__(TB) mdot_kernel(const double* __restrict__ V, int64_t ld, int nv,
+                                                  const double* __restrict__ z, int64_t n,
+                                                  double* __restrict__ partial) {
+  __shared__ double red[TB / 32][KMAXV];
+  double acc[KMAXV];
+#pragma unroll
+  for (int i = 0; i < KMAXV; ++i) acc[i] = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x; k < n; k += (int64_t)gridDim.x * TB) {
+    const double zk = z[k];
+#pragma unroll
+    for (int i = 0; i < KMAXV; ++i)
+      if (i < nv) acc[i] += V[i * ld + k] * zk;
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < KMAXV; ++i) {
+    if (i < nv) {
+      double v = warp_sum(acc[i]);
+      if (lane == 0) red[wid][i] = v;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nv; i += TB) {
+    double s = 0.0;
+    for (int w = 0; w < TB / 32; ++w) s += red[w][i];
+    partial[(int64_t)blockIdx.x * KMAXV + i] = s;
+  }
+}
+
+// z -= sum_i V[i] h[i]; then (mode 1) partial of V[i] . z_new, (mode 2)
+// partial of z_new . z_new, (mode 0) nothing
+template <int TB>
+__global__ void __launch_bounds__(TB) update_kernel(const double* __restrict__ V, int64_t ld, int nv,
+                                                    const double* __restrict__ h,
+                                                    double* __restrict__ z, int64_t n,
+                                                    double* __restrict__ partial, int mode) {
+  __shared__ double hs[KMAXV];
+  __shared__ double red[TB / 32][KMAXV];
+  for (int i = threadIdx.x; i < nv; i += TB) hs[i] = h[i];
+  __syncthreads();
+  double acc[KMAXV];
+#pragma unroll
+  for (int i = 0; i < KMAXV; ++i) acc[i] = 0.0;
+  for (int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x; k < n; k += (int64_t)gridDim.x * TB) {
+    double zk = z[k];
+#pragma unroll
+    for (int i = 0; i < KMAXV; ++i)
+      if (i < nv) zk -= V[i * ld + k] * hs[i];
+    z[k] = zk;
+    if (mode == 1) {
+#pragma unroll
+      for (int i = 0; i < KMAXV; ++i)
+        if (i < nv) acc[i] += V[i * ld + k] * zk;
+    } else if (mode == 2) {
+      acc[0] += zk * zk;
+    }
+  }
+  if (mode == 0) return;
+  const int nr = mode == 1 ? nv : 1;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < KMAXV; ++i) {
+    if (i < nr) {
+      double v = warp_sum(acc[i]);
+      if (lane == 0) red[wid][i] = v;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nr; i += TB) {
+    double s = 0.0;
+    for (int w = 0; w < TB / 32; ++w) s += red[w][i];
+    partial[(int64_t)blockIdx.x * KMAXV + i] = s;
+  }
+}
+
+// out[i] = (accumulate ? out[i] : 0) + sum_blk partial[blk][i]; optional sqrt
+__global__ void reduce_partial_kernel(const double* __restrict__ partial, int nblk, int nv,
+                                      double* __restrict__ out, int accumulate, int take_sqrt) {
+  const int i = threadIdx.x;
+  if (i >= nv) return;
+  double s = 0.0;
+  for (int b = 0; b < nblk; ++b) s += partial[(int64_t)b * KMAXV + i];
+  if (take_sqrt) s = sqrt(s);
+  out[i] = accumulate ? out[i] + s : s;
+}
+
+// v = z / (*den)
+__global__ void scale_kernel(const double* __restrict__ z, const double* __restrict__ den,
+                             double* __restrict__ v, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const double d = *den;
+  if (k < n) v[k] = z[k] / d;
+}
+
+// x += sum_i V[i] y[i]
+__global__ void combine_kernel(const double* __restrict__ V, int64_t ld, int nv,
+                               const double* __restrict__ y, double* __restrict__ x, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  double s = 0.0;
+  for (int i = 0; i < nv; ++i) s += V[i * ld + k] * y[i];
+  x[k] += s;
+}
+
+}  // namespace dg

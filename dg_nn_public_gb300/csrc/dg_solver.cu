@@ -1,0 +1,884 @@
+// libdgsip: context, operator assembly, preconditioner and GMRES drivers.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "dg_internal.h"
+#include "dg_kernels.cuh"
+#include "dg_kernels2.cuh"
+
+using namespace dg;
+
+namespace {
+
+constexpr int RED_TB = 256;
+std::atomic<long long> g_launches{0};   // kernels launched by this library
+inline void bump(long long k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+struct DevLevel {
+  int n = 0;
+  int* rowptr = nullptr;
+  int* col = nullptr;
+  double* val = nullptr;
+  double* diag = nullptr;
+  int* up = nullptr;        // for levels below the top: index into the next level
+  double* e = nullptr;      // error
+  double* e2 = nullptr;     // ping-pong buffer
+  double* r = nullptr;      // right-hand side on this level
+  double* rr = nullptr;     // residual scratch
+};
+
+}  // namespace
+
+struct dg_ctx {
+  int dev = 0;
+  int D = 0, N = 0, F = 0, NC = 0, VG = 0, SG = 0;
+  int64_t B = 0, nonods = 0, ncg = 0;
+  dg_config cfg{};
+  std::string err;
+  int nsm = 0;
+  // host copies
+  std::vector<int64_t> p1cg, sfc;      // (B*NC), (ncg) 1-based
+  std::vector<double> kappa;
+  std::vector<int> bf_elem, bf_face, bf_type;
+  // device allocations (released in dg_destroy)
+  std::vector<void*> allocs;
+  double* d_x = nullptr;
+  int *d_nbe = nullptr, *d_nbface = nullptr, *d_aln = nullptr, *d_bct = nullptr;
+  double* d_kappa = nullptr;
+  Tables T{};
+  double* d_blk = nullptr;
+  double* d_detw = nullptr;
+  int* d_err = nullptr;
+  // boundary faces for the right-hand side
+  int nbf = 0;
+  int *d_bf_elem = nullptr, *d_bf_face = nullptr, *d_bf_type = nullptr;
+  double *d_bf_sw = nullptr, *d_bf_gn = nullptr, *d_bf_gam = nullptr;
+  // P1CG
+  std::vector<int64_t> fina, cola, whichc;
+  int32_t ncolor = 0;
+  std::vector<std::vector<int64_t>> spidx, colidx;
+  int *d_p1cg = nullptr, *d_gptr = nullptr, *d_gent = nullptr, *d_pos = nullptr, *d_whichc = nullptr;
+  double* d_wdg = nullptr;
+  int *d_spidx = nullptr, *d_colidx = nullptr;
+  std::vector<int64_t> sp_off;
+  double* d_rar = nullptr;
+  std::vector<double> rar_host;
+  // SFC levels
+  std::vector<DevLevel> lev;
+  // scratch
+  double *d_t1 = nullptr, *d_t2 = nullptr, *d_t3 = nullptr, *d_t4 = nullptr, *d_t5 = nullptr;
+  double *d_cg1 = nullptr, *d_cg2 = nullptr;
+  // Krylov
+  double* d_V = nullptr;
+  int vcap = 0;
+  double *d_part = nullptr, *d_h1 = nullptr, *d_h2 = nullptr, *d_H = nullptr, *d_y = nullptr,
+         *d_scal = nullptr;
+  int nred = 0;
+  bool built = false;
+};
+
+namespace {
+
+int fail(dg_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  set_thread_error(code, msg);
+  return code;
+}
+
+#define CK(ctx, call)                                                                    \
+  do {                                                                                   \
+    cudaError_t _e = (call);                                                             \
+    if (_e != cudaSuccess)                                                               \
+      return fail((ctx), DG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+#define CKL(ctx) CK(ctx, cudaGetLastError())
+
+template <typename T>
+int dalloc(dg_ctx* c, T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) return fail(c, DG_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  c->allocs.push_back((void*)*p);
+  return DG_OK;
+}
+
+template <typename T>
+int upload(dg_ctx* c, T** p, const T* src, size_t count) {
+  int rc = dalloc(c, p, count);
+  if (rc) return rc;
+  if (count) CK(c, cudaMemcpy(*p, src, count * sizeof(T), cudaMemcpyHostToDevice));
+  return DG_OK;
+}
+
+template <typename T>
+int upload_vec(dg_ctx* c, T** p, const std::vector<T>& v) {
+  return upload(c, p, v.data(), v.size());
+}
+
+inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+inline unsigned nblk(int64_t n, int tb) { return (unsigned)((n + tb - 1) / tb); }
+
+// ---------------------------------------------------------------------------
+// template dispatch on the element type
+template <int D>
+struct Elem;
+template <>
+struct Elem<3> {
+  static constexpr int N = 20, F = 4, VG = 24, SG = 12, NC = 4, EPB = 8;
+};
+template <>
+struct Elem<2> {
+  static constexpr int N = 10, F = 3, VG = 12, SG = 4, NC = 3, EPB = 16;
+};
+
+template <int D>
+int launch_build(dg_ctx* c, cudaStream_t st) {
+  using E = Elem<D>;
+  using Sm = BuildSmem<D, E::N, E::F, E::VG, E::SG>;
+  BuildParams p;
+  p.T = c->T;
+  p.x = c->d_x;
+  p.nbe = c->d_nbe;
+  p.nbface = c->d_nbface;
+  p.aln = c->d_aln;
+  p.bct = c->d_bct;
+  p.kappa = c->d_kappa;
+  p.blk = c->d_blk;
+  p.detw = c->d_detw;
+  p.eta = c->cfg.eta_e;
+  p.mu = c->cfg.mu_f;
+  p.B = c->B;
+  p.err = c->d_err;
+  auto k = build_blocks_kernel<D, E::N, E::F, E::VG, E::SG>;
+  CK(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm)));
+  if (c->B > 0) k<<<(unsigned)c->B, E::N * E::N, sizeof(Sm), st>>>(p);
+  bump();
+  CKL(c);
+  if (c->nbf > 0) {
+    BFaceParams q;
+    q.T = c->T;
+    q.x = c->d_x;
+    q.elem = c->d_bf_elem;
+    q.face = c->d_bf_face;
+    q.sw = c->d_bf_sw;
+    q.gn = c->d_bf_gn;
+    q.gam = c->d_bf_gam;
+    q.eta = c->cfg.eta_e;
+    q.nbf = c->nbf;
+    bface_geom_kernel<D, E::N, E::F, E::SG><<<c->nbf, 64, 0, st>>>(q);
+    bump();
+    CKL(c);
+  }
+  return DG_OK;
+}
+
+template <int D>
+int launch_residual(dg_ctx* c, const double* x, const double* b, double* r, double* x_out, int flags,
+                    cudaStream_t st) {
+  using E = Elem<D>;
+  unsigned g = nblk(c->B, E::EPB);
+  if (g) residual_kernel<E::N, E::F, E::EPB><<<g, E::EPB * E::N, 0, st>>>(
+      c->d_blk, c->d_nbe, x, b, r, x_out, c->B, c->cfg.jac_wei, flags);
+  bump();
+  CKL(c);
+  return DG_OK;
+}
+
+int residual(dg_ctx* c, const double* x, const double* b, double* r, double* x_out, int flags,
+             cudaStream_t st) {
+  return c->D == 3 ? launch_residual<3>(c, x, b, r, x_out, flags, st)
+                   : launch_residual<2>(c, x, b, r, x_out, flags, st);
+}
+
+template <int D>
+int launch_restrict(dg_ctx* c, const double* r, double* out, bool sfc_order, cudaStream_t st) {
+  using E = Elem<D>;
+  restrict_cg_kernel<E::N, E::NC><<<nblk(c->ncg, 128), 128, 0, st>>>(
+      r, c->T.P, c->d_gptr, c->d_gent, c->d_wdg, sfc_order ? c->d_pos : nullptr, out, (int)c->ncg);
+  bump();
+  CKL(c);
+  return DG_OK;
+}
+
+int restrict_cg(dg_ctx* c, const double* r, double* out, bool sfc_order, cudaStream_t st) {
+  return c->D == 3 ? launch_restrict<3>(c, r, out, sfc_order, st) : launch_restrict<2>(c, r, out, sfc_order, st);
+}
+
+template <int D>
+int launch_prolong(dg_ctx* c, double* x, const double* ecg, bool sfc_order, int color, bool add,
+                   cudaStream_t st) {
+  using E = Elem<D>;
+  prolong_cg_kernel<E::N, E::NC><<<nblk(c->B * E::N, 256), 256, 0, st>>>(
+      x, ecg, sfc_order ? c->d_pos : nullptr, c->d_p1cg, c->d_wdg, c->T.P,
+      color > 0 ? c->d_whichc : nullptr, color, c->B, add ? 1 : 0);
+  bump();
+  CKL(c);
+  return DG_OK;
+}
+
+int prolong_cg(dg_ctx* c, double* x, const double* ecg, bool sfc_order, int color, bool add, cudaStream_t st) {
+  return c->D == 3 ? launch_prolong<3>(c, x, ecg, sfc_order, color, add, st)
+                   : launch_prolong<2>(c, x, ecg, sfc_order, color, add, st);
+}
+
+// One SFC V-cycle; r_sfc is level-0 input, result left in lev[0].e
+int vcycle(dg_ctx* c, const double* r_sfc, cudaStream_t st) {
+  const int nl = (int)c->lev.size();
+  const int top = nl - 1;
+  const double w = c->cfg.jac_wei;
+  const int TB = 128;
+  CK(c, cudaMemcpyAsync(c->lev[0].r, r_sfc, sizeof(double) * c->lev[0].n, cudaMemcpyDeviceToDevice, st));
+  CK(c, cudaMemsetAsync(c->lev[0].e, 0, sizeof(double) * c->lev[0].n, st));
+  for (int l = 0; l < top; ++l) {
+    DevLevel& L = c->lev[l];
+    for (int it = 0; it < c->cfg.pre_smooth_its; ++it) {
+      lev_jacobi_kernel<<<nblk(L.n, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r, L.e2,
+                                                       nullptr, L.n, w); bump();
+      std::swap(L.e, L.e2);
+    }
+    // the residual-forming call also updates e in place (reference quirk)
+    lev_jacobi_kernel<<<nblk(L.n, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r, L.e2, L.rr,
+                                                     L.n, w); bump();
+    std::swap(L.e, L.e2);
+    DevLevel& Nx = c->lev[l + 1];
+    lev_restrict_kernel<<<nblk(Nx.n, TB), TB, 0, st>>>(L.rr, L.e, Nx.r, Nx.e, L.n, Nx.n); bump();
+  }
+  {
+    DevLevel& L = c->lev[top];
+    if (L.n != 1) return fail(c, DG_ERR_STATE, "coarsest SFC level must hold one node");
+    lev_coarse_kernel<<<1, 32, 0, st>>>(L.val, L.r, L.e); bump();
+  }
+  for (int l = top - 1; l >= 0; --l) {
+    DevLevel& L = c->lev[l];
+    lev_prolong_kernel<<<nblk(L.n, TB), TB, 0, st>>>(L.e, c->lev[l + 1].e, L.up, L.n); bump();
+    for (int it = 0; it < c->cfg.post_smooth_its; ++it) {
+      lev_jacobi_kernel<<<nblk(L.n, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r, L.e2,
+                                                       nullptr, L.n, w); bump();
+      std::swap(L.e, L.e2);
+    }
+  }
+  CKL(c);
+  return DG_OK;
+}
+
+// z = M^{-1} r.  Scratch: t3, t4 (smoother iterates), t5 (residual); z and r
+// must be distinct and not among those.
+int precond(dg_ctx* c, const double* r, double* z, cudaStream_t st) {
+  int rc;
+  const int nsm = c->cfg.pre_smooth_its;
+  double* cur = c->d_t3;
+  double* other = c->d_t4;
+  // pre-smoothing from x = 0: the first sweep needs no operator apply
+  if (nsm > 0) {
+    if ((rc = residual(c, nullptr, r, nullptr, cur, RF_ZEROX | RF_SMOOTH, st))) return rc;
+    for (int it = 1; it < nsm; ++it) {
+      if ((rc = residual(c, cur, r, nullptr, other, RF_SMOOTH, st))) return rc;
+      std::swap(cur, other);
+    }
+  } else {
+    CK(c, cudaMemsetAsync(cur, 0, sizeof(double) * c->nonods, st));
+  }
+  // residual, restriction to P1CG in curve order, V-cycle, prolongation
+  if ((rc = residual(c, cur, r, c->d_t5, nullptr, 0, st))) return rc;
+  if ((rc = restrict_cg(c, c->d_t5, c->d_cg1, true, st))) return rc;
+  if ((rc = vcycle(c, c->d_cg1, st))) return rc;
+  if ((rc = prolong_cg(c, cur, c->lev[0].e, true, 0, true, st))) return rc;
+  // post-smoothing (the reference repeats pre_smooth_its times, :2021)
+  for (int it = 0; it < nsm; ++it) {
+    double* out = (it == nsm - 1) ? z : other;
+    if ((rc = residual(c, cur, r, nullptr, out, RF_SMOOTH, st))) return rc;
+    other = cur;
+    cur = out;
+  }
+  if (nsm == 0) CK(c, cudaMemcpyAsync(z, cur, sizeof(double) * c->nonods, cudaMemcpyDeviceToDevice, st));
+  return DG_OK;
+}
+
+int ensure_krylov(dg_ctx* c, int m) {
+  if (c->vcap >= m + 1) return DG_OK;
+  int rc;
+  if ((rc = dalloc(c, &c->d_V, (size_t)(m + 1) * c->nonods))) return rc;
+  if ((rc = dalloc(c, &c->d_H, (size_t)(m + 1) * m))) return rc;
+  c->vcap = m + 1;
+  return DG_OK;
+}
+
+// h[0..nv) = V[0..nv)^T z  (chunks of KMAXV)
+int mdot(dg_ctx* c, const double* V, int nv, const double* z, double* h, int accumulate, cudaStream_t st) {
+  for (int off = 0; off < nv; off += KMAXV) {
+    int cnt = std::min(KMAXV, nv - off);
+    mdot_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(V + (size_t)off * c->nonods, c->nonods, cnt, z, c->nonods,
+                                                    c->d_part); bump();
+    reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_part, c->nred, cnt, h + off, accumulate, 0); bump();
+  }
+  CKL(c);
+  return DG_OK;
+}
+
+// Norm of z into *out (device)
+int norm2(dg_ctx* c, const double* z, double* out, cudaStream_t st) {
+  mdot_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(z, c->nonods, 1, z, c->nonods, c->d_part); bump();
+  reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_part, c->nred, 1, out, 0, 1); bump();
+  CKL(c);
+  return DG_OK;
+}
+
+// CGS2 step: z <- z - V h with h = V^T z twice; H column j gets h1 + h2 and
+// H[j+1][j] = ||z||; V[j+1] = z / ||z||.
+int cgs2(dg_ctx* c, int j, double* z, int m, cudaStream_t st) {
+  const int nv = j + 1;
+  double* Hc = c->d_H + (size_t)j * (m + 1);     // column-major (m+1) x m
+  int rc;
+  if ((rc = mdot(c, c->d_V, nv, z, c->d_h1, 0, st))) return rc;
+  if (nv <= KMAXV) {
+    update_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(c->d_V, c->nonods, nv, c->d_h1, z, c->nonods, c->d_part, 1); bump();
+    reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_part, c->nred, nv, c->d_h2, 0, 0); bump();
+    update_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(c->d_V, c->nonods, nv, c->d_h2, z, c->nonods, c->d_part, 2); bump();
+    reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_part, c->nred, 1, Hc + nv, 0, 1); bump();
+  } else {
+    for (int off = 0; off < nv; off += KMAXV) {
+      int cnt = std::min(KMAXV, nv - off);
+      update_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(c->d_V + (size_t)off * c->nonods, c->nonods, cnt,
+                                                        c->d_h1 + off, z, c->nonods, c->d_part, 0); bump();
+    }
+    if ((rc = mdot(c, c->d_V, nv, z, c->d_h2, 0, st))) return rc;
+    for (int off = 0; off < nv; off += KMAXV) {
+      int cnt = std::min(KMAXV, nv - off);
+      update_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(c->d_V + (size_t)off * c->nonods, c->nonods, cnt,
+                                                        c->d_h2 + off, z, c->nonods, c->d_part, 0); bump();
+    }
+    if ((rc = norm2(c, z, Hc + nv, st))) return rc;
+  }
+  // H[0..nv) = h1 + h2
+  CK(c, cudaMemcpyAsync(Hc, c->d_h1, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st));
+  reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_h2, 1, std::min(nv, KMAXV), Hc, 1, 0); bump();
+  if (nv > KMAXV) {
+    for (int off = KMAXV; off < nv; off += KMAXV) {
+      int cnt = std::min(KMAXV, nv - off);
+      reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_h2 + off, 1, cnt, Hc + off, 1, 0); bump();
+    }
+  }
+  scale_kernel<<<nblk(c->nonods, 256), 256, 0, st>>>(z, Hc + nv, c->d_V + (size_t)nv * c->nonods, c->nonods); bump();
+  CKL(c);
+  return DG_OK;
+}
+
+// least squares min || beta e1 - H y || by Givens rotations (host, FP64)
+bool solve_hessenberg(const std::vector<double>& Hcm, int m, double beta, std::vector<double>& y) {
+  // Hcm column-major (m+1) x m
+  std::vector<double> R((size_t)(m + 1) * m);
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i <= m; ++i) R[(size_t)i * m + j] = Hcm[(size_t)j * (m + 1) + i];
+  std::vector<double> g(m + 1, 0.0);
+  g[0] = beta;
+  for (int j = 0; j < m; ++j) {
+    double a = R[(size_t)j * m + j], b = R[(size_t)(j + 1) * m + j];
+    double r = std::hypot(a, b);
+    if (r == 0.0) return false;
+    double cs = a / r, sn = b / r;
+    for (int k = j; k < m; ++k) {
+      double t1 = R[(size_t)j * m + k], t2 = R[(size_t)(j + 1) * m + k];
+      R[(size_t)j * m + k] = cs * t1 + sn * t2;
+      R[(size_t)(j + 1) * m + k] = -sn * t1 + cs * t2;
+    }
+    double g1 = g[j], g2 = g[j + 1];
+    g[j] = cs * g1 + sn * g2;
+    g[j + 1] = -sn * g1 + cs * g2;
+  }
+  y.assign(m, 0.0);
+  for (int i = m - 1; i >= 0; --i) {
+    double s = g[i];
+    for (int k = i + 1; k < m; ++k) s -= R[(size_t)i * m + k] * y[k];
+    if (R[(size_t)i * m + i] == 0.0) return false;
+    y[i] = s / R[(size_t)i * m + i];
+  }
+  return true;
+}
+
+int read_scalar(dg_ctx* c, const double* d, double* h, cudaStream_t st) {
+  CK(c, cudaMemcpyAsync(h, d, sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(c, cudaStreamSynchronize(st));
+  return DG_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+long long dg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+const char* dg_last_error(const dg_ctx* ctx) {
+  if (ctx) return ctx->err.c_str();
+  return g_thread_error.c_str();
+}
+
+void dg_destroy(dg_ctx* ctx) {
+  if (!ctx) return;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(ctx->dev);
+  for (void* p : ctx->allocs) cudaFree(p);
+  cudaSetDevice(cur);
+  delete ctx;
+}
+
+int dg_info(const dg_ctx* ctx, int64_t* out, int32_t nout) {
+  if (!ctx || !out) return set_thread_error(DG_ERR_ARG, "dg_info: null argument");
+  int64_t v[12] = {ctx->D, ctx->N, ctx->B, ctx->nonods, ctx->ncg, (int64_t)ctx->cola.size(), ctx->ncolor,
+                   (int64_t)ctx->lev.size(), ctx->nbf, ctx->built ? 1 : 0, ctx->VG, ctx->SG};
+  for (int i = 0; i < nout && i < 12; ++i) out[i] = v[i];
+  return DG_OK;
+}
+
+int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
+  if (!m || !cfg || !out) return set_thread_error(DG_ERR_ARG, "dg_create: null argument");
+  *out = nullptr;
+  const int D = m->ndim;
+  if (D != 2 && D != 3) return set_thread_error(DG_ERR_ARG, "dg_create: ndim must be 2 or 3");
+  const int N = D == 3 ? 20 : 10, F = D + 1, VG = D == 3 ? 24 : 12, SG = D == 3 ? 12 : 4;
+  if (m->nloc != N || m->ngi != VG || m->sngi != SG)
+    return set_thread_error(DG_ERR_ARG, "dg_create: only P3 elements with degree-6 quadrature are supported");
+  if (m->nele <= 0 || m->cg_nonods <= 0 || !m->x_ref_in || !m->nbf || !m->alnmt || !m->glb_bcface_type ||
+      !m->p1cg || !m->sfc_order || !m->n || !m->nlx || !m->weight || !m->sn || !m->snlx || !m->sweight ||
+      !m->gi_align || !m->drst_duv || !m->p1_to_p3)
+    return set_thread_error(DG_ERR_ARG, "dg_create: missing mesh array");
+  if (m->nele * (int64_t)N > (int64_t)INT32_MAX / 2)
+    return set_thread_error(DG_ERR_ARG, "dg_create: mesh too large for 32-bit element indexing");
+  std::unique_ptr<dg_ctx> c(new dg_ctx());
+  c->dev = cfg->device;
+  c->cfg = *cfg;
+  c->D = D; c->N = N; c->F = F; c->NC = D + 1; c->VG = VG; c->SG = SG;
+  c->B = m->nele;
+  c->nonods = c->B * N;
+  c->ncg = m->cg_nonods;
+  CK(c.get(), cudaSetDevice(c->dev));
+  cudaDeviceProp prop;
+  CK(c.get(), cudaGetDeviceProperties(&prop, c->dev));
+  c->nsm = prop.multiProcessorCount;
+  c->nred = 2 * c->nsm;
+  const int64_t nf = c->B * F;
+  // face arrays
+  std::vector<int> nbe(nf), nbface(nf), aln(nf), bct(nf);
+  for (int64_t k = 0; k < nf; ++k) {
+    int64_t t = m->glb_bcface_type[k];
+    int64_t nb = m->nbf[k];
+    bct[k] = (int)t;
+    aln[k] = (int)std::max<int64_t>(m->alnmt[k], 0);
+    if (t < 0) {
+      if (nb < 0 || nb >= nf)
+        return fail(c.get(), DG_ERR_MESH, "interior face without a neighbour (untagged boundary face)");
+      if (m->alnmt[k] < 0 || m->alnmt[k] >= D)
+        return fail(c.get(), DG_ERR_MESH, "interior face with an invalid alignment code");
+      nbe[k] = (int)(nb / F);
+      nbface[k] = (int)(nb % F);
+    } else {
+      nbe[k] = -1;
+      nbface[k] = 0;
+      if (t == 0 || t == 1) {
+        c->bf_elem.push_back((int)(k / F));
+        c->bf_face.push_back((int)(k % F));
+        c->bf_type.push_back((int)t);
+      }
+    }
+  }
+  c->nbf = (int)c->bf_elem.size();
+  c->p1cg.assign(m->p1cg, m->p1cg + c->B * c->NC);
+  c->sfc.assign(m->sfc_order, m->sfc_order + c->ncg);
+  for (int64_t v : c->p1cg)
+    if (v < 0 || v >= c->ncg) return fail(c.get(), DG_ERR_MESH, "p1cg vertex out of range");
+  int rc;
+  if ((rc = upload(c.get(), &c->d_x, m->x_ref_in, (size_t)c->B * D * N))) return rc;
+  if ((rc = upload_vec(c.get(), &c->d_nbe, nbe))) return rc;
+  if ((rc = upload_vec(c.get(), &c->d_nbface, nbface))) return rc;
+  if ((rc = upload_vec(c.get(), &c->d_aln, aln))) return rc;
+  if ((rc = upload_vec(c.get(), &c->d_bct, bct))) return rc;
+  c->kappa.assign(c->B, 1.0);
+  if ((rc = upload_vec(c.get(), &c->d_kappa, c->kappa))) return rc;
+  // element tables
+  {
+    double* p;
+    if ((rc = upload(c.get(), &p, m->n, (size_t)N * VG))) return rc;
+    c->T.n = p;
+    if ((rc = upload(c.get(), &p, m->nlx, (size_t)D * N * VG))) return rc;
+    c->T.nlx = p;
+    if ((rc = upload(c.get(), &p, m->weight, (size_t)VG))) return rc;
+    c->T.weight = p;
+    if ((rc = upload(c.get(), &p, m->sn, (size_t)F * N * SG))) return rc;
+    c->T.sn = p;
+    if ((rc = upload(c.get(), &p, m->snlx, (size_t)F * D * N * SG))) return rc;
+    c->T.snlx = p;
+    if ((rc = upload(c.get(), &p, m->sweight, (size_t)SG))) return rc;
+    c->T.sweight = p;
+    if ((rc = upload(c.get(), &p, m->drst_duv, (size_t)F * D * (D - 1)))) return rc;
+    c->T.drst = p;
+    if ((rc = upload(c.get(), &p, m->p1_to_p3, (size_t)N * (D + 1)))) return rc;
+    c->T.P = p;
+    std::vector<int> al(D * SG);
+    for (int k = 0; k < D * SG; ++k) {
+      if (m->gi_align[k] < 0 || m->gi_align[k] >= SG) return fail(c.get(), DG_ERR_ARG, "gi_align out of range");
+      al[k] = (int)m->gi_align[k];
+    }
+    int* q;
+    if ((rc = upload_vec(c.get(), &q, al))) return rc;
+    c->T.align = q;
+  }
+  if ((rc = dalloc(c.get(), &c->d_blk, (size_t)c->B * (F + 1) * N * N))) return rc;
+  if ((rc = dalloc(c.get(), &c->d_detw, (size_t)c->B * VG))) return rc;
+  if ((rc = dalloc(c.get(), &c->d_err, 1))) return rc;
+  CK(c.get(), cudaMemset(c->d_err, 0, sizeof(int)));
+  if (c->nbf) {
+    if ((rc = upload_vec(c.get(), &c->d_bf_elem, c->bf_elem))) return rc;
+    if ((rc = upload_vec(c.get(), &c->d_bf_face, c->bf_face))) return rc;
+    if ((rc = upload_vec(c.get(), &c->d_bf_type, c->bf_type))) return rc;
+    if ((rc = dalloc(c.get(), &c->d_bf_sw, (size_t)c->nbf * SG))) return rc;
+    if ((rc = dalloc(c.get(), &c->d_bf_gn, (size_t)c->nbf * N * SG))) return rc;
+    if ((rc = dalloc(c.get(), &c->d_bf_gam, (size_t)c->nbf))) return rc;
+  }
+  // P1CG sparsity, colours, probe indices, transfer lists
+  if ((rc = p1cg_sparsity(c->B, c->NC, c->p1cg.data(), c->ncg, c->fina, c->cola)))
+    return fail(c.get(), rc, g_thread_error);
+  if ((rc = color2(c->ncg, c->fina.data(), c->cola.data(), c->whichc, c->ncolor)))
+    return fail(c.get(), rc, g_thread_error);
+  sparse_idx_for_color(c->ncg, c->fina.data(), c->cola.data(), c->whichc, c->ncolor, c->spidx, c->colidx);
+  {
+    std::vector<int> sp, ci;
+    c->sp_off.assign(1, 0);
+    for (int k = 0; k < c->ncolor; ++k) {
+      for (int64_t v : c->spidx[k]) sp.push_back((int)v);
+      for (int64_t v : c->colidx[k]) ci.push_back((int)v);
+      c->sp_off.push_back((int64_t)sp.size());
+    }
+    if ((rc = upload_vec(c.get(), &c->d_spidx, sp))) return rc;
+    if ((rc = upload_vec(c.get(), &c->d_colidx, ci))) return rc;
+    std::vector<int> wc(c->whichc.begin(), c->whichc.end());
+    if ((rc = upload_vec(c.get(), &c->d_whichc, wc))) return rc;
+    std::vector<int> p1(c->p1cg.begin(), c->p1cg.end());
+    if ((rc = upload_vec(c.get(), &c->d_p1cg, p1))) return rc;
+    std::vector<double> cnt(c->ncg, 0.0), wdg(c->B * c->NC);
+    for (int64_t v : c->p1cg) cnt[v] += 1.0;
+    for (size_t k = 0; k < c->p1cg.size(); ++k) wdg[k] = 1.0 / cnt[c->p1cg[k]];
+    if ((rc = upload_vec(c.get(), &c->d_wdg, wdg))) return rc;
+    std::vector<int> gptr(c->ncg + 1, 0), gent(c->p1cg.size());
+    for (int64_t v : c->p1cg) gptr[v + 1]++;
+    for (int64_t i = 0; i < c->ncg; ++i) gptr[i + 1] += gptr[i];
+    std::vector<int> fill(gptr.begin(), gptr.end() - 1);
+    for (size_t k = 0; k < c->p1cg.size(); ++k) gent[fill[c->p1cg[k]]++] = (int)k;   // ascending DG index
+    if ((rc = upload_vec(c.get(), &c->d_gptr, gptr))) return rc;
+    if ((rc = upload_vec(c.get(), &c->d_gent, gent))) return rc;
+    std::vector<int> pos(c->ncg);
+    std::vector<char> seen(c->ncg, 0);
+    for (int64_t i = 0; i < c->ncg; ++i) {
+      int64_t p = c->sfc[i] - 1;
+      if (p < 0 || p >= c->ncg || seen[p]) return fail(c.get(), DG_ERR_ARG, "sfc_order is not a permutation of 1..cg_nonods");
+      seen[p] = 1;
+      pos[i] = (int)p;
+    }
+    if ((rc = upload_vec(c.get(), &c->d_pos, pos))) return rc;
+  }
+  if ((rc = dalloc(c.get(), &c->d_rar, c->cola.size()))) return rc;
+  for (double** t : {&c->d_t1, &c->d_t2, &c->d_t3, &c->d_t4, &c->d_t5})
+    if ((rc = dalloc(c.get(), t, (size_t)c->nonods))) return rc;
+  for (double** t : {&c->d_cg1, &c->d_cg2})
+    if ((rc = dalloc(c.get(), t, (size_t)c->ncg))) return rc;
+  if ((rc = dalloc(c.get(), &c->d_part, (size_t)c->nred * KMAXV))) return rc;
+  for (double** t : {&c->d_h1, &c->d_h2, &c->d_y, &c->d_scal})
+    if ((rc = dalloc(c.get(), t, 256))) return rc;
+  *out = c.release();
+  return DG_OK;
+}
+
+int dg_set_kappa(dg_ctx* c, const double* kappa) {
+  if (!c) return set_thread_error(DG_ERR_ARG, "dg_set_kappa: null context");
+  if (kappa) {
+    for (int64_t e = 0; e < c->B; ++e)
+      if (!(kappa[e] > 0.0) || !std::isfinite(kappa[e])) return fail(c, DG_ERR_ARG, "kappa must be positive and finite");
+    c->kappa.assign(kappa, kappa + c->B);
+  } else {
+    c->kappa.assign(c->B, 1.0);
+  }
+  CK(c, cudaSetDevice(c->dev));
+  CK(c, cudaMemcpy(c->d_kappa, c->kappa.data(), sizeof(double) * c->B, cudaMemcpyHostToDevice));
+  c->built = false;
+  return DG_OK;
+}
+
+int dg_build_operator(dg_ctx* c, void* stream) {
+  if (!c) return set_thread_error(DG_ERR_ARG, "dg_build_operator: null context");
+  cudaStream_t st = S(stream);
+  CK(c, cudaSetDevice(c->dev));
+  int rc;
+  CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
+  if ((rc = (c->D == 3 ? launch_build<3>(c, st) : launch_build<2>(c, st)))) return rc;
+  int herr = 0;
+  CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(c, cudaStreamSynchronize(st));
+  if (herr) return fail(c, DG_ERR_MESH, "non-positive element Jacobian (element not positively oriented)");
+  c->built = true;   // blocks are usable from here on (the probes below apply them)
+  // colour-probe Galerkin operator on P1CG (volume_mf_diff.py:1696-1754)
+  CK(c, cudaMemsetAsync(c->d_rar, 0, sizeof(double) * c->cola.size(), st));
+  for (int col = 1; col <= c->ncolor; ++col) {
+    if ((rc = prolong_cg(c, c->d_t1, nullptr, false, col, false, st))) return rc;
+    if ((rc = residual(c, c->d_t1, nullptr, c->d_t2, nullptr, RF_NEG, st))) return rc;   // t2 = A t1
+    if ((rc = restrict_cg(c, c->d_t2, c->d_cg1, false, st))) return rc;
+    int64_t a = c->sp_off[col - 1], b = c->sp_off[col];
+    if (b > a)
+      rar_scatter_kernel<<<nblk(b - a, 128), 128, 0, st>>>(c->d_rar, c->d_cg1, c->d_spidx + a, c->d_colidx + a,
+                                                            (int)(b - a)); bump();
+    CKL(c);
+  }
+  c->rar_host.assign(c->cola.size(), 0.0);
+  CK(c, cudaMemcpyAsync(c->rar_host.data(), c->d_rar, sizeof(double) * c->cola.size(), cudaMemcpyDeviceToHost, st));
+  CK(c, cudaStreamSynchronize(st));
+  // SFC levels (compact_fcode.f90 + get_a_diaga)
+  SfcHierarchy h;
+  if ((rc = sfc_levels(c->ncg, c->fina.data(), c->cola.data(), c->rar_host.data(), c->sfc.data(), h)))
+    return fail(c, rc, g_thread_error);
+  // (re)allocate the device levels
+  if (c->lev.size() != (size_t)h.nlevel) {
+    c->lev.assign(h.nlevel, DevLevel());
+    for (int l = 0; l < h.nlevel; ++l) {
+      DevLevel& L = c->lev[l];
+      L.n = (int)h.sizes[l];
+      int64_t nnz = h.row_ptr[h.start[l + 1]] - h.row_ptr[h.start[l]];
+      if ((rc = dalloc(c, &L.rowptr, L.n + 1))) return rc;
+      if ((rc = dalloc(c, &L.col, nnz))) return rc;
+      if ((rc = dalloc(c, &L.val, nnz))) return rc;
+      if ((rc = dalloc(c, &L.diag, L.n))) return rc;
+      if ((rc = dalloc(c, &L.e, L.n))) return rc;
+      if ((rc = dalloc(c, &L.e2, L.n))) return rc;
+      if ((rc = dalloc(c, &L.r, L.n))) return rc;
+      if ((rc = dalloc(c, &L.rr, L.n))) return rc;
+      if (l + 1 < h.nlevel) {
+        // nn.Upsample(scale_factor = n_l / n_{l+1}, nearest) source index:
+        // floor(float32(dst * (1 / s))) with the product in double
+        int nc = (int)h.sizes[l + 1];
+        double s = (double)L.n / (double)nc;
+        int out = (int)std::floor((double)nc * s);
+        if (out != L.n) return fail(c, DG_ERR_STATE, "upsampled level size differs from the fine level");
+        std::vector<int> up(L.n);
+        for (int i = 0; i < L.n; ++i) {
+          int src;
+          if (L.n == nc) src = i;
+          else if (L.n == 2 * nc) src = i >> 1;
+          else src = (int)std::floor((float)((double)i * (1.0 / s)));
+          up[i] = std::min(src, nc - 1);
+        }
+        if ((rc = upload_vec(c, &L.up, up))) return rc;
+      }
+    }
+  }
+  for (int l = 0; l < h.nlevel; ++l) {
+    DevLevel& L = c->lev[l];
+    int64_t r0 = h.start[l];
+    int64_t base = h.row_ptr[r0];
+    int64_t nnz = h.row_ptr[h.start[l + 1]] - base;
+    std::vector<int> rp(L.n + 1), cl(nnz);
+    std::vector<double> vl(nnz), dg(L.n, 0.0);
+    // sort each row by column (torch CSR from COO), take the diagonal
+    for (int i = 0; i < L.n; ++i) {
+      int64_t a = h.row_ptr[r0 + i], b = h.row_ptr[r0 + i + 1];
+      std::vector<std::pair<int64_t, double>> row;
+      for (int64_t k = a; k < b; ++k) row.emplace_back(h.col[k], h.val[k]);
+      std::sort(row.begin(), row.end(), [](auto& x, auto& y) { return x.first < y.first; });
+      rp[i] = (int)(a - base);
+      for (size_t k = 0; k < row.size(); ++k) {
+        cl[a - base + k] = (int)row[k].first;
+        vl[a - base + k] = row[k].second;
+        if (row[k].first == i) dg[i] = row[k].second;
+      }
+    }
+    rp[L.n] = (int)nnz;
+    CK(c, cudaMemcpy(L.rowptr, rp.data(), sizeof(int) * rp.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(L.col, cl.data(), sizeof(int) * cl.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(L.val, vl.data(), sizeof(double) * vl.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(L.diag, dg.data(), sizeof(double) * dg.size(), cudaMemcpyHostToDevice));
+  }
+  return DG_OK;
+}
+
+int dg_get_bdiag(dg_ctx* c, double* bdiag, double* diag, void* stream) {
+  if (!c || !bdiag) return set_thread_error(DG_ERR_ARG, "dg_get_bdiag: null argument");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_get_bdiag: operator not built");
+  cudaStream_t st = S(stream);
+  CK(c, cudaSetDevice(c->dev));
+  const int N = c->N, F = c->F;
+  // blocks are stored column-major: transpose block 0 of every element
+  CK(c, cudaMemcpy2DAsync(bdiag, sizeof(double) * N * N, c->d_blk, sizeof(double) * N * N * (F + 1),
+                          sizeof(double) * N * N, c->B, cudaMemcpyDeviceToDevice, st));
+  // in-place transpose on the device copy (row-major output)
+  // (A_ee is symmetric up to roundoff; transpose keeps the exact entries)
+  std::vector<double> h((size_t)c->B * N * N);
+  CK(c, cudaMemcpyAsync(h.data(), bdiag, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+  CK(c, cudaStreamSynchronize(st));
+  std::vector<double> t(h.size()), dgv((size_t)c->B * N);
+  for (int64_t e = 0; e < c->B; ++e)
+    for (int m = 0; m < N; ++m) {
+      for (int n = 0; n < N; ++n) t[(e * N + m) * N + n] = h[(e * N + n) * N + m];
+      dgv[e * N + m] = h[(e * N + m) * N + m];
+    }
+  CK(c, cudaMemcpyAsync(bdiag, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice, st));
+  if (diag) CK(c, cudaMemcpyAsync(diag, dgv.data(), sizeof(double) * dgv.size(), cudaMemcpyHostToDevice, st));
+  CK(c, cudaStreamSynchronize(st));
+  return DG_OK;
+}
+
+int dg_get_rar(dg_ctx* c, double* values, void* stream) {
+  if (!c || !values) return set_thread_error(DG_ERR_ARG, "dg_get_rar: null argument");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_get_rar: operator not built");
+  CK(c, cudaSetDevice(c->dev));
+  CK(c, cudaMemcpyAsync(values, c->d_rar, sizeof(double) * c->cola.size(), cudaMemcpyDeviceToDevice, S(stream)));
+  return DG_OK;
+}
+
+int dg_residual(dg_ctx* c, const double* x, const double* b, double* r, double* x_out, int32_t do_smooth,
+                void* stream) {
+  if (!c || !x || !r) return set_thread_error(DG_ERR_ARG, "dg_residual: null argument");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_residual: operator not built");
+  if (do_smooth && !x_out) return fail(c, DG_ERR_ARG, "dg_residual: x_out required for smoothing");
+  cudaStream_t st = S(stream);
+  CK(c, cudaSetDevice(c->dev));
+  if (!do_smooth) return residual(c, x, b, r, nullptr, 0, st);
+  double* dst = (x_out == x) ? c->d_t1 : x_out;
+  int rc = residual(c, x, b, r, dst, RF_SMOOTH, st);
+  if (rc) return rc;
+  if (dst != x_out) CK(c, cudaMemcpyAsync(x_out, dst, sizeof(double) * c->nonods, cudaMemcpyDeviceToDevice, st));
+  return DG_OK;
+}
+
+int dg_apply(dg_ctx* c, const double* x, double* y, void* stream) {
+  if (!c || !x || !y) return set_thread_error(DG_ERR_ARG, "dg_apply: null argument");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_apply: operator not built");
+  CK(c, cudaSetDevice(c->dev));
+  return residual(c, x, nullptr, y, nullptr, RF_NEG, S(stream));
+}
+
+int dg_rhs(dg_ctx* c, const double* f, const double* g, const double* gn, double* b, void* stream) {
+  if (!c || !f || !b) return set_thread_error(DG_ERR_ARG, "dg_rhs: null argument");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_rhs: operator not built");
+  cudaStream_t st = S(stream);
+  CK(c, cudaSetDevice(c->dev));
+  if (c->D == 3) {
+    using E = Elem<3>;
+    rhs_mass_kernel<E::N, E::VG, E::EPB><<<nblk(c->B, E::EPB), E::EPB * E::N, 0, st>>>(c->T.n, c->d_detw, f, b, c->B); bump();
+  } else {
+    using E = Elem<2>;
+    rhs_mass_kernel<E::N, E::VG, E::EPB><<<nblk(c->B, E::EPB), E::EPB * E::N, 0, st>>>(c->T.n, c->d_detw, f, b, c->B); bump();
+  }
+  CKL(c);
+  for (int mode = 0; mode < 2; ++mode) {
+    const double* src = mode == 0 ? g : gn;
+    if (!src || c->nbf == 0) continue;
+    for (int fsel = 0; fsel < c->F; ++fsel) {
+      if (c->D == 3)
+        rhs_bface_kernel<20, 12><<<nblk(c->nbf, 8), 8 * 20, 0, st>>>(
+            c->T.sn, c->d_bf_elem, c->d_bf_face, c->d_bf_type, c->d_bf_sw, c->d_bf_gn, c->d_bf_gam, c->d_kappa, src,
+            b, c->nbf, fsel, mode, c->cfg.mu_f);
+      else
+        rhs_bface_kernel<10, 4><<<nblk(c->nbf, 16), 16 * 10, 0, st>>>(
+            c->T.sn, c->d_bf_elem, c->d_bf_face, c->d_bf_type, c->d_bf_sw, c->d_bf_gn, c->d_bf_gam, c->d_kappa, src,
+            b, c->nbf, fsel, mode, c->cfg.mu_f);
+      bump();
+      CKL(c);
+    }
+  }
+  return DG_OK;
+}
+
+int dg_precond(dg_ctx* c, const double* r, double* z, void* stream) {
+  if (!c || !r || !z) return set_thread_error(DG_ERR_ARG, "dg_precond: null argument");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_precond: operator not built");
+  cudaStream_t st = S(stream);
+  CK(c, cudaSetDevice(c->dev));
+  if (z == r) {
+    int rc = precond(c, r, c->d_t1, st);
+    if (rc) return rc;
+    CK(c, cudaMemcpyAsync(z, c->d_t1, sizeof(double) * c->nonods, cudaMemcpyDeviceToDevice, st));
+    return DG_OK;
+  }
+  return precond(c, r, z, st);
+}
+
+int dg_mg_vcycle(dg_ctx* c, const double* r_sfc, double* e_sfc, void* stream) {
+  if (!c || !r_sfc || !e_sfc) return set_thread_error(DG_ERR_ARG, "dg_mg_vcycle: null argument");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_mg_vcycle: operator not built");
+  cudaStream_t st = S(stream);
+  CK(c, cudaSetDevice(c->dev));
+  int rc = vcycle(c, r_sfc, st);
+  if (rc) return rc;
+  CK(c, cudaMemcpyAsync(e_sfc, c->lev[0].e, sizeof(double) * c->ncg, cudaMemcpyDeviceToDevice, st));
+  return DG_OK;
+}
+
+int dg_gmres(dg_ctx* c, double* x, const double* b, double tol, int32_t m, int32_t max_its, int32_t* its_out,
+             double* res_out, void* stream) {
+  if (!c || !x || !b) return set_thread_error(DG_ERR_ARG, "dg_gmres: null argument");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_gmres: operator not built");
+  if (m <= 0 || m > 256 || max_its < 0) return fail(c, DG_ERR_ARG, "dg_gmres: 1 <= m <= 256 required");
+  cudaStream_t st = S(stream);
+  CK(c, cudaSetDevice(c->dev));
+  int rc;
+  if ((rc = ensure_krylov(c, m))) return rc;
+  double* r = c->d_t1;
+  double* w = c->d_t2;
+  int its = 0;
+  double r0l2 = 1.0;   // the reference starts from 1 and tests before each cycle
+  std::vector<double> Hh((size_t)(m + 1) * m), y;
+  int status = DG_OK;
+  while (r0l2 > tol && its < max_its) {
+    CK(c, cudaMemsetAsync(c->d_H, 0, sizeof(double) * (m + 1) * m, st));
+    if ((rc = residual(c, x, b, w, nullptr, 0, st))) return rc;          // w = b - A x
+    if ((rc = precond(c, w, r, st))) return rc;                           // r = M^-1 w
+    if ((rc = norm2(c, r, c->d_scal, st))) return rc;
+    double beta;
+    if ((rc = read_scalar(c, c->d_scal, &beta, st))) return rc;
+    if (!(beta > 0.0) || !std::isfinite(beta)) {
+      status = beta == 0.0 ? DG_OK : DG_ERR_NUMERIC;
+      break;
+    }
+    scale_kernel<<<nblk(c->nonods, 256), 256, 0, st>>>(r, c->d_scal, c->d_V, c->nonods); bump();
+    CKL(c);
+    for (int j = 0; j < m; ++j) {
+      if ((rc = residual(c, c->d_V + (size_t)j * c->nonods, nullptr, w, nullptr, RF_NEG, st))) return rc;  // w = A v
+      if ((rc = precond(c, w, r, st))) return rc;
+      if ((rc = cgs2(c, j, r, m, st))) return rc;
+      ++its;
+    }
+    CK(c, cudaMemcpyAsync(Hh.data(), c->d_H, sizeof(double) * Hh.size(), cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    if (!solve_hessenberg(Hh, m, beta, y)) {
+      status = DG_ERR_NUMERIC;
+      c->err = "GMRES breakdown: singular Hessenberg matrix";
+      break;
+    }
+    CK(c, cudaMemcpyAsync(c->d_y, y.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+    combine_kernel<<<nblk(c->nonods, 256), 256, 0, st>>>(c->d_V, c->nonods, m, c->d_y, x, c->nonods); bump();
+    CKL(c);
+    if ((rc = residual(c, x, b, w, nullptr, 0, st))) return rc;
+    if ((rc = norm2(c, w, c->d_scal, st))) return rc;
+    if ((rc = read_scalar(c, c->d_scal, &r0l2, st))) return rc;
+    if (!std::isfinite(r0l2)) {
+      status = DG_ERR_NUMERIC;
+      c->err = "GMRES produced a non-finite residual";
+      break;
+    }
+  }
+  if (its_out) *its_out = its;
+  if (res_out) *res_out = r0l2;
+  if (status == DG_OK && r0l2 > tol && its >= max_its) {
+    c->err = "GMRES reached the iteration limit";
+    return DG_ERR_NOCONV;
+  }
+  return status;
+}
+
+}  // extern "C"

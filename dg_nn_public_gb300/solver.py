@@ -1,0 +1,240 @@
+"""Host-side object around one libdgsip context (one mesh on one GPU).
+
+``DGSolver`` owns a C-ABI context and exposes the solve stages on torch CUDA
+tensors (FP64, element-major ``(nele, nloc)`` or flat).  It is the layer the
+reference-compatible modules (``volume_mf_diff``, ``multigrid_linearelastic``,
+``get_bdiag_diag``) are written on.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import _capi
+from .element import ElementTables, drst_duv, p3_element
+from .mesh import DGMesh
+
+
+@dataclass
+class SolverConfig:
+    """Solver knobs, named after the reference's config module (z06/config.py)."""
+    eta_e: float = 90.0            # penalty (reference default 36; 10 p^2 here)
+    mu_f: float = 1.0
+    jac_wei: float = 2.0 / 3.0
+    pre_smooth_its: int = 3
+    post_smooth_its: int = 3
+    gmres_m: int = 30
+    gmres_its: int = 400
+    device: int = 0
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class DGSolver:
+    """One mesh + operator resident on one GPU."""
+
+    def __init__(self, mesh: DGMesh, sfc_order: np.ndarray, cfg: Optional[SolverConfig] = None,
+                 el: Optional[ElementTables] = None):
+        self.mesh = mesh
+        self.cfg = cfg or SolverConfig()
+        self.el = el or p3_element(mesh.ndim)
+        L = _capi.lib()
+        D = mesh.ndim
+        keep = dict(
+            x=np.ascontiguousarray(mesh.x_ref_in, dtype=np.float64),
+            nbf=np.ascontiguousarray(mesh.nbf, dtype=np.int64),
+            aln=np.ascontiguousarray(mesh.alnmt, dtype=np.int64),
+            bct=np.ascontiguousarray(mesh.glb_bcface_type, dtype=np.int64),
+            p1=np.ascontiguousarray(mesh.p1cg, dtype=np.int64),
+            sfc=np.ascontiguousarray(np.asarray(sfc_order).reshape(-1), dtype=np.int64),
+            n=np.ascontiguousarray(self.el.n), nlx=np.ascontiguousarray(self.el.nlx),
+            w=np.ascontiguousarray(self.el.weight), sn=np.ascontiguousarray(self.el.sn),
+            snlx=np.ascontiguousarray(self.el.snlx), sw=np.ascontiguousarray(self.el.sweight),
+            al=np.ascontiguousarray(self.el.gi_align, dtype=np.int64),
+            dr=np.ascontiguousarray(drst_duv(D).reshape(D + 1, D, D - 1)),
+            P=np.ascontiguousarray(self.el.p1_to_p3),
+        )
+        self._keep = keep
+        md = _capi.dg_mesh_desc(
+            ndim=D, nloc=mesh.nloc, nele=mesh.nele, x_ref_in=keep["x"].ctypes.data,
+            nbf=keep["nbf"].ctypes.data, alnmt=keep["aln"].ctypes.data,
+            glb_bcface_type=keep["bct"].ctypes.data, cg_nonods=mesh.cg_nonods,
+            p1cg=keep["p1"].ctypes.data, sfc_order=keep["sfc"].ctypes.data,
+            ngi=self.el.ngi, sngi=self.el.sngi, n=keep["n"].ctypes.data, nlx=keep["nlx"].ctypes.data,
+            weight=keep["w"].ctypes.data, sn=keep["sn"].ctypes.data, snlx=keep["snlx"].ctypes.data,
+            sweight=keep["sw"].ctypes.data, gi_align=keep["al"].ctypes.data,
+            drst_duv=keep["dr"].ctypes.data, p1_to_p3=keep["P"].ctypes.data)
+        c = self.cfg
+        cf = _capi.dg_config(eta_e=c.eta_e, mu_f=c.mu_f, jac_wei=c.jac_wei,
+                             pre_smooth_its=c.pre_smooth_its, post_smooth_its=c.post_smooth_its,
+                             device=c.device)
+        h = C.c_void_p()
+        _capi.check(L.dg_create(C.byref(md), C.byref(cf), C.byref(h)))
+        self._ctx = h
+        self._lib = L
+        self.built = False
+        self.nonods = mesh.nele * mesh.nloc
+        info = self.info()
+        self.ncola = int(info["ncola"])
+        self.ncolor = int(info["ncolor"])
+        self.nlevel = int(info["nlevel"])
+
+    # -- plumbing --------------------------------------------------------
+    @property
+    def ctx(self):
+        return self._ctx
+
+    def _chk(self, rc):
+        _capi.check(rc, self._ctx)
+
+    @staticmethod
+    def _stream():
+        torch = _torch()
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def _dev(self):
+        return "cuda:%d" % self.cfg.device
+
+    def _vec(self, n=None):
+        torch = _torch()
+        return torch.empty(self.nonods if n is None else n, dtype=torch.float64, device=self._dev())
+
+    @staticmethod
+    def _check_t(t, n):
+        if t is None:
+            return None
+        if not (t.is_cuda and t.dtype == _torch().float64 and t.is_contiguous() and t.numel() == n):
+            raise ValueError("expected a contiguous FP64 CUDA tensor with %d entries" % n)
+        return t.data_ptr()
+
+    def info(self):
+        out = np.zeros(12, dtype=np.int64)
+        self._chk(self._lib.dg_info(self._ctx, out.ctypes.data, 12))
+        keys = ["ndim", "nloc", "nele", "nonods", "cg_nonods", "ncola", "ncolor", "nlevel", "nbface",
+                "built", "ngi", "sngi"]
+        return dict(zip(keys, out.tolist()))
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.dg_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- operator --------------------------------------------------------
+    def set_kappa(self, kappa: Optional[np.ndarray]):
+        k = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        self._keep["kappa"] = k
+        self._chk(self._lib.dg_set_kappa(self._ctx, None if k is None else k.ctypes.data))
+        self.built = False
+
+    def build_operator(self):
+        self._chk(self._lib.dg_build_operator(self._ctx, self._stream()))
+        self.built = True
+
+    def bdiag(self):
+        torch = _torch()
+        N = self.mesh.nloc
+        K = torch.empty(self.mesh.nele, N, N, dtype=torch.float64, device=self._dev())
+        d = torch.empty(self.mesh.nele, N, dtype=torch.float64, device=self._dev())
+        self._chk(self._lib.dg_get_bdiag(self._ctx, K.data_ptr(), d.data_ptr(), self._stream()))
+        return K, d
+
+    def rar_values(self):
+        v = self._vec(self.ncola)
+        self._chk(self._lib.dg_get_rar(self._ctx, v.data_ptr(), self._stream()))
+        return v
+
+    # -- stages ----------------------------------------------------------
+    def residual(self, x, b=None, r=None, x_out=None, smooth=False):
+        """r = b - A x; with smooth also x_out <- smoothed x (may alias x)."""
+        n = self.nonods
+        r = self._vec() if r is None else r
+        if smooth and x_out is None:
+            x_out = x
+        self._chk(self._lib.dg_residual(self._ctx, self._check_t(x, n), self._check_t(b, n),
+                                        self._check_t(r, n), self._check_t(x_out, n) if smooth else None,
+                                        1 if smooth else 0, self._stream()))
+        return r
+
+    def apply(self, x, y=None):
+        y = self._vec() if y is None else y
+        self._chk(self._lib.dg_apply(self._ctx, self._check_t(x, self.nonods), self._check_t(y, self.nonods),
+                                     self._stream()))
+        return y
+
+    def rhs(self, f, g=None, gn=None, b=None):
+        n = self.nonods
+        b = self._vec() if b is None else b
+        self._chk(self._lib.dg_rhs(self._ctx, self._check_t(f, n), self._check_t(g, n), self._check_t(gn, n),
+                                   self._check_t(b, n), self._stream()))
+        return b
+
+    def precond(self, r, z=None):
+        z = self._vec() if z is None else z
+        self._chk(self._lib.dg_precond(self._ctx, self._check_t(r, self.nonods), self._check_t(z, self.nonods),
+                                       self._stream()))
+        return z
+
+    def mg_vcycle(self, r_sfc, e_sfc=None):
+        n = self.mesh.cg_nonods
+        e_sfc = self._vec(n) if e_sfc is None else e_sfc
+        self._chk(self._lib.dg_mg_vcycle(self._ctx, self._check_t(r_sfc, n), self._check_t(e_sfc, n),
+                                         self._stream()))
+        return e_sfc
+
+    def solve(self, f, g=None, rtol=1e-10, x0=None, out=None):
+        """Solve A x = M f + lift(g) to ||b - A x|| <= rtol * ||b - A x0||.
+
+        f, g: nodal source / Dirichlet data, (nele*nloc) FP64, on the host
+        (numpy or torch CPU, preferably pinned) or on this GPU.  Host inputs
+        are copied in and the solution copied back into ``out`` (a host
+        tensor, allocated pinned when None); device inputs give a device
+        solution.  Returns (x, its, final residual norm).
+        """
+        torch = _torch()
+        dev = self._dev()
+        on_host = not (isinstance(f, torch.Tensor) and f.is_cuda)
+
+        def to_dev(a):
+            if a is None:
+                return None
+            if isinstance(a, np.ndarray):
+                a = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64).reshape(-1))
+            return a.reshape(-1).to(dev, non_blocking=True)
+        fd, gd = to_dev(f), to_dev(g)
+        b = self.rhs(fd, gd)
+        x = torch.zeros_like(b) if x0 is None else to_dev(x0).clone()
+        r0 = b if x0 is None else self.residual(x, b)
+        tol = rtol * float(torch.linalg.norm(r0))
+        its, res = self.gmres(x, b, tol)
+        if on_host:
+            if out is None:
+                out = torch.empty(self.nonods, dtype=torch.float64, pin_memory=True)
+            out.copy_(x, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            return out, its, res
+        return x, its, res
+
+    def gmres(self, x, b, tol, m=None, max_its=None, raise_noconv=False):
+        """Restarted GMRES(m) in place on x; returns (its, final ||b - A x||)."""
+        m = self.cfg.gmres_m if m is None else m
+        max_its = self.cfg.gmres_its if max_its is None else max_its
+        its = C.c_int32(0)
+        res = C.c_double(0.0)
+        rc = self._lib.dg_gmres(self._ctx, self._check_t(x, self.nonods), self._check_t(b, self.nonods),
+                                float(tol), int(m), int(max_its), C.byref(its), C.byref(res), self._stream())
+        if rc == _capi.DG_ERR_NOCONV and not raise_noconv:
+            return its.value, res.value
+        self._chk(rc)
+        return its.value, res.value

@@ -1,0 +1,171 @@
+/*
+ * dgsip.h -- C ABI of the GB300 SIP-DG diffusion solver (libdgsip.so).
+ *
+ * Symmetric interior-penalty DG for -div(kappa grad u) = f on cubic (P3)
+ * triangles (2D, 10 nodes) and tetrahedra (3D, 20 nodes), with the
+ * reference's DG->CG P1 + space-filling-curve multigrid preconditioner and
+ * restarted GMRES.  Every function returns 0 on success and a positive
+ * error code otherwise; dg_last_error() gives the message.  No function
+ * calls exit() or traps the device.
+ *
+ * Memory: arrays marked [host] are read during the call and copied; arrays
+ * marked [device] are caller-owned device pointers (e.g. torch CUDA tensor
+ * storage), FP64, element-major (nele, nloc).  A context owns every other
+ * device buffer.  All device work of a call is enqueued on `stream`
+ * (a cudaStream_t passed as void*, NULL = legacy default stream); calls on
+ * one context are not thread-safe.
+ *
+ * Reference: linfeng810/dg_nn_public, directory z02-implicit/z06-DGtoCG
+ * (cited below as z06/) and z00-fortran-src.
+ */
+#ifndef DGSIP_H
+#define DGSIP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dg_ctx dg_ctx;
+
+/* Error codes. */
+enum {
+  DG_OK = 0,
+  DG_ERR_ARG = 1,        /* invalid argument / size */
+  DG_ERR_CUDA = 2,       /* CUDA runtime error */
+  DG_ERR_MESH = 3,       /* inconsistent mesh arrays */
+  DG_ERR_STATE = 4,      /* call order (e.g. solve before build_operator) */
+  DG_ERR_NUMERIC = 5,    /* breakdown / non-finite values */
+  DG_ERR_NOCONV = 6,     /* iteration limit reached before the tolerance */
+  DG_ERR_ALLOC = 7       /* device or host allocation failed */
+};
+
+/* Storage precision of the stored operator blocks / multigrid. */
+enum { DG_F64 = 0, DG_F32 = 1, DG_BF16 = 2 };
+
+/* Mesh + reference element, in the reference's layout.
+ * Replaces the implicit inputs the reference reads from its FuncSpace /
+ * Element objects and cmmn_data.SfNdNb (z06/function_space.py:83-404,
+ * z06/cmmn_data.py:8-138). */
+typedef struct dg_mesh_desc {
+  int32_t ndim;                 /* 2 or 3 */
+  int32_t nloc;                 /* 10 (tri) or 20 (tet) */
+  int64_t nele;
+  const double*  x_ref_in;      /* [host] (nele, ndim, nloc) node coordinates */
+  const int64_t* nbf;           /* [host] (nele*nface) neighbour face, -1 = none */
+  const int64_t* alnmt;         /* [host] (nele*nface) quadrature alignment code */
+  const int64_t* glb_bcface_type; /* [host] (nele*nface) -1 interior, 0 Dirichlet, 1 Neumann */
+  int64_t cg_nonods;            /* number of P1CG vertices */
+  const int64_t* p1cg;          /* [host] (nele, ndim+1) P1CG vertex of each corner, 0-based */
+  const int64_t* sfc_order;     /* [host] (cg_nonods) 1-based curve position of each vertex */
+  /* reference-element tables (z06/shape_function.py:459-1317) */
+  int32_t ngi, sngi;
+  const double*  n;             /* [host] (nloc, ngi) */
+  const double*  nlx;           /* [host] (ndim, nloc, ngi) */
+  const double*  weight;        /* [host] (ngi) */
+  const double*  sn;            /* [host] (nface, nloc, sngi) */
+  const double*  snlx;          /* [host] (nface, ndim, nloc, sngi) */
+  const double*  sweight;       /* [host] (sngi) */
+  const int64_t* gi_align;      /* [host] (ndim, sngi) */
+  const double*  drst_duv;      /* [host] (nface, ndim, ndim-1) face tangents (z06/function_space.py:200-219) */
+  const double*  p1_to_p3;      /* [host] (nloc, ndim+1) element prolongator (z06/mesh_init.py:586-607) */
+} dg_mesh_desc;
+
+/* Solver knobs; names follow z06/config.py:103-149, 245. */
+typedef struct dg_config {
+  double  eta_e;                /* penalty coefficient (gamma = eta_e / h) */
+  double  mu_f;                 /* diffusion coefficient multiplier */
+  double  jac_wei;              /* Jacobi weight (2/3) */
+  int32_t pre_smooth_its;       /* smoothing steps before/after the coarse correction */
+  int32_t post_smooth_its;      /* SFC-level post smoothing (reference: post_smooth_its) */
+  int32_t device;               /* CUDA device ordinal */
+} dg_config;
+
+/* ---- context (replaces module state: z06/config.py, z06/cmmn_data.py) ---- */
+int  dg_create(const dg_mesh_desc* mesh, const dg_config* cfg, dg_ctx** out);
+void dg_destroy(dg_ctx* ctx);
+/* Message of the last failed call on ctx; ctx = NULL gives the last failed
+ * dg_create / host-only helper on this thread. */
+const char* dg_last_error(const dg_ctx* ctx);
+int  dg_info(const dg_ctx* ctx, int64_t* out, int32_t nout);
+/* Number of CUDA kernels this library has launched in this process (all
+ * contexts); used to account for device work in benchmarks. */
+long long dg_launch_count(void);
+
+/* ---- operator ---- */
+/* Per-element diffusivity (z05-ns/volume_mf_um_diff_varprop.py:422-426,
+ * 567, 682); NULL restores kappa = 1. */
+int dg_set_kappa(dg_ctx* ctx, const double* kappa /* [host] (nele) or NULL */);
+/* Assemble the stored element blocks, the block diagonal, the colour-probe
+ * Galerkin P1CG operator and the SFC levels.  Replaces get_bdiag_diag()
+ * (z06/get_bdiag_diag.py:30-62) and _get_RAR_and_sfc_data_Um()
+ * (z06/volume_mf_diff.py:1642-1693, multigrid_linearelastic.py:175-283). */
+int dg_build_operator(dg_ctx* ctx, void* stream);
+/* Copy bdiagK (nele, nloc, nloc) and diagK (nele, nloc) out. */
+int dg_get_bdiag(dg_ctx* ctx, double* bdiag /* [device] */, double* diag /* [device] or NULL */, void* stream);
+/* Copy the P1CG Galerkin values (ncola) into a device buffer. */
+int dg_get_rar(dg_ctx* ctx, double* values /* [device] */, void* stream);
+
+/* r = b - A x, and with do_smooth != 0 also x_out = x + w*c where c is three
+ * point-Jacobi sweeps on each element block.  b may be NULL (taken as 0).
+ * x_out may alias x.  Replaces get_residual_or_smooth
+ * (z06/volume_mf_diff.py:403-483) with its _k_res_one_batch (:487-617) and
+ * _s_res_one_batch (:1563-1639) callees. */
+int dg_residual(dg_ctx* ctx, const double* x, const double* b, double* r, double* x_out,
+                int32_t do_smooth, void* stream);
+/* y = A x */
+int dg_apply(dg_ctx* ctx, const double* x, double* y, void* stream);
+/* b = M f + Dirichlet lifting of g + Neumann flux gn (z06/volume_mf_diff.py:153-359).
+ * g, gn may be NULL. */
+int dg_rhs(dg_ctx* ctx, const double* f, const double* g, const double* gn, double* b, void* stream);
+
+/* ---- preconditioner ---- */
+/* z = one DG->CG + SFC multigrid V-cycle applied to r, starting from z = 0
+ * (_um_left_precond, z06/volume_mf_diff.py:1934-2029). */
+int dg_precond(dg_ctx* ctx, const double* r, double* z, void* stream);
+/* e = one SFC V-cycle on the P1CG residual r, both in SFC order
+ * (mg_on_P1CG, z06/multigrid_linearelastic.py:112-172). */
+int dg_mg_vcycle(dg_ctx* ctx, const double* r_sfc, double* e_sfc, void* stream);
+
+/* ---- Krylov (z06/volume_mf_diff.py:1757-1841) ---- */
+/* Left-preconditioned restarted GMRES(m) from the initial guess in x.
+ * Stops when ||b - A x|| <= tol (absolute, tested after each restart cycle
+ * as the reference does) or after max_its Arnoldi steps (status
+ * DG_ERR_NOCONV, x holds the last iterate).  Arnoldi uses classical
+ * Gram-Schmidt with one reorthogonalisation (CGS2).  its and res_norm
+ * (final ||b - A x||) may be NULL. */
+int dg_gmres(dg_ctx* ctx, double* x, const double* b, double tol, int32_t m, int32_t max_its,
+             int32_t* its, double* res_norm, void* stream);
+
+/* ---- host-only integer layer (no GPU needed) ---- */
+/* P1CG sparsity from the element corners: all vertex pairs sharing an
+ * element, rows sorted (z06/sparsity.py:102-122 with
+ * z00-fortran-src/get_neighbouring.f90:133-157).  fina has cg_nonods+1
+ * entries; cola capacity cap; *ncola gets the count. */
+int dg_p1cg_sparsity(int64_t nele, int32_t ncorner, const int64_t* p1cg, int64_t cg_nonods,
+                     int64_t* fina, int64_t* cola, int64_t cap, int64_t* ncola);
+/* Greedy distance-2 colouring in vertex order (z06/sparsity.py:235-269);
+ * colours are 1-based. */
+int dg_color2(int64_t n, const int64_t* fina, const int64_t* cola, int64_t* whichc, int32_t* ncolor);
+/* Number of SFC grid levels (z00-fortran-src/compact_fcode.f90:229-250). */
+int32_t dg_nlevel_sfc(int64_t nonods);
+/* All SFC grid levels of a CSR matrix (compact_fcode.f90:7-225):
+ * level_start (nlevel+1) gives each level's first row in the stacked
+ * numbering; row_ptr (total+1) indexes col (cap) and val (cap), which hold
+ * the stacked level matrices with 0-based level-local column indices in the
+ * Fortran first-appearance order and values summed in the Fortran traversal
+ * order.  The matrix rows and sfc_order use the caller's vertex numbering;
+ * the levels are in curve order. */
+int dg_sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double* a,
+                  const int64_t* sfc_order, int32_t* nlevel, int64_t* level_start,
+                  int64_t* row_ptr, int64_t* col, double* val, int64_t cap, int64_t* nnz);
+/* Face connectivity of cells in the reference's internal corner order
+ * (z06/mesh_init.py:298-401): nbf and alnmt for all nele*nface faces. */
+int dg_face_connectivity(int32_t ndim, int64_t nele, const int64_t* corners /* (nele, ndim+1) */,
+                         int64_t* nbf, int64_t* alnmt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DGSIP_H */

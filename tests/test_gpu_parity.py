@@ -1,0 +1,153 @@
+"""CUDA path (through the C ABI) against the reference's golden vectors and the oracle.
+
+Every stage of the plain FP64 solve is compared on the committed golden
+cases (outputs of the reference itself), then on larger meshes against the
+CPU oracle, and at the 3D benchmark size through size-independent checks.
+Tolerances are relative max-abs errors: 1e-12 for single stages (FP64
+roundoff of a different summation order), 1e-10 for GMRES solutions
+(roundoff amplified by the iteration, bounded by the condition number).
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from dg_nn_public_gb300 import element, mesh, sfc  # noqa: E402
+from dg_nn_public_gb300.solver import DGSolver, SolverConfig  # noqa: E402
+from oracle.dg_oracle import OracleDG  # noqa: E402
+from golden_util import SMALL_CASES, harness_vectors, load, rebuild, rel  # noqa: E402
+
+STAGE_TOL = 1e-12
+SOL_TOL = 1e-10
+DEV = "cuda:0"
+
+
+def T(a):
+    return torch.tensor(np.asarray(a, dtype=np.float64).ravel(), device=DEV)
+
+
+def N(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.fixture(scope="module", params=list(SMALL_CASES) + ["tri32_c1"])
+def golden(request):
+    d, meta = load(request.param)
+    g, m, el, order = rebuild(meta)
+    opts = meta["opts"]
+    cfg = SolverConfig(eta_e=opts.get("eta_e", 90.0), pre_smooth_its=opts.get("pre_smooth_its", 3),
+                       post_smooth_its=opts.get("post_smooth_its", 3))
+    s = DGSolver(m, order, cfg, el)
+    s.build_operator()
+    return request.param, d, meta, m, el, order, s
+
+
+def _inputs(name, d, m):
+    if "apply_x" in d:
+        return d["apply_x"], d["apply_b"], d["mg_r"], d["pc_r"]
+    return harness_vectors(m)
+
+
+def test_apply_and_smoother(golden):
+    name, d, meta, m, el, order, s = golden
+    x, b, r_cg, rp = _inputs(name, d, m)
+    r = s.residual(T(x), T(b))
+    assert rel(N(r), d["apply_r"]) < STAGE_TOL
+    if "smooth_x" in d:
+        xs = T(x)
+        r2 = s.residual(xs, T(b), smooth=True)
+        if "smooth_r" in d:
+            assert rel(N(r2), d["smooth_r"]) < STAGE_TOL
+        assert rel(N(xs), d["smooth_x"]) < STAGE_TOL
+
+
+def test_block_diagonal(golden):
+    name, d, meta, m, el, order, s = golden
+    if "bdiagK" not in d:
+        pytest.skip("reduced golden case")
+    K, dK = s.bdiag()
+    assert rel(N(K), d["bdiagK"]) < STAGE_TOL
+    assert rel(N(dK), d["diagK"]) < STAGE_TOL
+
+
+def test_rhs(golden):
+    name, d, meta, m, el, order, s = golden
+    if "f" in d:
+        f, g = d["f"], d["g"]
+    else:
+        X = m.x_ref_in
+        f = m.ndim * np.pi ** 2 * np.prod([np.sin(np.pi * X[:, k]) for k in range(m.ndim)], axis=0)
+        g = np.zeros_like(f)
+    b = s.rhs(T(f), T(g))
+    assert rel(N(b), d["rhs"]) < STAGE_TOL
+
+
+def test_rar_vcycle_precond(golden):
+    name, d, meta, m, el, order, s = golden
+    x, b, r_cg, rp = _inputs(name, d, m)
+    assert rel(N(s.rar_values()), d["RARvalues"]) < STAGE_TOL
+    assert rel(N(s.mg_vcycle(T(r_cg))), d["mg_e"]) < STAGE_TOL
+    assert rel(N(s.precond(T(rp))), d["pc_x"]) < STAGE_TOL
+
+
+def test_gmres_matches_reference(golden):
+    name, d, meta, m, el, order, s = golden
+    opts = meta["opts"]
+    bt = T(d["rhs"])
+    tol = opts.get("rtol", 1e-10) * float(np.linalg.norm(d["rhs"]))
+    xt = torch.zeros_like(bt)
+    its, res = s.gmres(xt, bt, tol, m=opts.get("gmres_m", 30), max_its=opts.get("gmres_its", 400))
+    assert its == int(d["its"])
+    assert res <= tol
+    assert rel(N(xt), d["x_solution"]) < SOL_TOL
+
+
+@pytest.fixture(scope="module")
+def tet8():
+    m = mesh.build_mesh("tet", 8, seed=3)
+    order = sfc.hilbert_sfc_order(m.cg_coords)
+    el = element.p3_element(3)
+    s = DGSolver(m, order, SolverConfig(), el)
+    s.build_operator()
+    O = OracleDG(m, el, element.drst_duv(3))
+    return m, order, s, O
+
+
+def test_tet8_against_oracle(tet8):
+    m, order, s, O = tet8
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(s.nonods)
+    b = rng.standard_normal(s.nonods)
+    assert rel(N(s.residual(T(x), T(b))), O.residual(x, b)) < STAGE_TOL
+    ctx = O.setup(order)
+    assert rel(N(s.rar_values()), ctx["rar"]) < STAGE_TOL
+    assert rel(N(s.precond(T(b))), O.precond(b, ctx)) < 1e-11
+
+
+def test_kappa_operator_against_oracle(tet8):
+    m, order, s0, _ = tet8
+    rng = np.random.default_rng(5)
+    kappa = np.exp(rng.standard_normal(m.nele))
+    el = element.p3_element(3)
+    s = DGSolver(m, order, SolverConfig(), el)
+    s.set_kappa(kappa)
+    s.build_operator()
+    O = OracleDG(m, el, element.drst_duv(3), kappa=kappa)
+    x = rng.standard_normal(s.nonods)
+    b = rng.standard_normal(s.nonods)
+    assert rel(N(s.residual(T(x), T(b))), O.residual(x, b)) < STAGE_TOL
+    K, _ = s.bdiag()
+    assert rel(N(K), O.bdiag()[0]) < STAGE_TOL
+
+
+def test_operator_symmetry_and_zero_input(tet8):
+    m, order, s, O = tet8
+    rng = np.random.default_rng(2)
+    x = T(rng.standard_normal(s.nonods))
+    y = T(rng.standard_normal(s.nonods))
+    xAy = float(torch.dot(x, s.apply(y)))
+    yAx = float(torch.dot(y, s.apply(x)))
+    assert abs(xAy - yAx) <= 1e-12 * abs(xAy)
+    z = torch.zeros(s.nonods, dtype=torch.float64, device=DEV)
+    assert float(torch.abs(s.apply(z)).max()) == 0.0
