@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--smooth", type=int, default=2, help="V(s,s) smoothing steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-roofline", action="store_true", help="skip the isolated apply timing")
     return ap.parse_args()
 
 
@@ -276,6 +278,13 @@ def run_ours(args):
     err_inf = float(np.abs(x.cpu().numpy() - u).max())
 
     # end to end through the public solve() with pinned host buffers
+    if args.no_e2e:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "DOF/s", "ms_per_step": t_ms / args.steps,
+                              "its": its_list, "rel_residual": rel_res, "gpu_launches": launches}))
+        return
     f_host = torch.tensor(f, dtype=torch.float64).pin_memory()
     x_host = torch.empty(dofs, dtype=torch.float64).pin_memory()
     for _ in range(1):

@@ -281,22 +281,54 @@ __global__ void __launch_bounds__(N* N) build_blocks_kernel(BuildParams p) {
 }
 
 // ---------------------------------------------------------------------------
+// Smoother matrix.  The reference smooths with three point-Jacobi sweeps on
+// each element block, c <- c + w D^-1 (r - A_ee c) from c = 0, then
+// x += w c (z06/volume_mf_diff.py:474-480).  That is the fixed linear map
+// x += W_e r with W_e = w^2 (I + G + G^2) D^-1, G = I - w D^-1 A_ee, which is
+// formed once per operator here (one CTA per element, N*N threads) and
+// stored column-major like the blocks.
+template <int N, int F>
+__global__ void __launch_bounds__(N* N) smoother_matrix_kernel(const double* __restrict__ blk,
+                                                               double* __restrict__ W, int64_t B,
+                                                               double w) {
+  __shared__ double G[N][N];
+  __shared__ double G2[N][N];
+  __shared__ double dinv[N];
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int m = tid % N, n = tid / N;                 // entry (m, n)
+  const double* A = blk + (size_t)e * (F + 1) * N * N; // A(m, n) at [n*N + m]
+  if (tid < N) dinv[tid] = 1.0 / A[tid * N + tid];
+  __syncthreads();
+  G[m][n] = (m == n ? 1.0 : 0.0) - w * dinv[m] * A[n * N + m];
+  __syncthreads();
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < N; ++k) s += G[m][k] * G[k][n];
+  G2[m][n] = s;
+  __syncthreads();
+  const double poly = (m == n ? 1.0 : 0.0) + G[m][n] + G2[m][n];
+  W[(size_t)e * N * N + n * N + m] = w * w * poly * dinv[n];
+}
+
+// ---------------------------------------------------------------------------
 // Residual / smoother: EPB elements per CTA, one thread per (element, row).
 //   res = b - A x            (b = 0 when null; x = 0 when ZEROX)
 //   r  <- sgn * res          (when r != null)
-//   SMOOTH: c = 3 Jacobi sweeps on A_ee c = res; x_out = x + w c
+//   SMOOTH: x_out = x + W_e res  (the three-sweep block-Jacobi step)
 enum { RF_ZEROX = 1, RF_SMOOTH = 2, RF_NEG = 4 };
 
 template <int N, int F, int EPB>
 __global__ void __launch_bounds__(EPB* N) residual_kernel(const double* __restrict__ blk,
+                                                          const double* __restrict__ W,
                                                           const int* __restrict__ nbe,
                                                           const double* __restrict__ x,
                                                           const double* __restrict__ b,
                                                           double* __restrict__ r,
                                                           double* __restrict__ x_out, int64_t B,
-                                                          double w, int flags) {
+                                                          int flags) {
   __shared__ double xs[EPB][F + 1][N];
-  __shared__ double cs[EPB][N];
+  __shared__ double rs[EPB][N];
   __shared__ int nbs[EPB][F];
   const int le = threadIdx.x / N, m = threadIdx.x % N;
   const int64_t e = (int64_t)blockIdx.x * EPB + le;
@@ -314,24 +346,16 @@ __global__ void __launch_bounds__(EPB* N) residual_kernel(const double* __restri
   }
   __syncthreads();
   double acc = 0.0;
-  double aee[N];
   const double* A = blk + (size_t)e * (F + 1) * N * N;
-  const bool smooth = flags & RF_SMOOTH;
-  if (valid) {
-    if (!zerox || smooth) {
+  if (valid && !zerox) {
 #pragma unroll
-      for (int n = 0; n < N; ++n) aee[n] = A[n * N + m];
-    }
-    if (!zerox) {
+    for (int n = 0; n < N; ++n) acc += A[n * N + m] * xs[le][0][n];
 #pragma unroll
-      for (int n = 0; n < N; ++n) acc += aee[n] * xs[le][0][n];
+    for (int f = 0; f < F; ++f) {
+      if (nbs[le][f] >= 0) {
+        const double* Af = A + (size_t)(1 + f) * N * N;
 #pragma unroll
-      for (int f = 0; f < F; ++f) {
-        if (nbs[le][f] >= 0) {
-          const double* Af = A + (size_t)(1 + f) * N * N;
-#pragma unroll
-          for (int n = 0; n < N; ++n) acc += Af[n * N + m] * xs[le][1 + f][n];
-        }
+        for (int n = 0; n < N; ++n) acc += Af[n * N + m] * xs[le][1 + f][n];
       }
     }
   }
@@ -340,27 +364,16 @@ __global__ void __launch_bounds__(EPB* N) residual_kernel(const double* __restri
     res = (b ? b[e * N + m] : 0.0) - acc;
     if (r) r[e * N + m] = (flags & RF_NEG) ? -res : res;
   }
-  if (smooth) {
-    // three point-Jacobi sweeps on the element block (volume_mf_diff.py:474-480)
-    double dgm = valid ? aee[0] : 1.0;
+  if (flags & RF_SMOOTH) {
+    rs[le][m] = res;
+    __syncthreads();
+    if (valid) {
+      const double* We = W + (size_t)e * N * N;
+      double c = 0.0;
 #pragma unroll
-    for (int n = 0; n < N; ++n)
-      if (n == m) dgm = aee[n];
-    double c = 0.0;
-    cs[le][m] = 0.0;
-    for (int it = 0; it < 3; ++it) {
-      __syncthreads();
-      double s = 0.0;
-      if (valid) {
-#pragma unroll
-        for (int n = 0; n < N; ++n) s += aee[n] * cs[le][n];
-      }
-      double cn = c + w * (res - s) / dgm;
-      __syncthreads();
-      cs[le][m] = cn;
-      c = cn;
+      for (int n = 0; n < N; ++n) c += We[n * N + m] * rs[le][n];
+      x_out[e * N + m] = (zerox ? 0.0 : xs[le][0][m]) + c;
     }
-    if (valid) x_out[e * N + m] = (zerox ? 0.0 : xs[le][0][m]) + w * c;
   }
 }
 

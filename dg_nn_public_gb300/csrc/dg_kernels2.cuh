@@ -179,16 +179,23 @@ __global__ void rar_scatter_kernel(double* __restrict__ value, const double* __r
 // ---------------------------------------------------------------------------
 // SFC levels (multigrid_linearelastic.py:25-172)
 
-// rr = b - A e_in;  e_out = e_in + w * rr / diag   (mg_smooth_one_level)
+// rr = b - A e_in;  e_out = e_in + w * rr / diag   (mg_smooth_one_level).
+// LPR lanes share a row (strided over its entries, shuffle-reduced) so the
+// dependent loads of a row are spread over lanes instead of chained.
+constexpr int LPR = 8;
 __global__ void lev_jacobi_kernel(const int* __restrict__ rowptr, const int* __restrict__ col,
                                   const double* __restrict__ val, const double* __restrict__ diag,
                                   const double* __restrict__ e_in, const double* __restrict__ b,
                                   double* __restrict__ e_out, double* __restrict__ rr_out, int n,
                                   double w) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / LPR, lane = t % LPR;
   double s = 0.0;
-  for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += val[k] * e_in[col[k]];
+  if (i < n)
+    for (int k = rowptr[i] + lane; k < rowptr[i + 1]; k += LPR) s += val[k] * e_in[col[k]];
+#pragma unroll
+  for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
+  if (i >= n || lane != 0) return;
   const double rr = b[i] - s;
   e_out[i] = e_in[i] + rr / diag[i] * w;
   if (rr_out) rr_out[i] = rr;
@@ -332,6 +339,159 @@ __global__ void combine_kernel(const double* __restrict__ V, int64_t ld, int nv,
   double s = 0.0;
   for (int i = 0; i < nv; ++i) s += V[i * ld + k] * y[i];
   x[k] += s;
+}
+
+}  // namespace dg
+
+namespace dg {
+
+// ---------------------------------------------------------------------------
+// Whole SFC V-cycle in one launch on a thread-block cluster.  Each CTA owns
+// a contiguous slice of every level's rows; phases are separated by cluster
+// barriers (the CTAs of a cluster are co-resident, so the barrier cannot
+// wait on an unscheduled block).  Values written by other CTAs of the
+// cluster are read with L2-coherent loads.  Semantics are those of
+// vcycle() in the host driver (multigrid_linearelastic.py:112-172).
+struct VLevel {
+  const int* rowptr;
+  const int* col;
+  const double* val;
+  const double* diag;
+  const int* up;    // into the next coarser level (levels above the top)
+  double* e;
+  double* e2;
+  double* r;
+  double* rr;
+  int n;
+};
+
+constexpr int VMAXLEV = 40;
+
+struct VCycleParams {
+  VLevel lev[VMAXLEV];
+  int nlevel;
+  int pre, post;
+  double w;
+  const double* r_in;   // level-0 right-hand side (curve order)
+  double* e_out;        // level-0 result
+};
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ unsigned cluster_size() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;\n" : "=r"(r));
+  return r;
+}
+
+// rows [lo, hi) of a level owned by this CTA
+__device__ __forceinline__ void slice(int n, unsigned rank, unsigned ncta, int& lo, int& hi) {
+  long long per = ((long long)n + ncta - 1) / ncta;
+  lo = (int)min((long long)n, per * rank);
+  hi = (int)min((long long)n, per * (rank + 1));
+}
+
+__device__ __forceinline__ void vjacobi(const VLevel& L, const double* e_in, const double* b, double* e_out,
+                                        double* rr_out, int lo, int hi, double w) {
+  const int lane = threadIdx.x % LPR;
+  const int groups = blockDim.x / LPR;
+  // whole warps iterate together so the shuffles see converged lanes
+  for (int base = lo; base < hi; base += groups) {
+    const int i = base + (int)threadIdx.x / LPR;
+    double s = 0.0;
+    if (i < hi) {
+      const int k1 = __ldg(L.rowptr + i + 1);
+      for (int k = __ldg(L.rowptr + i) + lane; k < k1; k += LPR)
+        s += __ldg(L.val + k) * __ldcg(e_in + __ldg(L.col + k));
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
+    if (i < hi && lane == 0) {
+      const double rr = __ldcg(b + i) - s;
+      e_out[i] = __ldcg(e_in + i) + rr / __ldg(L.diag + i) * w;
+      if (rr_out) rr_out[i] = rr;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(1024) vcycle_cluster_kernel(VCycleParams p) {
+  const unsigned rank = cluster_rank(), ncta = cluster_size();
+  const int top = p.nlevel - 1;
+  int lo, hi;
+  // level 0 input, zero initial error
+  {
+    const VLevel& L = p.lev[0];
+    slice(L.n, rank, ncta, lo, hi);
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      L.r[i] = __ldcg(p.r_in + i);
+      L.e[i] = 0.0;
+    }
+  }
+  cluster_barrier();
+  for (int l = 0; l < top; ++l) {
+    const VLevel& L = p.lev[l];
+    slice(L.n, rank, ncta, lo, hi);
+    double* ea = L.e;
+    double* eb = L.e2;
+    for (int it = 0; it < p.pre; ++it) {
+      vjacobi(L, ea, L.r, eb, nullptr, lo, hi, p.w);
+      cluster_barrier();
+      double* t = ea; ea = eb; eb = t;
+    }
+    // the residual-forming smoothing call also updates e (reference quirk)
+    vjacobi(L, ea, L.r, eb, L.rr, lo, hi, p.w);
+    cluster_barrier();
+    // the final error of this level lives in eb; remember it for the way up
+    const VLevel& Nx = p.lev[l + 1];
+    int clo, chi;
+    slice(Nx.n, rank, ncta, clo, chi);
+    for (int i = clo + threadIdx.x; i < chi; i += blockDim.x) {
+      const int a = 2 * i, b2 = 2 * i + 1;
+      Nx.r[i] = __ldcg(L.rr + a) + (b2 < L.n ? __ldcg(L.rr + b2) : 0.0);
+      Nx.e[i] = __ldcg(eb + a) + (b2 < L.n ? __ldcg(eb + b2) : 0.0);
+    }
+    // copy the level's current error into L.e when it sits in e2
+    if (eb != L.e)
+      for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) L.e[i] = __ldcg(eb + i);
+    cluster_barrier();
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    const VLevel& T = p.lev[top];
+    T.e[0] = __ldcg(T.r) / __ldg(T.val);
+  }
+  cluster_barrier();
+  for (int l = top - 1; l >= 0; --l) {
+    const VLevel& L = p.lev[l];
+    const VLevel& Nx = p.lev[l + 1];
+    slice(L.n, rank, ncta, lo, hi);
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) L.e[i] = __ldcg(L.e + i) + __ldcg(Nx.e + __ldg(L.up + i));
+    cluster_barrier();
+    double* ea = L.e;
+    double* eb = L.e2;
+    for (int it = 0; it < p.post; ++it) {
+      vjacobi(L, ea, L.r, eb, nullptr, lo, hi, p.w);
+      cluster_barrier();
+      double* t = ea; ea = eb; eb = t;
+    }
+    if (ea != L.e) {
+      for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) L.e[i] = __ldcg(ea + i);
+      cluster_barrier();
+    }
+  }
+  if (p.e_out) {
+    const VLevel& L = p.lev[0];
+    slice(L.n, rank, ncta, lo, hi);
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) p.e_out[i] = __ldcg(L.e + i);
+  }
 }
 
 }  // namespace dg

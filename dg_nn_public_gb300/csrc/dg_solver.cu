@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -54,6 +55,7 @@ struct dg_ctx {
   double* d_kappa = nullptr;
   Tables T{};
   double* d_blk = nullptr;
+  double* d_W = nullptr;        // (B, N, N) smoother matrices
   double* d_detw = nullptr;
   int* d_err = nullptr;
   // boundary faces for the right-hand side
@@ -82,6 +84,14 @@ struct dg_ctx {
          *d_scal = nullptr;
   int nred = 0;
   bool built = false;
+  // SFC V-cycle as one thread-block-cluster kernel (0 = per-level launches)
+  int vc_cluster = 0;
+  // captured Arnoldi cycle (GMRES(m) inner loop) replayed as one CUDA graph
+  bool use_graph = true;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t arnoldi_exec = nullptr;
+  int arnoldi_m = 0;
+  const double* arnoldi_vptr = nullptr;
 };
 
 namespace {
@@ -162,6 +172,9 @@ int launch_build(dg_ctx* c, cudaStream_t st) {
   CK(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm)));
   if (c->B > 0) k<<<(unsigned)c->B, E::N * E::N, sizeof(Sm), st>>>(p);
   bump();
+  if (c->B > 0) smoother_matrix_kernel<E::N, E::F><<<(unsigned)c->B, E::N * E::N, 0, st>>>(
+      c->d_blk, c->d_W, c->B, c->cfg.jac_wei);
+  bump();
   CKL(c);
   if (c->nbf > 0) {
     BFaceParams q;
@@ -187,7 +200,7 @@ int launch_residual(dg_ctx* c, const double* x, const double* b, double* r, doub
   using E = Elem<D>;
   unsigned g = nblk(c->B, E::EPB);
   if (g) residual_kernel<E::N, E::F, E::EPB><<<g, E::EPB * E::N, 0, st>>>(
-      c->d_blk, c->d_nbe, x, b, r, x_out, c->B, c->cfg.jac_wei, flags);
+      c->d_blk, c->d_W, c->d_nbe, x, b, r, x_out, c->B, flags);
   bump();
   CKL(c);
   return DG_OK;
@@ -230,8 +243,73 @@ int prolong_cg(dg_ctx* c, double* x, const double* ecg, bool sfc_order, int colo
                    : launch_prolong<2>(c, x, ecg, sfc_order, color, add, st);
 }
 
+// Pick the cluster size for the one-launch V-cycle (16 if the device can
+// co-schedule it, else 8, else 0 = fall back to per-level launches).
+void choose_vcycle_cluster(dg_ctx* c) {
+  c->vc_cluster = 0;
+  if ((int)c->lev.size() > VMAXLEV) return;
+  // Default off: inside the captured GMRES cycle the per-level launches
+  // (~0.9 us apart) beat the one-launch cluster V-cycle, whose row sweeps on
+  // 16 SMs are latency-bound.  DG_VCYCLE_CLUSTER=16|8 selects it.
+  const char* env = std::getenv("DG_VCYCLE_CLUSTER");
+  int want[2] = {0, 0};
+  if (env && env[0]) want[0] = std::atoi(env);
+  cudaFuncSetAttribute(vcycle_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  for (int cs : want) {
+    if (cs <= 0) continue;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs, 1, 1);
+    cfg.blockDim = dim3(1024, 1, 1);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, vcycle_cluster_kernel, &cfg) == cudaSuccess && nclusters > 0) {
+      c->vc_cluster = cs;
+      break;
+    }
+    cudaGetLastError();
+  }
+}
+
+int vcycle_cluster(dg_ctx* c, const double* r_sfc, cudaStream_t st) {
+  VCycleParams p;
+  p.nlevel = (int)c->lev.size();
+  for (int l = 0; l < p.nlevel; ++l) {
+    const DevLevel& L = c->lev[l];
+    p.lev[l] = VLevel{L.rowptr, L.col, L.val, L.diag, L.up, L.e, L.e2, L.r, L.rr, L.n};
+  }
+  p.pre = c->cfg.pre_smooth_its;
+  p.post = c->cfg.post_smooth_its;
+  p.w = c->cfg.jac_wei;
+  p.r_in = r_sfc;
+  p.e_out = nullptr;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(c->vc_cluster, 1, 1);
+  cfg.blockDim = dim3(1024, 1, 1);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = c->vc_cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  CK(c, cudaLaunchKernelEx(&cfg, vcycle_cluster_kernel, p));
+  bump();
+  return DG_OK;
+}
+
 // One SFC V-cycle; r_sfc is level-0 input, result left in lev[0].e
 int vcycle(dg_ctx* c, const double* r_sfc, cudaStream_t st) {
+  if (c->vc_cluster > 0) {
+    if (c->lev.back().n != 1) return fail(c, DG_ERR_STATE, "coarsest SFC level must hold one node");
+    return vcycle_cluster(c, r_sfc, st);
+  }
   const int nl = (int)c->lev.size();
   const int top = nl - 1;
   const double w = c->cfg.jac_wei;
@@ -241,13 +319,13 @@ int vcycle(dg_ctx* c, const double* r_sfc, cudaStream_t st) {
   for (int l = 0; l < top; ++l) {
     DevLevel& L = c->lev[l];
     for (int it = 0; it < c->cfg.pre_smooth_its; ++it) {
-      lev_jacobi_kernel<<<nblk(L.n, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r, L.e2,
-                                                       nullptr, L.n, w); bump();
+      lev_jacobi_kernel<<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r,
+                                                                      L.e2, nullptr, L.n, w); bump();
       std::swap(L.e, L.e2);
     }
     // the residual-forming call also updates e in place (reference quirk)
-    lev_jacobi_kernel<<<nblk(L.n, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r, L.e2, L.rr,
-                                                     L.n, w); bump();
+    lev_jacobi_kernel<<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r,
+                                                                    L.e2, L.rr, L.n, w); bump();
     std::swap(L.e, L.e2);
     DevLevel& Nx = c->lev[l + 1];
     lev_restrict_kernel<<<nblk(Nx.n, TB), TB, 0, st>>>(L.rr, L.e, Nx.r, Nx.e, L.n, Nx.n); bump();
@@ -261,8 +339,8 @@ int vcycle(dg_ctx* c, const double* r_sfc, cudaStream_t st) {
     DevLevel& L = c->lev[l];
     lev_prolong_kernel<<<nblk(L.n, TB), TB, 0, st>>>(L.e, c->lev[l + 1].e, L.up, L.n); bump();
     for (int it = 0; it < c->cfg.post_smooth_its; ++it) {
-      lev_jacobi_kernel<<<nblk(L.n, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r, L.e2,
-                                                       nullptr, L.n, w); bump();
+      lev_jacobi_kernel<<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r,
+                                                                      L.e2, nullptr, L.n, w); bump();
       std::swap(L.e, L.e2);
     }
   }
@@ -372,6 +450,47 @@ int cgs2(dg_ctx* c, int j, double* z, int m, cudaStream_t st) {
   return DG_OK;
 }
 
+// The m Arnoldi steps of one GMRES cycle (V[0] already set): w = A v_j,
+// r = M^-1 w, CGS2 against V[0..j], V[j+1] = r / ||r||.
+int arnoldi_steps(dg_ctx* c, int m, cudaStream_t st) {
+  int rc;
+  double* r = c->d_t1;
+  double* w = c->d_t2;
+  for (int j = 0; j < m; ++j) {
+    if ((rc = residual(c, c->d_V + (size_t)j * c->nonods, nullptr, w, nullptr, RF_NEG, st))) return rc;
+    if ((rc = precond(c, w, r, st))) return rc;
+    if ((rc = cgs2(c, j, r, m, st))) return rc;
+  }
+  return DG_OK;
+}
+
+int run_arnoldi(dg_ctx* c, int m, cudaStream_t st) {
+  if (!c->use_graph) return arnoldi_steps(c, m, st);
+  if (!c->arnoldi_exec || c->arnoldi_m != m || c->arnoldi_vptr != c->d_V) {
+    if (c->arnoldi_exec) {
+      cudaGraphExecDestroy(c->arnoldi_exec);
+      c->arnoldi_exec = nullptr;
+    }
+    if (!c->cap_stream) CK(c, cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    CK(c, cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
+    int rc = arnoldi_steps(c, m, c->cap_stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(c->cap_stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ee != cudaSuccess) return fail(c, DG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
+    cudaError_t ie = cudaGraphInstantiate(&c->arnoldi_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return fail(c, DG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    c->arnoldi_m = m;
+    c->arnoldi_vptr = c->d_V;
+  }
+  CK(c, cudaGraphLaunch(c->arnoldi_exec, st));
+  return DG_OK;
+}
+
 // least squares min || beta e1 - H y || by Givens rotations (host, FP64)
 bool solve_hessenberg(const std::vector<double>& Hcm, int m, double beta, std::vector<double>& y) {
   // Hcm column-major (m+1) x m
@@ -427,6 +546,8 @@ void dg_destroy(dg_ctx* ctx) {
   int cur = 0;
   cudaGetDevice(&cur);
   cudaSetDevice(ctx->dev);
+  if (ctx->arnoldi_exec) cudaGraphExecDestroy(ctx->arnoldi_exec);
+  if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
   for (void* p : ctx->allocs) cudaFree(p);
   cudaSetDevice(cur);
   delete ctx;
@@ -465,6 +586,10 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
   cudaDeviceProp prop;
   CK(c.get(), cudaGetDeviceProperties(&prop, c->dev));
   c->nsm = prop.multiProcessorCount;
+  {
+    const char* ng = std::getenv("DG_NO_GRAPH");
+    c->use_graph = !(ng && ng[0] && ng[0] != '0');
+  }
   c->nred = 2 * c->nsm;
   const int64_t nf = c->B * F;
   // face arrays
@@ -533,6 +658,7 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     c->T.align = q;
   }
   if ((rc = dalloc(c.get(), &c->d_blk, (size_t)c->B * (F + 1) * N * N))) return rc;
+  if ((rc = dalloc(c.get(), &c->d_W, (size_t)c->B * N * N))) return rc;
   if ((rc = dalloc(c.get(), &c->d_detw, (size_t)c->B * VG))) return rc;
   if ((rc = dalloc(c.get(), &c->d_err, 1))) return rc;
   CK(c.get(), cudaMemset(c->d_err, 0, sizeof(int)));
@@ -677,6 +803,7 @@ int dg_build_operator(dg_ctx* c, void* stream) {
       }
     }
   }
+  choose_vcycle_cluster(c);
   for (int l = 0; l < h.nlevel; ++l) {
     DevLevel& L = c->lev[l];
     int64_t r0 = h.start[l];
@@ -847,12 +974,8 @@ int dg_gmres(dg_ctx* c, double* x, const double* b, double tol, int32_t m, int32
     }
     scale_kernel<<<nblk(c->nonods, 256), 256, 0, st>>>(r, c->d_scal, c->d_V, c->nonods); bump();
     CKL(c);
-    for (int j = 0; j < m; ++j) {
-      if ((rc = residual(c, c->d_V + (size_t)j * c->nonods, nullptr, w, nullptr, RF_NEG, st))) return rc;  // w = A v
-      if ((rc = precond(c, w, r, st))) return rc;
-      if ((rc = cgs2(c, j, r, m, st))) return rc;
-      ++its;
-    }
+    if ((rc = run_arnoldi(c, m, st))) return rc;
+    its += m;
     CK(c, cudaMemcpyAsync(Hh.data(), c->d_H, sizeof(double) * Hh.size(), cudaMemcpyDeviceToHost, st));
     CK(c, cudaStreamSynchronize(st));
     if (!solve_hessenberg(Hh, m, beta, y)) {

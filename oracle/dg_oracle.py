@@ -426,6 +426,40 @@ class OracleDG:
             hist.append((its, r0l2))
         return x, its, hist
 
+    def cg_mg(self, b, ctx, tol, max_its):
+        """Preconditioned CG with the multigrid preconditioner (volume_mf_diff.py:1875-1931)."""
+        b = np.asarray(b, dtype=np.float64).reshape(-1)
+        x = np.zeros_like(b)
+        r = self.residual(x, b).reshape(-1)
+        z = self.precond(r, ctx).reshape(-1)
+        p = z.copy()
+        its, r0l2 = 0, 1.0
+        while r0l2 > tol and its < max_its:
+            Ap = self.apply_Ax(p).reshape(-1)
+            rz = r @ z
+            alpha = rz / (Ap @ p)
+            x = x + alpha * p
+            r = r - alpha * Ap
+            z = self.precond(r, ctx).reshape(-1)
+            r0l2 = np.linalg.norm(r)
+            beta = (r @ z) / rz
+            p = beta * p + z
+            its += 1
+        return x, its
+
+    def mg_solve(self, b, ctx, tol, max_its):
+        """Multigrid as a stand-alone iteration (volume_mf_diff.py:1844-1873)."""
+        b = np.asarray(b, dtype=np.float64).reshape(-1)
+        x = np.zeros_like(b)
+        r = self.residual(x, b).reshape(-1)
+        its, r0l2 = 0, 1.0
+        while r0l2 > tol and its < max_its:
+            x = x + self.precond(r, ctx).reshape(-1)
+            r = self.residual(x, b).reshape(-1)
+            r0l2 = np.linalg.norm(r)
+            its += 1
+        return x, its
+
     def l2_error(self, x, u):
         """get_l2_error (volume_mf_diff.py:2032-2056): sum_n sum_g (phi_n (x_n - u_n))^2 w|J|."""
         d = (np.asarray(x) - np.asarray(u)).reshape(self.B, self.N)
