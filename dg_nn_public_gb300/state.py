@@ -21,7 +21,7 @@ from .mesh import DGMesh
 from .solver import DGSolver, SolverConfig
 
 # knob names and defaults of z06/config.py:103-149, 207, 245 -- with the
-# spec solver selection (GMRES + SFC multigrid, eta = 10 p^2)
+# benchmark solver selection (GMRES + SFC multigrid, eta = 10 p^2)
 config = types.SimpleNamespace(
     linear_solver="gmres-mg", tol=1.0e-9, jac_its=500, jac_wei=2.0 / 3.0,
     pre_smooth_its=3, post_smooth_its=3, mg_opt_D=2, gmres_m=30, gmres_its=400,

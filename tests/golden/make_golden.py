@@ -36,6 +36,9 @@ CASES = {
     "tet2_sin": ("tet", 2, dict(problem="sin", gmres_its=90)),
     "tet3_v22": ("tet", 3, dict(problem="sin", pre_smooth_its=2, post_smooth_its=2, gmres_its=120)),
     "tri32_c1": ("tri", 32, dict(problem="sin", gmres_its=400, full=False)),
+    # the 3D benchmark mesh: about 40 minutes of reference CPU time
+    "tet20_c2_summary": ("tet", 20, dict(problem="sin", pre_smooth_its=2, post_smooth_its=2, gmres_its=400,
+                                         apply_reps=4, summary=True)),
 }
 
 FULL_KEYS_SKIP = ()
@@ -55,9 +58,11 @@ def array_digest(a) -> str:
 
 
 def run_case(name: str) -> str:
+    """Run the reference on one case and store its golden file."""
     kind, n, opts = CASES[name]
     opts = dict(opts)
     full = opts.pop("full", True)
+    summary = opts.pop("summary", False)
     g = dgmesh.unit_square_tri_mesh(n) if kind == "tri" else dgmesh.unit_cube_kuhn_mesh(n)
     m = dgmesh.ingest(g)
     order = dgsfc.hilbert_sfc_order(m.cg_coords)
@@ -72,6 +77,8 @@ def run_case(name: str) -> str:
     raw = os.path.join(work, "out.npz")
     subprocess.run([sys.executable, "-m", "oracle.refrun.run_reference", mp, sp, raw, op],
                    cwd=REPO, check=True, stdout=subprocess.DEVNULL)
+    if summary:
+        return c2_summary(raw, name)
     d = dict(np.load(raw))
     meta = dict(kind=kind, n=n, seed=0, opts=opts, full=full)
     if full:
@@ -85,7 +92,36 @@ def run_case(name: str) -> str:
     return out
 
 
+
+def c2_summary(raw_npz: str, out_name: str = "tet20_c2_summary") -> str:
+    """Compact record of the reference's full 3D benchmark solve (48,000 P3
+    tets, 960,000 DOFs, V(2,2), GMRES(30), rtol 1e-10): every 97th entry of
+    the solution and of the residual of the harness vectors, norms and the
+    residual history.  raw_npz is the output of oracle/refrun/run_reference.py
+    for that mesh (options pre_smooth_its = post_smooth_its = 2)."""
+    d = dict(np.load(raw_npz))
+    keep = {
+        "x_sub": d["x_solution"][::97].copy(), "x_norm": np.linalg.norm(d["x_solution"]),
+        "x_sum": d["x_solution"].sum(), "apply_r_sub": d["apply_r"][::97].copy(),
+        "rar_sub": d["RARvalues"][::7].copy(), "its": d["its"], "res_hist": d["res_hist"],
+        "l2err": d["l2err"], "linferr": d["linferr"], "t_apply": d["t_apply"], "t_solve": d["t_solve"],
+        "t_rar": d["t_rar"], "t_precond": d["t_precond"], "threads": d["threads"],
+        "rhs_norm": np.linalg.norm(d["rhs"]), "nodes_per_level": d["nodes_per_level"],
+        "ncolor": d["ncolor"],
+    }
+    meta = dict(kind="tet", n=20, seed=0, opts=dict(pre_smooth_its=2, post_smooth_its=2, gmres_its=400),
+                full=False, stride_x=97, stride_rar=7)
+    keep["meta_json"] = np.asarray(json.dumps(meta))
+    out = os.path.join(HERE, out_name + ".npz")
+    np.savez_compressed(out, **keep)
+    return out
+
+
 if __name__ == "__main__":
-    names = sys.argv[1:] or list(CASES)
-    for nm in names:
-        print("generated", run_case(nm))
+    args = sys.argv[1:]
+    if args[:1] == ["--c2-summary"]:
+        # args[1]: output of oracle/refrun/run_reference.py for the 20^3 Kuhn mesh
+        print("generated", c2_summary(args[1]))
+    else:
+        for nm in args or list(CASES):
+            print("generated", run_case(nm))
