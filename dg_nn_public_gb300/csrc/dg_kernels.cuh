@@ -9,6 +9,7 @@
 // threads of an element (one per row m) read a column with one coalesced
 // 8*N-byte access.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -311,24 +312,73 @@ __global__ void __launch_bounds__(N* N) smoother_matrix_kernel(const double* __r
   W[(size_t)e * N * N + n * N + m] = w * w * poly * dinv[n];
 }
 
+// Damped block inverse W_e = w A_ee^{-1} (the mixed preconditioner's
+// smoother option), stored column-major like the blocks.  Gauss-Jordan in
+// FP64 without pivoting: A_ee is symmetric positive definite for a
+// sufficient penalty, so every pivot is positive (a non-positive pivot sets
+// the error word and leaves W_e as the Jacobi inverse of the diagonal).
+template <int N, int F>
+__global__ void __launch_bounds__(N* N) block_inverse_kernel(const double* __restrict__ blk,
+                                                             double* __restrict__ W, int64_t B, double w,
+                                                             int* err) {
+  __shared__ double a[N][N + 1];
+  __shared__ double inv[N][N + 1];
+  __shared__ int bad;
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x;
+  const int m = tid % N, n = tid / N;
+  const double* A = blk + (size_t)e * (F + 1) * N * N;
+  a[m][n] = A[n * N + m];
+  inv[m][n] = (m == n) ? 1.0 : 0.0;
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  for (int k = 0; k < N; ++k) {
+    const double piv = a[k][k];
+    if (!(piv > 0.0)) {
+      if (tid == 0) bad = 1;
+      break;   // uniform: every thread reads the same pivot
+    }
+    const double fm = a[m][k] / piv;   // factor of row m
+    const double akn = a[k][n], ikn = inv[k][n];
+    __syncthreads();
+    if (m == k) {
+      a[m][n] = akn / piv;
+      inv[m][n] = ikn / piv;
+    } else {
+      a[m][n] -= fm * akn;
+      inv[m][n] -= fm * ikn;
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (bad) {
+    if (tid == 0) atomicExch(err, 2);
+    W[(size_t)e * N * N + n * N + m] = (m == n) ? w / A[m * N + m] : 0.0;
+    return;
+  }
+  W[(size_t)e * N * N + n * N + m] = w * inv[m][n];
+}
+
 // ---------------------------------------------------------------------------
 // Residual / smoother: EPB elements per CTA, one thread per (element, row).
 //   res = b - A x            (b = 0 when null; x = 0 when ZEROX)
 //   r  <- sgn * res          (when r != null)
 //   SMOOTH: x_out = x + W_e res  (the three-sweep block-Jacobi step)
-enum { RF_ZEROX = 1, RF_SMOOTH = 2, RF_NEG = 4 };
+enum { RF_ZEROX = 1, RF_SMOOTH = 2, RF_NEG = 4, RF_RESTRICT = 8 };
 
-template <int N, int F, int EPB>
-__global__ void __launch_bounds__(EPB* N) residual_kernel(const double* __restrict__ blk,
-                                                          const double* __restrict__ W,
+// MT: stored matrix type; VT: vector type; AT: accumulation type.
+template <int N, int F, int EPB, typename MT = double, typename VT = double, typename AT = double>
+__global__ void __launch_bounds__(EPB* N) residual_kernel(const MT* __restrict__ blk,
+                                                          const MT* __restrict__ W,
                                                           const int* __restrict__ nbe,
-                                                          const double* __restrict__ x,
-                                                          const double* __restrict__ b,
-                                                          double* __restrict__ r,
-                                                          double* __restrict__ x_out, int64_t B,
-                                                          int flags) {
-  __shared__ double xs[EPB][F + 1][N];
-  __shared__ double rs[EPB][N];
+                                                          const VT* __restrict__ x,
+                                                          const VT* __restrict__ b,
+                                                          VT* __restrict__ r,
+                                                          VT* __restrict__ x_out, int64_t B,
+                                                          int flags, const double* __restrict__ P = nullptr,
+                                                          VT* __restrict__ r1 = nullptr) {
+  __shared__ AT xs[EPB][F + 1][N];
+  __shared__ AT rs[EPB][N];
   __shared__ int nbs[EPB][F];
   const int le = threadIdx.x / N, m = threadIdx.x % N;
   const int64_t e = (int64_t)blockIdx.x * EPB + le;
@@ -337,42 +387,55 @@ __global__ void __launch_bounds__(EPB* N) residual_kernel(const double* __restri
   if (valid && m < F) nbs[le][m] = nbe[e * F + m];
   __syncthreads();
   if (valid && !zerox) {
-    xs[le][0][m] = x[e * N + m];
+    xs[le][0][m] = (AT)x[e * N + m];
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       int nb = nbs[le][f];
-      xs[le][1 + f][m] = nb >= 0 ? x[(int64_t)nb * N + m] : 0.0;
+      xs[le][1 + f][m] = nb >= 0 ? (AT)x[(int64_t)nb * N + m] : (AT)0;
     }
   }
   __syncthreads();
-  double acc = 0.0;
-  const double* A = blk + (size_t)e * (F + 1) * N * N;
+  AT acc = 0;
+  const MT* A = blk + (size_t)e * (F + 1) * N * N;
   if (valid && !zerox) {
 #pragma unroll
-    for (int n = 0; n < N; ++n) acc += A[n * N + m] * xs[le][0][n];
+    for (int n = 0; n < N; ++n) acc += (AT)A[n * N + m] * xs[le][0][n];
 #pragma unroll
     for (int f = 0; f < F; ++f) {
       if (nbs[le][f] >= 0) {
-        const double* Af = A + (size_t)(1 + f) * N * N;
+        const MT* Af = A + (size_t)(1 + f) * N * N;
 #pragma unroll
-        for (int n = 0; n < N; ++n) acc += Af[n * N + m] * xs[le][1 + f][n];
+        for (int n = 0; n < N; ++n) acc += (AT)Af[n * N + m] * xs[le][1 + f][n];
       }
     }
   }
-  double res = 0.0;
+  AT res = 0;
   if (valid) {
-    res = (b ? b[e * N + m] : 0.0) - acc;
-    if (r) r[e * N + m] = (flags & RF_NEG) ? -res : res;
+    res = (b ? (AT)b[e * N + m] : (AT)0) - acc;
+    if (r) r[e * N + m] = (VT)((flags & RF_NEG) ? -res : res);
+  }
+  if (flags & RF_RESTRICT) {
+    // P3 -> P1 element restriction of the residual (the DG->CG transfer
+    // needs only these ncorner values per element)
+    rs[le][m] = res;
+    __syncthreads();
+    constexpr int NC = F;   // corners = faces for simplices
+    if (valid && m < NC) {
+      AT s = 0;
+#pragma unroll
+      for (int n = 0; n < N; ++n) s += (AT)P[n * NC + m] * rs[le][n];
+      r1[e * NC + m] = (VT)s;
+    }
   }
   if (flags & RF_SMOOTH) {
     rs[le][m] = res;
     __syncthreads();
     if (valid) {
-      const double* We = W + (size_t)e * N * N;
-      double c = 0.0;
+      const MT* We = W + (size_t)e * N * N;
+      AT c = 0;
 #pragma unroll
-      for (int n = 0; n < N; ++n) c += We[n * N + m] * rs[le][n];
-      x_out[e * N + m] = (zerox ? 0.0 : xs[le][0][m]) + c;
+      for (int n = 0; n < N; ++n) c += (AT)We[n * N + m] * rs[le][n];
+      x_out[e * N + m] = (VT)((zerox ? (AT)0 : xs[le][0][m]) + c);
     }
   }
 }

@@ -123,30 +123,46 @@ __global__ void rhs_bface_kernel(const double* __restrict__ sn_tab, const int* _
 // multigrid_linearelastic.py:286-297; sparsity.py:125-165)
 
 // out[pos(i)] = sum over DG copies (e, c) of vertex i of w_ec * sum_n P[n][c] r[e][n]
-template <int N, int NC>
-__global__ void restrict_cg_kernel(const double* __restrict__ r, const double* __restrict__ P,
+template <int N, int NC, typename T = double>
+__global__ void restrict_cg_kernel(const T* __restrict__ r, const double* __restrict__ P,
                                    const int* __restrict__ gptr, const int* __restrict__ gent,
                                    const double* __restrict__ wdg, const int* __restrict__ pos,
-                                   double* __restrict__ out, int ncg) {
+                                   T* __restrict__ out, int ncg) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ncg) return;
-  double acc = 0.0;
+  T acc = 0;
   for (int k = gptr[i]; k < gptr[i + 1]; ++k) {
     const int ent = gent[k];
     const int64_t e = ent / NC;
     const int c = ent % NC;
-    double v = 0.0;
+    T v = 0;
 #pragma unroll
-    for (int n = 0; n < N; ++n) v += P[n * NC + c] * r[e * N + n];
-    acc += wdg[ent] * v;
+    for (int n = 0; n < N; ++n) v += (T)P[n * NC + c] * r[e * N + n];
+    acc += (T)wdg[ent] * v;
+  }
+  out[pos ? pos[i] : i] = acc;
+}
+
+// out[pos(i)] = sum over DG copies (e, c) of vertex i of w_ec * r1[e][c],
+// r1 the P3->P1 element restriction formed by the residual kernel
+template <typename T>
+__global__ void gather_cg_kernel(const T* __restrict__ r1, const int* __restrict__ gptr,
+                                 const int* __restrict__ gent, const double* __restrict__ wdg,
+                                 const int* __restrict__ pos, T* __restrict__ out, int ncg) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncg) return;
+  T acc = 0;
+  for (int k = gptr[i]; k < gptr[i + 1]; ++k) {
+    const int ent = gent[k];
+    acc += (T)wdg[ent] * r1[ent];
   }
   out[pos ? pos[i] : i] = acc;
 }
 
 // x[e][n] (+)= sum_c P[n][c] * w_ec * ecg[idx(p1cg[e][c])]; with whichc set,
 // ecg is the indicator of colour `color` (colour-probe prolongation).
-template <int N, int NC>
-__global__ void prolong_cg_kernel(double* __restrict__ x, const double* __restrict__ ecg,
+template <int N, int NC, typename T = double>
+__global__ void prolong_cg_kernel(T* __restrict__ x, const T* __restrict__ ecg,
                                   const int* __restrict__ pos, const int* __restrict__ p1cg,
                                   const double* __restrict__ wdg, const double* __restrict__ P,
                                   const int* __restrict__ whichc, int color, int64_t B, int add) {
@@ -154,16 +170,16 @@ __global__ void prolong_cg_kernel(double* __restrict__ x, const double* __restri
   if (t >= B * N) return;
   const int64_t e = t / N;
   const int n = t % N;
-  double v = 0.0;
+  T v = 0;
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
     const int vtx = p1cg[e * NC + c];
-    double ev;
+    T ev;
     if (whichc)
-      ev = whichc[vtx] == color ? 1.0 : 0.0;
+      ev = whichc[vtx] == color ? (T)1 : (T)0;
     else
       ev = ecg[pos ? pos[vtx] : vtx];
-    v += P[n * NC + c] * (wdg[e * NC + c] * ev);
+    v += (T)P[n * NC + c] * ((T)wdg[e * NC + c] * ev);
   }
   x[t] = add ? x[t] + v : v;
 }
@@ -183,45 +199,49 @@ __global__ void rar_scatter_kernel(double* __restrict__ value, const double* __r
 // LPR lanes share a row (strided over its entries, shuffle-reduced) so the
 // dependent loads of a row are spread over lanes instead of chained.
 constexpr int LPR = 8;
+template <typename T = double>
 __global__ void lev_jacobi_kernel(const int* __restrict__ rowptr, const int* __restrict__ col,
-                                  const double* __restrict__ val, const double* __restrict__ diag,
-                                  const double* __restrict__ e_in, const double* __restrict__ b,
-                                  double* __restrict__ e_out, double* __restrict__ rr_out, int n,
+                                  const T* __restrict__ val, const T* __restrict__ diag,
+                                  const T* __restrict__ e_in, const T* __restrict__ b,
+                                  T* __restrict__ e_out, T* __restrict__ rr_out, int n,
                                   double w) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / LPR, lane = t % LPR;
-  double s = 0.0;
+  T s = 0;
   if (i < n)
     for (int k = rowptr[i] + lane; k < rowptr[i + 1]; k += LPR) s += val[k] * e_in[col[k]];
 #pragma unroll
   for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
   if (i >= n || lane != 0) return;
-  const double rr = b[i] - s;
-  e_out[i] = e_in[i] + rr / diag[i] * w;
+  const T rr = b[i] - s;
+  e_out[i] = e_in[i] + rr / diag[i] * (T)w;
   if (rr_out) rr_out[i] = rr;
 }
 
 // pair sums with a zero pad (F.pad + Conv1d([1, 1], stride 2), :147-153)
-__global__ void lev_restrict_kernel(const double* __restrict__ rr, const double* __restrict__ e,
-                                    double* __restrict__ r_next, double* __restrict__ e_next,
+template <typename T = double>
+__global__ void lev_restrict_kernel(const T* __restrict__ rr, const T* __restrict__ e,
+                                    T* __restrict__ r_next, T* __restrict__ e_next,
                                     int n, int nn) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nn) return;
   const int a = 2 * i, b = 2 * i + 1;
-  r_next[i] = rr[a] + (b < n ? rr[b] : 0.0);
-  e_next[i] = e[a] + (b < n ? e[b] : 0.0);
+  r_next[i] = rr[a] + (b < n ? rr[b] : (T)0);
+  e_next[i] = e[a] + (b < n ? e[b] : (T)0);
 }
 
 // e_l[i] += e_next[up[i]]  (nn.Upsample nearest, :163-164)
-__global__ void lev_prolong_kernel(double* __restrict__ e, const double* __restrict__ e_next,
+template <typename T = double>
+__global__ void lev_prolong_kernel(T* __restrict__ e, const T* __restrict__ e_next,
                                    const int* __restrict__ up, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) e[i] += e_next[up[i]];
 }
 
 // coarsest level: one node, e = r / a (scipy spsolve on a 1x1 system, :157-160)
-__global__ void lev_coarse_kernel(const double* __restrict__ val, const double* __restrict__ r,
-                                  double* __restrict__ e) {
+template <typename T = double>
+__global__ void lev_coarse_kernel(const T* __restrict__ val, const T* __restrict__ r,
+                                  T* __restrict__ e) {
   if (threadIdx.x == 0 && blockIdx.x == 0) e[0] = r[0] / val[0];
 }
 
@@ -235,110 +255,113 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// partial[blk][i] = sum over this block's slice of V[i] . z   (i < nv)
-template <int TB>
-__global__ void __launch_bounds__(TB) mdot_kernel(const double* __restrict__ V, int64_t ld, int nv,
-                                                  const double* __restrict__ z, int64_t n,
-                                                  double* __restrict__ partial) {
-  __shared__ double red[TB / 32][KMAXV];
-  double acc[KMAXV];
-#pragma unroll
-  for (int i = 0; i < KMAXV; ++i) acc[i] = 0.0;
-  for (int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x; k < n; k += (int64_t)gridDim.x * TB) {
-    const double zk = z[k];
-#pragma unroll
-    for (int i = 0; i < KMAXV; ++i)
-      if (i < nv) acc[i] += V[i * ld + k] * zk;
-  }
+// Per-thread accumulation type of the multi-dot / multi-axpy kernels: the
+// vectors' own type (each thread sums ~n / (grid * TB) terms; the partial
+// sums are combined in FP64).  FP32 vectors thus stay off the FP64 pipe.
+template <int TB, typename VT = double>
+__global__ void __launch_bounds__(TB) mdot2d_kernel(const VT* __restrict__ V, int64_t ld,
+                                                    const VT* __restrict__ z, int64_t n,
+                                                    double* __restrict__ partial) {
+  __shared__ double red[TB / 32];
+  const int i = blockIdx.y;
+  const VT* Vi = V + (size_t)i * ld;
+  VT acc = 0;
+  for (int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x; k < n; k += (int64_t)gridDim.x * TB)
+    acc += Vi[k] * z[k];
+  double a = warp_sum((double)acc);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int i = 0; i < KMAXV; ++i) {
-    if (i < nv) {
-      double v = warp_sum(acc[i]);
-      if (lane == 0) red[wid][i] = v;
-    }
-  }
+  if (lane == 0) red[wid] = a;
   __syncthreads();
-  for (int i = threadIdx.x; i < nv; i += TB) {
+  if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int w = 0; w < TB / 32; ++w) s += red[w][i];
+    for (int w = 0; w < TB / 32; ++w) s += red[w];
     partial[(int64_t)blockIdx.x * KMAXV + i] = s;
   }
 }
 
-// z -= sum_i V[i] h[i]; then (mode 1) partial of V[i] . z_new, (mode 2)
-// partial of z_new . z_new, (mode 0) nothing
-template <int TB>
-__global__ void __launch_bounds__(TB) update_kernel(const double* __restrict__ V, int64_t ld, int nv,
-                                                    const double* __restrict__ h,
-                                                    double* __restrict__ z, int64_t n,
-                                                    double* __restrict__ partial, int mode) {
-  __shared__ double hs[KMAXV];
-  __shared__ double red[TB / 32][KMAXV];
-  for (int i = threadIdx.x; i < nv; i += TB) hs[i] = h[i];
+// z -= sum_i V[i] h[i] (any nv <= 256); with want_norm also partial[bx][0] = slice of |z_new|^2
+template <int TB, typename VT = double>
+__global__ void __launch_bounds__(TB) axpy_multi_kernel(const VT* __restrict__ V, int64_t ld, int nv,
+                                                        const double* __restrict__ h, VT* __restrict__ z,
+                                                        int64_t n, double* __restrict__ partial,
+                                                        int want_norm) {
+  __shared__ VT hs[256];
+  __shared__ double red[TB / 32];
+  for (int i = threadIdx.x; i < nv; i += TB) hs[i] = (VT)h[i];
   __syncthreads();
-  double acc[KMAXV];
-#pragma unroll
-  for (int i = 0; i < KMAXV; ++i) acc[i] = 0.0;
+  VT acc = 0;
   for (int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x; k < n; k += (int64_t)gridDim.x * TB) {
-    double zk = z[k];
+    VT zk = z[k];
+    // groups of 8 independent loads keep enough requests in flight
+    for (int i0 = 0; i0 < nv; i0 += 8) {
+      VT v[8];
 #pragma unroll
-    for (int i = 0; i < KMAXV; ++i)
-      if (i < nv) zk -= V[i * ld + k] * hs[i];
+      for (int q = 0; q < 8; ++q) v[q] = (i0 + q < nv) ? V[(size_t)(i0 + q) * ld + k] : (VT)0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (i0 + q < nv) zk -= v[q] * hs[i0 + q];
+    }
     z[k] = zk;
-    if (mode == 1) {
-#pragma unroll
-      for (int i = 0; i < KMAXV; ++i)
-        if (i < nv) acc[i] += V[i * ld + k] * zk;
-    } else if (mode == 2) {
-      acc[0] += zk * zk;
-    }
+    if (want_norm) acc += zk * zk;
   }
-  if (mode == 0) return;
-  const int nr = mode == 1 ? nv : 1;
+  if (!want_norm) return;
+  double a = warp_sum((double)acc);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int i = 0; i < KMAXV; ++i) {
-    if (i < nr) {
-      double v = warp_sum(acc[i]);
-      if (lane == 0) red[wid][i] = v;
-    }
-  }
+  if (lane == 0) red[wid] = a;
   __syncthreads();
-  for (int i = threadIdx.x; i < nr; i += TB) {
+  if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int w = 0; w < TB / 32; ++w) s += red[w][i];
-    partial[(int64_t)blockIdx.x * KMAXV + i] = s;
+    for (int w = 0; w < TB / 32; ++w) s += red[w];
+    partial[(int64_t)blockIdx.x * KMAXV] = s;
   }
 }
 
-// out[i] = (accumulate ? out[i] : 0) + sum_blk partial[blk][i]; optional sqrt
+// out[i] = (accumulate ? out[i] : 0) + sum_blk partial[blk][i]; optional
+// sqrt.  One block per vector i (gridDim.x = nv), a fixed-order tree sum.
 __global__ void reduce_partial_kernel(const double* __restrict__ partial, int nblk, int nv,
                                       double* __restrict__ out, int accumulate, int take_sqrt) {
-  const int i = threadIdx.x;
+  __shared__ double red[32];
+  const int i = blockIdx.x;
   if (i >= nv) return;
   double s = 0.0;
-  for (int b = 0; b < nblk; ++b) s += partial[(int64_t)b * KMAXV + i];
-  if (take_sqrt) s = sqrt(s);
-  out[i] = accumulate ? out[i] + s : s;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += partial[(int64_t)b * KMAXV + i];
+  s = warp_sum(s);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) t += red[w];
+    if (take_sqrt) t = sqrt(t);
+    out[i] = accumulate ? out[i] + t : t;
+  }
 }
 
-// v = z / (*den)
-__global__ void scale_kernel(const double* __restrict__ z, const double* __restrict__ den,
-                             double* __restrict__ v, int64_t n) {
+// v = z / (*den): FP64 vectors divide (bitwise like the reference's
+// w / h); other types multiply by the reciprocal formed once
+template <typename VT = double>
+__global__ void scale_kernel(const VT* __restrict__ z, const double* __restrict__ den,
+                             VT* __restrict__ v, int64_t n) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const double d = *den;
-  if (k < n) v[k] = z[k] / d;
+  if (k >= n) return;
+  if constexpr (sizeof(VT) == 8) {
+    v[k] = z[k] / (VT)(*den);
+  } else {
+    const VT inv = (VT)(1.0 / *den);
+    v[k] = z[k] * inv;
+  }
 }
 
-// x += sum_i V[i] y[i]
-__global__ void combine_kernel(const double* __restrict__ V, int64_t ld, int nv,
-                               const double* __restrict__ y, double* __restrict__ x, int64_t n) {
+// x += alpha * sum_i V[i] y[i]
+template <typename VT = double, typename XT = double>
+__global__ void combine_kernel(const VT* __restrict__ V, int64_t ld, int nv,
+                               const double* __restrict__ y, XT* __restrict__ x, int64_t n,
+                               double alpha = 1.0) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   double s = 0.0;
-  for (int i = 0; i < nv; ++i) s += V[i * ld + k] * y[i];
-  x[k] += s;
+  for (int i = 0; i < nv; ++i) s += (double)V[i * ld + k] * y[i];
+  x[k] = (XT)((double)x[k] + alpha * s);
 }
 
 }  // namespace dg
@@ -491,6 +514,108 @@ __global__ void __launch_bounds__(1024) vcycle_cluster_kernel(VCycleParams p) {
     const VLevel& L = p.lev[0];
     slice(L.n, rank, ncta, lo, hi);
     for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) p.e_out[i] = __ldcg(L.e + i);
+  }
+}
+
+}  // namespace dg
+
+namespace dg {
+
+// ---------------------------------------------------------------------------
+// Coarse tail of the SFC V-cycle in one CTA: levels l0 .. top (down sweeps,
+// pair-sum restriction, the one-node solve, prolongation and up sweeps),
+// separated by __syncthreads instead of kernel boundaries.  On entry level
+// l0 holds its right-hand side r and initial error e (restricted from the
+// level above); on exit its final error is in lev[l0].e.  All data stays in
+// the L1/L2 of one SM, which is fast for the small levels (n <= a few
+// thousand rows).  Same arithmetic as the per-level kernels.
+template <typename T>
+struct TLevel {
+  const int* rowptr;
+  const int* col;
+  const T* val;
+  const T* diag;
+  const int* up;
+  T* e;
+  T* e2;
+  T* r;
+  T* rr;
+  int n;
+};
+
+template <typename T>
+struct TailParams {
+  TLevel<T> lev[VMAXLEV];
+  int l0, top;
+  int pre, post;
+  double w;
+};
+
+template <typename T>
+__device__ __forceinline__ void tail_jacobi(const TLevel<T>& L, const T* e_in, T* e_out, T* rr_out, T w) {
+  constexpr int TL = 4;   // lanes per row
+  const int lane = threadIdx.x % TL;
+  const int groups = blockDim.x / TL;
+  for (int base = 0; base < L.n; base += groups) {
+    const int i = base + (int)threadIdx.x / TL;
+    T s = 0;
+    if (i < L.n)
+      for (int k = L.rowptr[i] + lane; k < L.rowptr[i + 1]; k += TL) s += L.val[k] * e_in[L.col[k]];
+#pragma unroll
+    for (int o = TL / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, TL);
+    if (i < L.n && lane == 0) {
+      const T rr = L.r[i] - s;
+      e_out[i] = e_in[i] + rr / L.diag[i] * w;
+      if (rr_out) rr_out[i] = rr;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) vcycle_tail_kernel(TailParams<T> p) {
+  const T w = (T)p.w;
+  for (int l = p.l0; l < p.top; ++l) {
+    const TLevel<T>& L = p.lev[l];
+    T* ea = L.e;
+    T* eb = L.e2;
+    for (int it = 0; it < p.pre; ++it) {
+      tail_jacobi(L, ea, eb, (T*)nullptr, w);
+      __syncthreads();
+      T* t = ea; ea = eb; eb = t;
+    }
+    tail_jacobi(L, ea, eb, L.rr, w);     // the residual-forming call also updates e
+    __syncthreads();
+    const TLevel<T>& Nx = p.lev[l + 1];
+    for (int i = threadIdx.x; i < Nx.n; i += blockDim.x) {
+      const int a = 2 * i, b2 = 2 * i + 1;
+      Nx.r[i] = L.rr[a] + (b2 < L.n ? L.rr[b2] : (T)0);
+      Nx.e[i] = eb[a] + (b2 < L.n ? eb[b2] : (T)0);
+    }
+    if (eb != L.e)
+      for (int i = threadIdx.x; i < L.n; i += blockDim.x) L.e[i] = eb[i];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const TLevel<T>& Tp = p.lev[p.top];
+    Tp.e[0] = Tp.r[0] / Tp.val[0];
+  }
+  __syncthreads();
+  for (int l = p.top - 1; l >= p.l0; --l) {
+    const TLevel<T>& L = p.lev[l];
+    const TLevel<T>& Nx = p.lev[l + 1];
+    for (int i = threadIdx.x; i < L.n; i += blockDim.x) L.e[i] = L.e[i] + Nx.e[L.up[i]];
+    __syncthreads();
+    T* ea = L.e;
+    T* eb = L.e2;
+    for (int it = 0; it < p.post; ++it) {
+      tail_jacobi(L, ea, eb, (T*)nullptr, w);
+      __syncthreads();
+      T* t = ea; ea = eb; eb = t;
+    }
+    if (ea != L.e) {
+      for (int i = threadIdx.x; i < L.n; i += blockDim.x) L.e[i] = ea[i];
+      __syncthreads();
+    }
   }
 }
 

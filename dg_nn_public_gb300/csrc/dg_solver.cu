@@ -1,9 +1,11 @@
 // libdgsip: context, operator assembly, preconditioner and GMRES drivers.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -72,11 +74,13 @@ struct dg_ctx {
   std::vector<int64_t> sp_off;
   double* d_rar = nullptr;
   std::vector<double> rar_host;
-  // SFC levels
+  // SFC levels (device) and the host copy of the hierarchy
   std::vector<DevLevel> lev;
+  SfcHierarchy sfc_h;
   // scratch
   double *d_t1 = nullptr, *d_t2 = nullptr, *d_t3 = nullptr, *d_t4 = nullptr, *d_t5 = nullptr;
   double *d_cg1 = nullptr, *d_cg2 = nullptr;
+  double* d_r1 = nullptr;   // (nele, ncorner) element P1 restriction scratch
   // Krylov
   double* d_V = nullptr;
   int vcap = 0;
@@ -86,12 +90,29 @@ struct dg_ctx {
   bool built = false;
   // SFC V-cycle as one thread-block-cluster kernel (0 = per-level launches)
   int vc_cluster = 0;
+  // levels with at most this many rows run in the one-CTA tail kernel
+  int tail_max64 = 320, tail_max32 = 800;
+  // mixed preconditioner: exact (dense inverse) solve on the first SFC level
+  // with at most this many rows (0 = keep the V-cycle to the one-node level)
+  int dense_max32 = 1200;
+  int dense_n = 0;
+  // mixed preconditioner reads BF16 copies of the blocks / smoother matrices
+  bool precond_bf16 = true;
+  bool verbose = false;
+  // mixed preconditioner smoother: 0 = the reference's three point-Jacobi
+  // sweeps, 1 = damped exact block inverse w_b * A_ee^{-1}
+  int mixed_smoother = 1;
+  double mixed_smooth_w = 0.8;
   // captured Arnoldi cycle (GMRES(m) inner loop) replayed as one CUDA graph
   bool use_graph = true;
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t arnoldi_exec = nullptr;
   int arnoldi_m = 0;
   const double* arnoldi_vptr = nullptr;
+  // mixed-precision state (dg_mixed.cuh) and operator versions
+  void* mixed_state = nullptr;
+  int build_version = 0;
+  int mixed_version = -1;
 };
 
 namespace {
@@ -196,20 +217,32 @@ int launch_build(dg_ctx* c, cudaStream_t st) {
 
 template <int D>
 int launch_residual(dg_ctx* c, const double* x, const double* b, double* r, double* x_out, int flags,
-                    cudaStream_t st) {
+                    cudaStream_t st, double* r1) {
   using E = Elem<D>;
   unsigned g = nblk(c->B, E::EPB);
   if (g) residual_kernel<E::N, E::F, E::EPB><<<g, E::EPB * E::N, 0, st>>>(
-      c->d_blk, c->d_W, c->d_nbe, x, b, r, x_out, c->B, flags);
+      c->d_blk, c->d_W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, r1);
   bump();
   CKL(c);
   return DG_OK;
 }
 
+// flags RF_*; with RF_RESTRICT, r1 (nele, ncorner) receives the P3->P1
+// element restriction of the residual (not combined with RF_SMOOTH)
 int residual(dg_ctx* c, const double* x, const double* b, double* r, double* x_out, int flags,
-             cudaStream_t st) {
-  return c->D == 3 ? launch_residual<3>(c, x, b, r, x_out, flags, st)
-                   : launch_residual<2>(c, x, b, r, x_out, flags, st);
+             cudaStream_t st, double* r1 = nullptr) {
+  return c->D == 3 ? launch_residual<3>(c, x, b, r, x_out, flags, st, r1)
+                   : launch_residual<2>(c, x, b, r, x_out, flags, st, r1);
+}
+
+// vertex gather of the element restrictions r1 (curve order when sfc_order)
+template <typename T>
+int gather_cg(dg_ctx* c, const T* r1, T* out, bool sfc_order, cudaStream_t st) {
+  gather_cg_kernel<T><<<nblk(c->ncg, 128), 128, 0, st>>>(r1, c->d_gptr, c->d_gent, c->d_wdg,
+                                                         sfc_order ? c->d_pos : nullptr, out, (int)c->ncg);
+  bump();
+  CKL(c);
+  return DG_OK;
 }
 
 template <int D>
@@ -241,6 +274,16 @@ int launch_prolong(dg_ctx* c, double* x, const double* ecg, bool sfc_order, int 
 int prolong_cg(dg_ctx* c, double* x, const double* ecg, bool sfc_order, int color, bool add, cudaStream_t st) {
   return c->D == 3 ? launch_prolong<3>(c, x, ecg, sfc_order, color, add, st)
                    : launch_prolong<2>(c, x, ecg, sfc_order, color, add, st);
+}
+
+// First SFC level handled by the one-CTA tail kernel (<= top; == top means
+// only the one-node solve).  Levels above it use per-level launches.
+int tail_start(const dg_ctx* c, int tail_max) {
+  const int nl = (int)c->lev.size();
+  if (nl > VMAXLEV) return nl - 1;
+  for (int l = 0; l < nl; ++l)
+    if (c->lev[l].n <= tail_max) return std::max(l, 0);
+  return nl - 1;
 }
 
 // Pick the cluster size for the one-launch V-cycle (16 if the device can
@@ -314,32 +357,46 @@ int vcycle(dg_ctx* c, const double* r_sfc, cudaStream_t st) {
   const int top = nl - 1;
   const double w = c->cfg.jac_wei;
   const int TB = 128;
+  const int l0 = tail_start(c, c->tail_max64);
   CK(c, cudaMemcpyAsync(c->lev[0].r, r_sfc, sizeof(double) * c->lev[0].n, cudaMemcpyDeviceToDevice, st));
   CK(c, cudaMemsetAsync(c->lev[0].e, 0, sizeof(double) * c->lev[0].n, st));
-  for (int l = 0; l < top; ++l) {
+  for (int l = 0; l < std::min(l0, top); ++l) {
     DevLevel& L = c->lev[l];
     for (int it = 0; it < c->cfg.pre_smooth_its; ++it) {
-      lev_jacobi_kernel<<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r,
+      lev_jacobi_kernel<double><<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r,
                                                                       L.e2, nullptr, L.n, w); bump();
       std::swap(L.e, L.e2);
     }
     // the residual-forming call also updates e in place (reference quirk)
-    lev_jacobi_kernel<<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r,
+    lev_jacobi_kernel<double><<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r,
                                                                     L.e2, L.rr, L.n, w); bump();
     std::swap(L.e, L.e2);
     DevLevel& Nx = c->lev[l + 1];
-    lev_restrict_kernel<<<nblk(Nx.n, TB), TB, 0, st>>>(L.rr, L.e, Nx.r, Nx.e, L.n, Nx.n); bump();
+    lev_restrict_kernel<double><<<nblk(Nx.n, TB), TB, 0, st>>>(L.rr, L.e, Nx.r, Nx.e, L.n, Nx.n); bump();
   }
-  {
+  if (c->lev[top].n != 1) return fail(c, DG_ERR_STATE, "coarsest SFC level must hold one node");
+  if (l0 < top) {
+    TailParams<double> tp;
+    tp.l0 = l0;
+    tp.top = top;
+    tp.pre = c->cfg.pre_smooth_its;
+    tp.post = c->cfg.post_smooth_its;
+    tp.w = w;
+    for (int l = 0; l < nl; ++l) {
+      const DevLevel& L = c->lev[l];
+      tp.lev[l] = TLevel<double>{L.rowptr, L.col, L.val, L.diag, L.up, L.e, L.e2, L.r, L.rr, L.n};
+    }
+    vcycle_tail_kernel<double><<<1, 1024, 0, st>>>(tp);
+    bump();
+  } else {
     DevLevel& L = c->lev[top];
-    if (L.n != 1) return fail(c, DG_ERR_STATE, "coarsest SFC level must hold one node");
-    lev_coarse_kernel<<<1, 32, 0, st>>>(L.val, L.r, L.e); bump();
+    lev_coarse_kernel<double><<<1, 32, 0, st>>>(L.val, L.r, L.e); bump();
   }
-  for (int l = top - 1; l >= 0; --l) {
+  for (int l = std::min(l0, top) - 1; l >= 0; --l) {
     DevLevel& L = c->lev[l];
-    lev_prolong_kernel<<<nblk(L.n, TB), TB, 0, st>>>(L.e, c->lev[l + 1].e, L.up, L.n); bump();
+    lev_prolong_kernel<double><<<nblk(L.n, TB), TB, 0, st>>>(L.e, c->lev[l + 1].e, L.up, L.n); bump();
     for (int it = 0; it < c->cfg.post_smooth_its; ++it) {
-      lev_jacobi_kernel<<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r,
+      lev_jacobi_kernel<double><<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e, L.r,
                                                                       L.e2, nullptr, L.n, w); bump();
       std::swap(L.e, L.e2);
     }
@@ -365,9 +422,10 @@ int precond(dg_ctx* c, const double* r, double* z, cudaStream_t st) {
   } else {
     CK(c, cudaMemsetAsync(cur, 0, sizeof(double) * c->nonods, st));
   }
-  // residual, restriction to P1CG in curve order, V-cycle, prolongation
-  if ((rc = residual(c, cur, r, c->d_t5, nullptr, 0, st))) return rc;
-  if ((rc = restrict_cg(c, c->d_t5, c->d_cg1, true, st))) return rc;
+  // residual restricted to P1 per element, gathered to P1CG in curve order,
+  // V-cycle, prolongation
+  if ((rc = residual(c, cur, r, nullptr, nullptr, RF_RESTRICT, st, c->d_r1))) return rc;
+  if ((rc = gather_cg<double>(c, c->d_r1, c->d_cg1, true, st))) return rc;
   if ((rc = vcycle(c, c->d_cg1, st))) return rc;
   if ((rc = prolong_cg(c, cur, c->lev[0].e, true, 0, true, st))) return rc;
   // post-smoothing (the reference repeats pre_smooth_its times, :2021)
@@ -390,65 +448,69 @@ int ensure_krylov(dg_ctx* c, int m) {
   return DG_OK;
 }
 
-// h[0..nv) = V[0..nv)^T z  (chunks of KMAXV)
-int mdot(dg_ctx* c, const double* V, int nv, const double* z, double* h, int accumulate, cudaStream_t st) {
+// h[0..nv) = V[0..nv)^T z (FP64 accumulation; chunks of KMAXV vectors)
+template <typename VT>
+int mdot_t(dg_ctx* c, const VT* V, int nv, const VT* z, double* h, cudaStream_t st) {
   for (int off = 0; off < nv; off += KMAXV) {
     int cnt = std::min(KMAXV, nv - off);
-    mdot_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(V + (size_t)off * c->nonods, c->nonods, cnt, z, c->nonods,
-                                                    c->d_part); bump();
-    reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_part, c->nred, cnt, h + off, accumulate, 0); bump();
+    dim3 grid(c->nred, cnt);
+    mdot2d_kernel<RED_TB, VT><<<grid, RED_TB, 0, st>>>(V + (size_t)off * c->nonods, c->nonods, z, c->nonods,
+                                                       c->d_part);
+    bump();
+    reduce_partial_kernel<<<cnt, 128, 0, st>>>(c->d_part, c->nred, cnt, h + off, 0, 0);
+    bump();
   }
   CKL(c);
   return DG_OK;
+}
+
+int mdot(dg_ctx* c, const double* V, int nv, const double* z, double* h, int accumulate, cudaStream_t st) {
+  (void)accumulate;
+  return mdot_t<double>(c, V, nv, z, h, st);
 }
 
 // Norm of z into *out (device)
-int norm2(dg_ctx* c, const double* z, double* out, cudaStream_t st) {
-  mdot_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(z, c->nonods, 1, z, c->nonods, c->d_part); bump();
-  reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_part, c->nred, 1, out, 0, 1); bump();
+template <typename VT>
+int norm_t(dg_ctx* c, const VT* z, double* out, cudaStream_t st) {
+  dim3 grid(c->nred, 1);
+  mdot2d_kernel<RED_TB, VT><<<grid, RED_TB, 0, st>>>(z, c->nonods, z, c->nonods, c->d_part);
+  bump();
+  reduce_partial_kernel<<<1, 128, 0, st>>>(c->d_part, c->nred, 1, out, 0, 1);
+  bump();
   CKL(c);
   return DG_OK;
 }
 
-// CGS2 step: z <- z - V h with h = V^T z twice; H column j gets h1 + h2 and
-// H[j+1][j] = ||z||; V[j+1] = z / ||z||.
-int cgs2(dg_ctx* c, int j, double* z, int m, cudaStream_t st) {
+int norm2(dg_ctx* c, const double* z, double* out, cudaStream_t st) { return norm_t<double>(c, z, out, st); }
+
+// CGS2 step: h1 = V^T z, z -= V h1, h2 = V^T z, z -= V h2 (with |z|^2);
+// H column j = h1 + h2, H[j+1][j] = |z|, V[j+1] = z / |z|.
+template <typename VT>
+int cgs2_t(dg_ctx* c, VT* Vbase, double* Hbase, int j, VT* z, int m, cudaStream_t st) {
   const int nv = j + 1;
-  double* Hc = c->d_H + (size_t)j * (m + 1);     // column-major (m+1) x m
+  double* Hc = Hbase + (size_t)j * (m + 1);     // column-major (m+1) x m
   int rc;
-  if ((rc = mdot(c, c->d_V, nv, z, c->d_h1, 0, st))) return rc;
-  if (nv <= KMAXV) {
-    update_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(c->d_V, c->nonods, nv, c->d_h1, z, c->nonods, c->d_part, 1); bump();
-    reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_part, c->nred, nv, c->d_h2, 0, 0); bump();
-    update_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(c->d_V, c->nonods, nv, c->d_h2, z, c->nonods, c->d_part, 2); bump();
-    reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_part, c->nred, 1, Hc + nv, 0, 1); bump();
-  } else {
-    for (int off = 0; off < nv; off += KMAXV) {
-      int cnt = std::min(KMAXV, nv - off);
-      update_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(c->d_V + (size_t)off * c->nonods, c->nonods, cnt,
-                                                        c->d_h1 + off, z, c->nonods, c->d_part, 0); bump();
-    }
-    if ((rc = mdot(c, c->d_V, nv, z, c->d_h2, 0, st))) return rc;
-    for (int off = 0; off < nv; off += KMAXV) {
-      int cnt = std::min(KMAXV, nv - off);
-      update_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(c->d_V + (size_t)off * c->nonods, c->nonods, cnt,
-                                                        c->d_h2 + off, z, c->nonods, c->d_part, 0); bump();
-    }
-    if ((rc = norm2(c, z, Hc + nv, st))) return rc;
-  }
-  // H[0..nv) = h1 + h2
+  if ((rc = mdot_t<VT>(c, Vbase, nv, z, c->d_h1, st))) return rc;
+  axpy_multi_kernel<RED_TB, VT><<<c->nred, RED_TB, 0, st>>>(Vbase, c->nonods, nv, c->d_h1, z, c->nonods, c->d_part, 0);
+  bump();
+  if ((rc = mdot_t<VT>(c, Vbase, nv, z, c->d_h2, st))) return rc;
+  axpy_multi_kernel<RED_TB, VT><<<c->nred, RED_TB, 0, st>>>(Vbase, c->nonods, nv, c->d_h2, z, c->nonods, c->d_part, 1);
+  bump();
+  reduce_partial_kernel<<<1, 128, 0, st>>>(c->d_part, c->nred, 1, Hc + nv, 0, 1);
+  bump();
   CK(c, cudaMemcpyAsync(Hc, c->d_h1, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st));
-  reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_h2, 1, std::min(nv, KMAXV), Hc, 1, 0); bump();
-  if (nv > KMAXV) {
-    for (int off = KMAXV; off < nv; off += KMAXV) {
-      int cnt = std::min(KMAXV, nv - off);
-      reduce_partial_kernel<<<1, KMAXV, 0, st>>>(c->d_h2 + off, 1, cnt, Hc + off, 1, 0); bump();
-    }
+  for (int off = 0; off < nv; off += KMAXV) {
+    int cnt = std::min(KMAXV, nv - off);
+    reduce_partial_kernel<<<cnt, 32, 0, st>>>(c->d_h2 + off, 1, cnt, Hc + off, 1, 0);
+    bump();
   }
-  scale_kernel<<<nblk(c->nonods, 256), 256, 0, st>>>(z, Hc + nv, c->d_V + (size_t)nv * c->nonods, c->nonods); bump();
+  scale_kernel<VT><<<nblk(c->nonods, 256), 256, 0, st>>>(z, Hc + nv, Vbase + (size_t)nv * c->nonods, c->nonods);
+  bump();
   CKL(c);
   return DG_OK;
 }
+
+int cgs2(dg_ctx* c, int j, double* z, int m, cudaStream_t st) { return cgs2_t<double>(c, c->d_V, c->d_H, j, z, m, st); }
 
 // The m Arnoldi steps of one GMRES cycle (V[0] already set): w = A v_j,
 // r = M^-1 w, CGS2 against V[0..j], V[j+1] = r / ||r||.
@@ -531,6 +593,8 @@ int read_scalar(dg_ctx* c, const double* d, double* h, cudaStream_t st) {
 
 }  // namespace
 
+#include "dg_mixed.cuh"
+
 // ===========================================================================
 extern "C" {
 
@@ -547,6 +611,7 @@ void dg_destroy(dg_ctx* ctx) {
   cudaGetDevice(&cur);
   cudaSetDevice(ctx->dev);
   if (ctx->arnoldi_exec) cudaGraphExecDestroy(ctx->arnoldi_exec);
+  destroy_mixed(ctx);
   if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
   for (void* p : ctx->allocs) cudaFree(p);
   cudaSetDevice(cur);
@@ -586,6 +651,22 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
   cudaDeviceProp prop;
   CK(c.get(), cudaGetDeviceProperties(&prop, c->dev));
   c->nsm = prop.multiProcessorCount;
+  {
+    const char* t64 = std::getenv("DG_TAIL_MAX64");
+    const char* t32 = std::getenv("DG_TAIL_MAX32");
+    if (t64 && t64[0]) c->tail_max64 = std::atoi(t64);
+    if (t32 && t32[0]) c->tail_max32 = std::atoi(t32);
+    const char* dm = std::getenv("DG_DENSE_MAX32");
+    if (dm && dm[0]) c->dense_max32 = std::atoi(dm);
+    const char* vb = std::getenv("DG_VERBOSE");
+    c->verbose = vb && vb[0] && vb[0] != '0';
+    const char* ms = std::getenv("DG_MIXED_SMOOTHER");
+    if (ms && ms[0]) c->mixed_smoother = std::atoi(ms);
+    const char* mw = std::getenv("DG_MIXED_SMOOTH_W");
+    if (mw && mw[0]) c->mixed_smooth_w = std::atof(mw);
+    const char* pb = std::getenv("DG_PRECOND_BF16");
+    if (pb && pb[0]) c->precond_bf16 = pb[0] != '0';
+  }
   {
     const char* ng = std::getenv("DG_NO_GRAPH");
     c->use_graph = !(ng && ng[0] && ng[0] != '0');
@@ -716,6 +797,7 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if ((rc = dalloc(c.get(), t, (size_t)c->nonods))) return rc;
   for (double** t : {&c->d_cg1, &c->d_cg2})
     if ((rc = dalloc(c.get(), t, (size_t)c->ncg))) return rc;
+  if ((rc = dalloc(c.get(), &c->d_r1, (size_t)c->B * c->NC))) return rc;
   if ((rc = dalloc(c.get(), &c->d_part, (size_t)c->nred * KMAXV))) return rc;
   for (double** t : {&c->d_h1, &c->d_h2, &c->d_y, &c->d_scal})
     if ((rc = dalloc(c.get(), t, 256))) return rc;
@@ -750,6 +832,7 @@ int dg_build_operator(dg_ctx* c, void* stream) {
   CK(c, cudaStreamSynchronize(st));
   if (herr) return fail(c, DG_ERR_MESH, "non-positive element Jacobian (element not positively oriented)");
   c->built = true;   // blocks are usable from here on (the probes below apply them)
+  ++c->build_version;
   // colour-probe Galerkin operator on P1CG (volume_mf_diff.py:1696-1754)
   CK(c, cudaMemsetAsync(c->d_rar, 0, sizeof(double) * c->cola.size(), st));
   for (int col = 1; col <= c->ncolor; ++col) {
@@ -766,7 +849,8 @@ int dg_build_operator(dg_ctx* c, void* stream) {
   CK(c, cudaMemcpyAsync(c->rar_host.data(), c->d_rar, sizeof(double) * c->cola.size(), cudaMemcpyDeviceToHost, st));
   CK(c, cudaStreamSynchronize(st));
   // SFC levels (compact_fcode.f90 + get_a_diaga)
-  SfcHierarchy h;
+  SfcHierarchy& h = c->sfc_h;
+  h = SfcHierarchy();
   if ((rc = sfc_levels(c->ncg, c->fina.data(), c->cola.data(), c->rar_host.data(), c->sfc.data(), h)))
     return fail(c, rc, g_thread_error);
   // (re)allocate the device levels

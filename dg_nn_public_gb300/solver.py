@@ -173,6 +173,15 @@ class DGSolver:
                                      self._stream()))
         return y
 
+    def apply_f32(self, x, y=None):
+        """y = A x with the FP32 operator copy (FP32 CUDA tensors)."""
+        torch = _torch()
+        if not (x.is_cuda and x.dtype == torch.float32 and x.is_contiguous() and x.numel() == self.nonods):
+            raise ValueError("expected a contiguous FP32 CUDA tensor with %d entries" % self.nonods)
+        y = torch.empty_like(x) if y is None else y
+        self._chk(self._lib.dg_apply_f32(self._ctx, x.data_ptr(), y.data_ptr(), self._stream()))
+        return y
+
     def rhs(self, f, g=None, gn=None, b=None):
         n = self.nonods
         b = self._vec() if b is None else b
@@ -193,7 +202,7 @@ class DGSolver:
                                          self._stream()))
         return e_sfc
 
-    def solve(self, f, g=None, rtol=1e-10, x0=None, out=None):
+    def solve(self, f, g=None, rtol=1e-10, x0=None, out=None, mode="fp64"):
         """Solve A x = M f + lift(g) to ||b - A x|| <= rtol * ||b - A x0||.
 
         f, g: nodal source / Dirichlet data, (nele*nloc) FP64, on the host
@@ -217,7 +226,12 @@ class DGSolver:
         x = torch.zeros_like(b) if x0 is None else to_dev(x0).clone()
         r0 = b if x0 is None else self.residual(x, b)
         tol = rtol * float(torch.linalg.norm(r0))
-        its, res = self.gmres(x, b, tol)
+        if mode == "mixed":
+            its, res, _ = self.solve_mixed(x, b, tol)
+        elif mode == "fp64":
+            its, res = self.gmres(x, b, tol)
+        else:
+            raise ValueError("mode must be 'fp64' or 'mixed'")
         if on_host:
             if out is None:
                 out = torch.empty(self.nonods, dtype=torch.float64, pin_memory=True)
@@ -225,6 +239,33 @@ class DGSolver:
             torch.cuda.current_stream().synchronize()
             return out, its, res
         return x, its, res
+
+    def set_mixed_options(self, smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=1200):
+        """Mixed preconditioner: smoother 'jacobi3' (three point-Jacobi sweeps,
+        as the reference) or 'blockinv' (smooth_w * A_ee^-1); BF16 block copies
+        for the preconditioner; exact dense solve on the first SFC level with
+        at most dense_max rows."""
+        code = {"jacobi3": 0, "blockinv": 1}[smoother]
+        self._chk(self._lib.dg_set_mixed_options(self._ctx, code, float(smooth_w), 1 if precond_bf16 else 0,
+                                                 int(dense_max)))
+
+    def solve_mixed(self, x, b, tol, m=None, max_its=None, inner_rtol=1e-3, raise_noconv=False):
+        """FP64 iterative refinement around an FP32 right-preconditioned
+        flexible GMRES(m) with the FP32 copy of the multigrid preconditioner;
+        in place on x until ||b - A x|| <= tol.  Returns (inner its, final
+        residual norm, refinement steps)."""
+        m = self.cfg.gmres_m if m is None else m
+        max_its = self.cfg.gmres_its if max_its is None else max_its
+        its = C.c_int32(0)
+        outer = C.c_int32(0)
+        res = C.c_double(0.0)
+        rc = self._lib.dg_solve_mixed(self._ctx, self._check_t(x, self.nonods), self._check_t(b, self.nonods),
+                                      float(tol), int(m), int(max_its), float(inner_rtol), C.byref(its),
+                                      C.byref(res), C.byref(outer), self._stream())
+        if rc == _capi.DG_ERR_NOCONV and not raise_noconv:
+            return its.value, res.value, outer.value
+        self._chk(rc)
+        return its.value, res.value, outer.value
 
     def gmres(self, x, b, tol, m=None, max_its=None, raise_noconv=False):
         """Restarted GMRES(m) in place on x; returns (its, final ||b - A x||)."""

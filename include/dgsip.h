@@ -138,6 +138,27 @@ int dg_mg_vcycle(dg_ctx* ctx, const double* r_sfc, double* e_sfc, void* stream);
 int dg_gmres(dg_ctx* ctx, double* x, const double* b, double tol, int32_t m, int32_t max_its,
              int32_t* its, double* res_norm, void* stream);
 
+/* ---- mixed precision (new in this build; no counterpart in the reference) ----
+ * FP64 iterative refinement around an FP32 inner solve: r = b - A x in FP64;
+ * the correction solves A d = r/||r|| with right-preconditioned flexible
+ * GMRES(m) in FP32 (FP32 copies of the operator blocks, smoother matrices
+ * and SFC levels, FP64-accumulated CGS2, FP64 Hessenberg least squares),
+ * stopping when the inner residual estimate is below inner_rtol; x += ||r|| d
+ * in FP64, until ||b - A x|| <= tol (absolute).  its counts inner Arnoldi
+ * steps, outer the refinement steps; all three outputs may be NULL. */
+int dg_solve_mixed(dg_ctx* ctx, double* x, const double* b, double tol, int32_t m, int32_t max_its,
+                   double inner_rtol, int32_t* its, double* res_norm, int32_t* outer, void* stream);
+/* y = A x with the FP32 copy of the operator blocks (FP32 vectors). */
+int dg_apply_f32(dg_ctx* ctx, const float* x, float* y, void* stream);
+/* Options of the mixed preconditioner, applied at the next mixed solve:
+ * smoother 0 = three point-Jacobi sweeps per element block (as the
+ * reference), 1 = damped exact block inverse smooth_w * A_ee^{-1};
+ * precond_bf16 != 0 keeps the preconditioner's blocks in BF16; dense_max =
+ * size limit of the first SFC level solved exactly with a dense inverse
+ * (0 = run the V-cycle down to the one-node level). */
+int dg_set_mixed_options(dg_ctx* ctx, int32_t smoother, double smooth_w, int32_t precond_bf16,
+                         int32_t dense_max);
+
 /* ---- host-only integer layer (no GPU needed) ---- */
 /* P1CG sparsity from the element corners: all vertex pairs sharing an
  * element, rows sorted (z06/sparsity.py:102-122 with

@@ -1,0 +1,84 @@
+"""The C ABI without a GPU: the library builds and loads, exports every entry
+point declared in include/dgsip.h, and its host-only integer layer (P1CG
+sparsity, distance-2 colouring, SFC levels, face connectivity) reproduces
+the oracle bit for bit."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from dg_nn_public_gb300 import _capi, build, element, mesh, sfc
+from oracle import fortran_restated as fr
+from oracle.dg_oracle import OracleDG
+from golden_util import load, rebuild
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "dgsip.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _capi.lib()
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(dg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_all_declared_symbols_exported(lib):
+    names = declared_functions()
+    assert len(names) >= 20
+    raw = ctypes.CDLL(_capi.LIB_PATH)
+    missing = [n for n in names if not hasattr(raw, n)]
+    assert not missing, missing
+
+
+def test_error_path_without_context(lib):
+    rc = lib.dg_p1cg_sparsity(-1, 4, None, 0, None, None, 0, None)
+    assert rc == _capi.DG_ERR_ARG
+    assert b"bad arguments" in lib.dg_last_error(None)
+
+
+@pytest.mark.parametrize("kind,n", [("tet", 3), ("tri", 6), ("tet", 6)])
+def test_integer_layer_matches_oracle(lib, kind, n):
+    m = mesh.build_mesh(kind, n, seed=1)
+    O = OracleDG(m, element.p3_element(m.ndim), element.drst_duv(m.ndim))
+    pc = O.p1cg()
+    fina, cola = _capi.p1cg_sparsity(m.p1cg, m.cg_nonods)
+    assert np.array_equal(fina, pc["fina"]) and np.array_equal(cola, pc["cola"])
+    whichc, ncolor = _capi.color2(fina, cola)
+    assert np.array_equal(whichc, pc["whichc"]) and ncolor == pc["ncolor"]
+    order = sfc.hilbert_sfc_order(m.cg_coords)
+    vals = np.random.default_rng(0).standard_normal(cola.size)
+    nl, start, rowp, col, val = _capi.sfc_levels(fina, cola, vals, order)
+    ref = fr.best_sfc_mapping_to_sfc_matrix_unstructured(
+        vals, np.zeros(m.cg_nonods), np.zeros(m.cg_nonods), fina + 1, cola + 1, order.reshape(-1),
+        5 * m.cg_nonods, 10 * cola.size, fr.calculate_nlevel_sfc(m.cg_nonods) + 1, cola.size, m.cg_nonods)
+    a_all, fina_all, cola_all, ncola_all, _, _, fin, nall, nlevel = ref
+    assert nl == nlevel == _capi.nlevel_sfc(m.cg_nonods)
+    assert np.array_equal(start, fin[:nl + 1] - 1)
+    assert np.array_equal(rowp, fina_all[:nall + 1] - 1)
+    # Fortran stores stacked global columns, the C ABI level-local ones
+    glob = np.concatenate([col[rowp[start[l]]:rowp[start[l + 1]]] + start[l] for l in range(nl)])
+    assert np.array_equal(glob, cola_all[:ncola_all] - 1)
+    assert np.array_equal(val, a_all[:ncola_all])          # same summation order: bit-identical
+    nbf, aln = _capi.face_connectivity(m.ndim, m.cg_ndglno[:, :m.ndim + 1])
+    assert np.array_equal(nbf, m.nbf) and np.array_equal(aln, m.alnmt)
+
+
+def test_face_connectivity_against_reference_golden(lib):
+    d, meta = load("tet3_v22")
+    nbf, aln = _capi.face_connectivity(3, d["cg_ndglno"][:, :4])
+    assert np.array_equal(nbf, d["nbf"]) and np.array_equal(aln, d["alnmt"])
+
+
+def test_sfc_levels_rejects_bad_ordering(lib):
+    m = mesh.build_mesh("tri", 3)
+    fina, cola = _capi.p1cg_sparsity(m.p1cg, m.cg_nonods)
+    bad = np.ones(m.cg_nonods, dtype=np.int64)
+    with pytest.raises(_capi.DGError):
+        _capi.sfc_levels(fina, cola, np.ones(cola.size), bad)

@@ -50,4 +50,5 @@ def test_c2_solve_matches_reference(c2):
     assert rel(xn[::97], d["x_sub"]) < 1e-10
     assert abs(np.linalg.norm(xn) - float(d["x_norm"])) <= 1e-10 * float(d["x_norm"])
     u = np.prod([np.sin(np.pi * X[:, k]) for k in range(3)], axis=0).ravel()
-    assert abs(np.abs(xn - u).max() - float(d["linferr"])) <= 1e-8 * float(d["linferr"])
+    # solutions agreeing to 1e-10 relative move the nodal error by <= ~1e-10
+    assert abs(np.abs(xn - u).max() - float(d["linferr"])) <= 1e-9

@@ -1,0 +1,75 @@
+"""Mixed-precision solve (FP32 inner FGMRES + FP32 multigrid inside FP64
+refinement) against the FP64 path and the manufactured solution.
+
+Both solves stop at ||b - A x|| <= 1e-10 ||b|| in FP64, so they are two
+approximations of the same discrete solution; their difference is bounded
+by the condition number times the tolerance.  The tests check the FP64
+residual independently, the solution difference (<= 1e-7 relative, max-abs)
+and that the discretisation error against the exact solution is unchanged.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from dg_nn_public_gb300 import element, mesh, sfc  # noqa: E402
+from dg_nn_public_gb300.solver import DGSolver, SolverConfig  # noqa: E402
+
+
+def _setup(kind, n, smooth, kappa_sigma=0.0, seed=0):
+    m = mesh.build_mesh(kind, n, seed=seed)
+    order = sfc.hilbert_sfc_order(m.cg_coords)
+    s = DGSolver(m, order, SolverConfig(pre_smooth_its=smooth, post_smooth_its=smooth),
+                 element.p3_element(m.ndim))
+    if kappa_sigma > 0:
+        kap = np.exp(kappa_sigma * np.random.default_rng(seed).standard_normal(m.nele))
+        s.set_kappa(kap)
+    s.build_operator()
+    X = m.x_ref_in
+    u = np.prod([np.sin(np.pi * X[:, k]) for k in range(m.ndim)], axis=0).ravel()
+    f = m.ndim * np.pi ** 2 * u
+    return m, s, f, u
+
+
+@pytest.mark.parametrize("kind,n,smooth", [("tet", 6, 2), ("tri", 16, 3), ("tet", 12, 2)])
+def test_mixed_matches_fp64(kind, n, smooth):
+    m, s, f, u = _setup(kind, n, smooth)
+    b = s.rhs(torch.tensor(f, device="cuda:0"))
+    tol = 1e-10 * float(torch.linalg.norm(b))
+    x64 = torch.zeros_like(b)
+    its64, res64 = s.gmres(x64, b, tol)
+    xm = torch.zeros_like(b)
+    its, res, outer = s.solve_mixed(xm, b, tol)
+    assert res <= tol
+    r = s.residual(xm, b)
+    assert float(torch.linalg.norm(r)) <= tol * (1 + 1e-12)
+    d = float(torch.abs(xm - x64).max() / torch.abs(x64).max())
+    assert d < 1e-7, d
+    e64 = float(torch.abs(x64.cpu() - torch.tensor(u)).max())
+    em = float(torch.abs(xm.cpu() - torch.tensor(u)).max())
+    assert abs(em - e64) <= 1e-6 * e64
+    assert outer >= 1 and its >= 1
+
+
+def test_mixed_variable_kappa_and_nonzero_guess():
+    m, s, f, u = _setup("tet", 6, 2, kappa_sigma=1.0, seed=4)
+    b = s.rhs(torch.tensor(f, device="cuda:0"))
+    tol = 1e-10 * float(torch.linalg.norm(b))
+    x64 = torch.zeros_like(b)
+    s.gmres(x64, b, tol)
+    x0 = torch.randn_like(b)
+    its, res, outer = s.solve_mixed(x0, b, tol)
+    assert res <= tol
+    assert float(torch.abs(x0 - x64).max() / torch.abs(x64).max()) < 1e-7
+
+
+def test_mixed_iteration_limit_reports_noconv():
+    from dg_nn_public_gb300 import _capi
+    m, s, f, u = _setup("tet", 4, 2)
+    b = s.rhs(torch.tensor(f, device="cuda:0"))
+    x = torch.zeros_like(b)
+    with pytest.raises(_capi.DGError) as ei:
+        s.solve_mixed(x, b, 1e-30, max_its=5, raise_noconv=True)
+    assert ei.value.code == _capi.DG_ERR_NOCONV
+    assert torch.isfinite(x).all()
