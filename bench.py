@@ -152,6 +152,17 @@ def config_block(args, m, extra=None):
     return d
 
 
+# DRAM bytes (read + write) per launch of the roofline kernels on the
+# 20^3 Kuhn-cube workload (48,000 tets), from one ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum (per-launch table in
+# profiles/residual_kernel_bf16_smooth_c2.md); other workloads report null.
+TRAFFIC_C2 = {
+    "smooth_pc": {"bytes_per_launch": 237.8e6},
+    "apply_f32": {"bytes_per_launch": 384.2e6},
+    "apply_f64": {"bytes_per_launch": 768.0e6},
+}
+
+
 def apply_bytes(m):
     """Algorithmic bytes of one stored-block FP64 apply y = A x."""
     N = m.nloc
@@ -323,40 +334,59 @@ def run_ours(args):
         torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
     e2e_value = ws * dofs * args.steps / float(te.item())
 
-    # roofline of the dominant kernel of the headline mode: the stored-block
-    # apply (FP32 copy in mixed mode, FP64 otherwise), timed alone
+    # roofline of the dominant kernel of the headline mode, timed alone with
+    # CUDA events on the launching stream.  Mixed mode: the preconditioner's
+    # smoothing step (BF16 block copies, FP32 vectors), the largest share of
+    # the solve's device time; FP64 mode: the stored-block FP64 apply.
     nbytes64, s_int = apply_bytes(m)
-    if mode == "mixed":
-        xa = torch.randn(dofs, dtype=torch.float32, device=dev)
-        apply_fn = lambda: s.apply_f32(xa, ya)
-        nbytes = (m.nele + s_int) * m.nloc * m.nloc * 4 + 2 * dofs * 4 + s_int * 4
-        kname = "residual_kernel<20,4,8,float,float,float> (stored-block FP32 apply)"
-    else:
-        xa = torch.randn(dofs, dtype=torch.float64, device=dev)
-        apply_fn = lambda: s.apply(xa, ya)
-        nbytes = nbytes64
-        kname = "residual_kernel<20,4,8> (stored-block FP64 apply)"
-    ya = torch.empty_like(xa)
-    for _ in range(3):
-        apply_fn()
-    reps = 20
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(reps):
-        apply_fn()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    t_apply = e0.elapsed_time(e1) / reps / 1e3
+    N = m.nloc
+    F = m.ndim + 1                                   # faces per simplex
+
+    def time_launch(fn, reps=20):
+        for _ in range(3):
+            fn()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3
+
     peaks, kind = load_peaks()
     peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
-    achieved = nbytes / t_apply / 1e9
-    flops = 2.0 * m.nloc * m.nloc * (m.nele + s_int)
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "apply_traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as fh:
-            traffic = json.load(fh).get(mode, {}).get("bytes_per_launch")
+    traffic_tab = TRAFFIC_C2 if (m.ndim == 3 and m.nele == 48000) else {}
+    rooflines = []
+    if mode == "mixed":
+        xs = torch.randn(dofs, dtype=torch.float32, device=dev)
+        bs = torch.randn(dofs, dtype=torch.float32, device=dev)
+        xo = torch.empty_like(xs)
+        mb = 2 if s.mixed_options.get("precond_bf16", True) else 4
+        nb = (m.nele + s_int) * N * N * mb + m.nele * N * N * mb + 3 * dofs * 4 + m.nele * F * 4
+        t = time_launch(lambda: s.smooth_pc(xs, bs, xo))
+        rooflines.append(("smooth_pc", "residual_kernel<20,4,8,__nv_bfloat16,float,float> (preconditioner "
+                          "smoothing step, BF16 blocks + smoother matrices, FP32 vectors)", nb, t,
+                          2.0 * N * N * (2 * m.nele + s_int)))
+        ya = torch.empty_like(xs)
+        nb = (m.nele + s_int) * N * N * 4 + 2 * dofs * 4 + m.nele * F * 4
+        t = time_launch(lambda: s.apply_f32(xs, ya))
+        rooflines.append(("apply_f32", "residual_kernel<20,4,8,float,float,float> (stored-block FP32 apply)",
+                          nb, t, 2.0 * N * N * (m.nele + s_int)))
+    else:
+        xa = torch.randn(dofs, dtype=torch.float64, device=dev)
+        ya = torch.empty_like(xa)
+        t = time_launch(lambda: s.apply(xa, ya))
+        rooflines.append(("apply_f64", "residual_kernel<20,4,8> (stored-block FP64 apply)", nbytes64, t,
+                          2.0 * N * N * (m.nele + s_int)))
+
+    def roof(entry):
+        key, kname, nbytes, t_launch, flops = entry
+        achieved = nbytes / t_launch / 1e9
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic_tab.get(key, {}).get("bytes_per_launch"), "peak_source": kind,
+                "kernel": kname, "bytes_per_launch": nbytes, "launch_ms": t_launch * 1e3,
+                "tflops": flops / t_launch / 1e12}
 
     out = {
         "metric": METRIC, "value": value, "unit": "DOF/s", "n_gpus": ws, "steps": args.steps,
@@ -378,10 +408,8 @@ def run_ours(args):
         "setup_s": t_setup,
         "e2e": {"value": e2e_value, "unit": "DOF/s", "h2d_bytes_per_step": dofs * 8,
                 "d2h_bytes_per_step": dofs * 8, "api": "DGSolver.solve(mode=%r) (pinned host f -> x)" % mode},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_source": kind,
-                     "kernel": kname, "bytes_per_launch": nbytes, "launch_ms": t_apply * 1e3,
-                     "tflops": flops / t_apply / 1e12},
+        "roofline": roof(rooflines[0]),
+        "roofline_other": [roof(e) for e in rooflines[1:]],
         "gpu_launches": launches,
         "clocks": clk,
     }

@@ -671,6 +671,25 @@ extern "C" int dg_apply_f32(dg_ctx* c, const float* x, float* y, void* stream) {
   return residual32(c, x, nullptr, y, nullptr, RF_NEG, st);
 }
 
+// One smoothing step of the mixed preconditioner on FP32 vectors:
+// x_out = x + W_pc (b - A_pc x), with the preconditioner's stored blocks
+// (BF16 when precond_bf16) and smoother matrices -- the reduced-precision
+// form of get_residual_or_smooth(do_smooth=True).  x_out must not alias x.
+extern "C" int dg_smooth_pc(dg_ctx* c, const float* x, const float* b, float* x_out, void* stream) {
+  if (!c || !x || !b || !x_out) return set_thread_error(DG_ERR_ARG, "dg_smooth_pc: null argument");
+  if (x_out == x) return fail(c, DG_ERR_ARG, "dg_smooth_pc: x_out must not alias x");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_smooth_pc: operator not built");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  CK(c, cudaSetDevice(c->dev));
+  Mixed& M = mixed_of(c);
+  int rc;
+  if (!M.built || c->mixed_version != c->build_version) {
+    if ((rc = build_mixed(c, st))) return rc;
+    c->mixed_version = c->build_version;
+  }
+  return residual_pc(c, x, b, nullptr, x_out, RF_SMOOTH, st);
+}
+
 // Options of the mixed-precision preconditioner (take effect at the next
 // mixed solve): smoother 0 = three point-Jacobi sweeps as the reference,
 // 1 = damped block inverse smooth_w * A_ee^{-1}; precond_bf16 != 0 stores

@@ -182,6 +182,18 @@ class DGSolver:
         self._chk(self._lib.dg_apply_f32(self._ctx, x.data_ptr(), y.data_ptr(), self._stream()))
         return y
 
+    def smooth_pc(self, x, b, x_out=None):
+        """One smoothing step of the mixed preconditioner, x_out = x + W (b - A x),
+        with its FP32/BF16 block copies (FP32 CUDA tensors; x_out distinct from x)."""
+        torch = _torch()
+        for t in (x, b):
+            if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and t.numel() == self.nonods):
+                raise ValueError("expected a contiguous FP32 CUDA tensor with %d entries" % self.nonods)
+        x_out = torch.empty_like(x) if x_out is None else x_out
+        self._chk(self._lib.dg_smooth_pc(self._ctx, x.data_ptr(), b.data_ptr(), x_out.data_ptr(),
+                                         self._stream()))
+        return x_out
+
     def rhs(self, f, g=None, gn=None, b=None):
         n = self.nonods
         b = self._vec() if b is None else b
@@ -248,6 +260,11 @@ class DGSolver:
         code = {"jacobi3": 0, "blockinv": 1}[smoother]
         self._chk(self._lib.dg_set_mixed_options(self._ctx, code, float(smooth_w), 1 if precond_bf16 else 0,
                                                  int(dense_max)))
+        self.mixed_options = dict(smoother=smoother, smooth_w=float(smooth_w), precond_bf16=bool(precond_bf16),
+                                  dense_max=int(dense_max))
+
+    # library defaults of the mixed preconditioner (dg_create)
+    mixed_options = dict(smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=1200)
 
     def solve_mixed(self, x, b, tol, m=None, max_its=None, inner_rtol=1e-3, raise_noconv=False):
         """FP64 iterative refinement around an FP32 right-preconditioned

@@ -150,6 +150,12 @@ int dg_solve_mixed(dg_ctx* ctx, double* x, const double* b, double tol, int32_t 
                    double inner_rtol, int32_t* its, double* res_norm, int32_t* outer, void* stream);
 /* y = A x with the FP32 copy of the operator blocks (FP32 vectors). */
 int dg_apply_f32(dg_ctx* ctx, const float* x, float* y, void* stream);
+/* One smoothing step of the mixed preconditioner on FP32 vectors,
+ * x_out = x + W (b - A x) with the preconditioner's block copies (BF16 when
+ * precond_bf16) -- the reduced-precision counterpart of
+ * get_residual_or_smooth(do_smooth=True), z06/volume_mf_diff.py:403.
+ * x_out must not alias x. */
+int dg_smooth_pc(dg_ctx* ctx, const float* x, const float* b, float* x_out, void* stream);
 /* Options of the mixed preconditioner, applied at the next mixed solve:
  * smoother 0 = three point-Jacobi sweeps per element block (as the
  * reference), 1 = damped exact block inverse smooth_w * A_ee^{-1};

@@ -73,3 +73,30 @@ def test_mixed_iteration_limit_reports_noconv():
         s.solve_mixed(x, b, 1e-30, max_its=5, raise_noconv=True)
     assert ei.value.code == _capi.DG_ERR_NOCONV
     assert torch.isfinite(x).all()
+
+
+@pytest.mark.parametrize("smoother,bf16,tol", [("jacobi3", False, 1e-5), ("blockinv", False, 1e-5),
+                                               ("blockinv", True, 3e-2)])
+def test_smooth_pc_matches_fp64_smoothing(smoother, bf16, tol):
+    """One preconditioner smoothing step (FP32 vectors; FP32 or BF16 blocks)
+    against the same step in FP64: the three-sweep Jacobi map through
+    dg_residual(do_smooth=1), or x + w A_ee^-1 (b - A x) with the FP64
+    diagonal blocks from dg_get_bdiag.  Tolerance relative to max|x_out|."""
+    m, s, f, u = _setup("tet", 6, 2)
+    w = 0.8
+    s.set_mixed_options(smoother=smoother, smooth_w=w, precond_bf16=bf16)
+    g = torch.Generator(device="cuda:0").manual_seed(3)
+    x = torch.randn(s.nonods, dtype=torch.float64, device="cuda:0", generator=g)
+    b = torch.randn(s.nonods, dtype=torch.float64, device="cuda:0", generator=g)
+    if smoother == "jacobi3":
+        ref = torch.empty_like(x)
+        s.residual(x, b, x_out=ref, smooth=True)
+    else:
+        K, _ = s.bdiag()
+        r = s.residual(x, b).view(m.nele, m.nloc, 1)
+        ref = x + w * torch.linalg.solve(K.view(m.nele, m.nloc, m.nloc), r).view(-1)
+    out = s.smooth_pc(x.float().contiguous(), b.float().contiguous())
+    err = float(torch.abs(out.double() - ref).max() / torch.abs(ref).max())
+    assert err < tol, err
+    out2 = s.smooth_pc(x.float().contiguous(), b.float().contiguous())
+    assert torch.equal(out, out2)
