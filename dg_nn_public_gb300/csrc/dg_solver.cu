@@ -1089,3 +1089,5 @@ int dg_gmres(dg_ctx* c, double* x, const double* b, double tol, int32_t m, int32
 }
 
 }  // extern "C"
+
+#include "dg_noalloc.cuh"

@@ -167,6 +167,20 @@ class DGSolver:
                                         1 if smooth else 0, self._stream()))
         return r
 
+    def residual_norm_noalloc(self, x, b=None, r=None, norm_out=None):
+        """r = b - A x and ||r||_2 through dg_residual_norm_noalloc, which
+        allocates nothing (static device scratch; at most 524288 tetrahedra or
+        1048576 triangles).  Pass r (or None to skip it) and a one-entry FP64
+        device tensor norm_out to keep the call free of allocations; returns
+        norm_out."""
+        torch = _torch()
+        n = self.nonods
+        norm_out = torch.empty(1, dtype=torch.float64, device=self._dev()) if norm_out is None else norm_out
+        self._chk(self._lib.dg_residual_norm_noalloc(self._ctx, self._check_t(x, n), self._check_t(b, n),
+                                                     self._check_t(r, n), self._check_t(norm_out, 1),
+                                                     self._stream()))
+        return norm_out
+
     def apply(self, x, y=None):
         y = self._vec() if y is None else y
         self._chk(self._lib.dg_apply(self._ctx, self._check_t(x, self.nonods), self._check_t(y, self.nonods),

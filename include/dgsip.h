@@ -165,6 +165,19 @@ int dg_smooth_pc(dg_ctx* ctx, const float* x, const float* b, float* x_out, void
 int dg_set_mixed_options(dg_ctx* ctx, int32_t smoother, double smooth_w, int32_t precond_bf16,
                          int32_t dense_max);
 
+/* Allocation-free residual norm (no counterpart in the reference):
+ * r = b - A x and *norm_out = ||r||_2, both written on the device (r may be
+ * NULL for the norm alone; b NULL means b = 0).  It allocates nothing: its
+ * scratch is a static device array of 65536 FP64 partial sums (512 KiB), one
+ * per CTA of the residual launch, so meshes above 524288 tetrahedra or
+ * 1048576 triangles are rejected with DG_ERR_ARG.  The first call for a
+ * device looks up that array's address (cudaGetSymbolAddress, device
+ * current) and caches it; make that first call before any stream capture.
+ * Nothing has to start at zero.  Calls whose kernels overlap in time on one
+ * device (other streams or other contexts) share the scratch and race. */
+int dg_residual_norm_noalloc(dg_ctx* ctx, const double* x, const double* b, double* r, double* norm_out,
+                             void* stream);
+
 /* ---- host-only integer layer (no GPU needed) ---- */
 /* P1CG sparsity from the element corners: all vertex pairs sharing an
  * element, rows sorted (z06/sparsity.py:102-122 with
