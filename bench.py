@@ -48,7 +48,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=20, help="cells per cube side")
+    ap.add_argument("--config", default="c2", choices=["c2", "c3"],
+                    help="c2: 20^3 Kuhn cube, kappa = 1; c3: 40^3 (384,000 tets), log-normal kappa (sigma 1)")
+    ap.add_argument("--n", type=int, default=None, help="cells per cube side (overrides --config)")
+    ap.add_argument("--kappa-sigma", type=float, default=None,
+                    help="per-element log-normal diffusivity exp(sigma N(0,1)) (overrides --config)")
+    ap.add_argument("--face-kappa", default=None, choices=["mean", "harmonic"],
+                    help="interior-face kappa: arithmetic mean (the reference's convention) or harmonic "
+                         "mean (weighted-average SIP); c3 uses harmonic")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--smooth", type=int, default=2, help="V(s,s) smoothing steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -56,7 +63,15 @@ def parse():
     ap.add_argument("--no-roofline", action="store_true", help="skip the isolated apply timing")
     ap.add_argument("--mode", default="both", choices=["both", "fp64", "mixed"],
                     help="which solver(s) to time; the faster converged one is the headline")
-    return ap.parse_args()
+    a = ap.parse_args()
+    preset = {"c2": (20, 0.0, "mean"), "c3": (40, 1.0, "harmonic")}[a.config]
+    if a.n is None:
+        a.n = preset[0]
+    if a.kappa_sigma is None:
+        a.kappa_sigma = preset[1]
+    if a.face_kappa is None:
+        a.face_kappa = preset[2]
+    return a
 
 
 def dist_env():
@@ -136,13 +151,23 @@ def workload(args):
     X = m.x_ref_in
     f = 3 * np.pi ** 2 * np.prod([np.sin(np.pi * X[:, d]) for d in range(3)], axis=0)
     u = np.prod([np.sin(np.pi * X[:, d]) for d in range(3)], axis=0)
-    return m, order, el, f.reshape(-1), u.reshape(-1)
+    kappa = None
+    if args.kappa_sigma > 0:
+        # piecewise-constant log-normal diffusivity; f_e = kappa_e * 3 pi^2 prod sin
+        # (with jumps in kappa the smooth u is no longer the exact solution)
+        kappa = np.exp(args.kappa_sigma * np.random.default_rng(args.seed + 1).standard_normal(m.nele))
+        f = f * kappa[:, None]
+    return m, order, el, f.reshape(-1), u.reshape(-1), kappa
 
 
 def config_block(args, m, extra=None):
-    d = {"workload": "3D P3 SIP-DG Poisson, Kuhn cube %d^3 (%d tets, %d DOFs), jitter 0.15h seed %d, "
+    kap = ("log-normal per-element kappa sigma %g (seed %d), %s face kappa"
+           % (args.kappa_sigma, args.seed + 1, args.face_kappa) if args.kappa_sigma > 0 else "kappa = 1")
+    d = {"workload": "3D P3 SIP-DG Poisson, Kuhn cube %d^3 (%d tets, %d DOFs), jitter 0.15h seed %d, %s, "
                      "SFC-MG V(%d,%d) + GMRES(30), rtol 1e-10 on the FP64 true residual"
-                     % (args.n, m.nele, m.nele * m.nloc, args.seed, args.smooth, args.smooth),
+                     % (args.n, m.nele, m.nele * m.nloc, args.seed, kap, args.smooth, args.smooth),
+         "config": args.config if (args.n, args.kappa_sigma, args.face_kappa) in
+                   ((20, 0.0, "mean"), (40, 1.0, "harmonic")) else "custom",
          "nele": int(m.nele), "dofs": int(m.nele * m.nloc), "eta_e": 90.0, "gmres_m": 30,
          "smoothing": "V(%d,%d)" % (args.smooth, args.smooth),
          "l2_policy": "inputs larger than L2: the FP64 operator blocks (%.0f MB) stream from HBM every apply"
@@ -238,10 +263,13 @@ def run_ours(args):
         torch.distributed.barrier()
     from dg_nn_public_gb300.solver import DGSolver, SolverConfig
 
-    m, order, el, f, u = workload(args)
+    m, order, el, f, u, kappa = workload(args)
     cfg = SolverConfig(pre_smooth_its=args.smooth, post_smooth_its=args.smooth, device=local)
     t0 = time.perf_counter()
     s = DGSolver(m, order, cfg, el)
+    if kappa is not None:
+        s.set_kappa(kappa)
+        s.set_face_kappa(args.face_kappa)
     s.build_operator()
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
@@ -308,14 +336,25 @@ def run_ours(args):
     b = s.rhs(f_dev)
     rel_res = float(torch.linalg.norm(s.residual(x, b)) / torch.linalg.norm(b))
     err_inf = float(np.abs(x.cpu().numpy() - u).max())
+    # mixed solution against the FP64 GPU solution of the same system
+    mixed_vs_fp64 = None
+    if R64 is not None and RMX is not None:
+        mixed_vs_fp64 = float(torch.abs(RMX["x"] - R64["x"]).max() / torch.abs(R64["x"]).max())
 
     # end to end through the public solve() with pinned host buffers
     if args.no_e2e:
         if ws > 1:
             torch.distributed.destroy_process_group()
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": value, "unit": "DOF/s", "ms_per_step": t_ms / args.steps,
-                              "mode": mode, "its": its_list, "rel_residual": rel_res, "gpu_launches": launches}))
+            short = {"metric": METRIC, "value": value, "unit": "DOF/s", "ms_per_step": t_ms / args.steps,
+                     "mode": mode, "its": its_list, "rel_residual": rel_res, "gpu_launches": launches,
+                     "max_nodal_error_vs_exact": err_inf, "mixed_vs_fp64_max_rel": mixed_vs_fp64,
+                     "setup_s": t_setup, "config": config_block(args, m)}
+            for key, R in (("fp64", R64), ("mixed", RMX)):
+                if R is not None:
+                    short[key] = {"value": R["value"], "ms_per_step": R["t_ms"] / args.steps, "its": R["its"],
+                                  "final_residual": R["res"], "tol": R["tol"]}
+            print(json.dumps(short))
         return
     f_host = torch.tensor(f, dtype=torch.float64).pin_memory()
     x_host = torch.empty(dofs, dtype=torch.float64).pin_memory()
@@ -358,6 +397,7 @@ def run_ours(args):
     peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
     traffic_tab = TRAFFIC_C2 if (m.ndim == 3 and m.nele == 48000) else {}
     rooflines = []
+    breakdown = None
     if mode == "mixed":
         xs = torch.randn(dofs, dtype=torch.float32, device=dev)
         bs = torch.randn(dofs, dtype=torch.float32, device=dev)
@@ -373,6 +413,13 @@ def run_ours(args):
         t = time_launch(lambda: s.apply_f32(xs, ya))
         rooflines.append(("apply_f32", "residual_kernel<20,4,8,float,float,float> (stored-block FP32 apply)",
                           nb, t, 2.0 * N * N * (m.nele + s_int)))
+        # per inner iteration: preconditioner + apply; the rest is Gram-Schmidt,
+        # Hessenberg updates and the refinement steps
+        t_pc = time_launch(lambda: s.precond_f32(bs, xo))
+        it_ms = RMX["t_ms"] / args.steps / max(1, int(np.median(RMX["its"])))
+        breakdown = {"iteration_ms": it_ms, "precond_f32_ms": t_pc * 1e3, "apply_f32_ms": t * 1e3,
+                     "smooth_pc_ms": rooflines[0][3] * 1e3,
+                     "rest_ms": it_ms - t_pc * 1e3 - t * 1e3}
     else:
         xa = torch.randn(dofs, dtype=torch.float64, device=dev)
         ya = torch.empty_like(xa)
@@ -405,15 +452,21 @@ def run_ours(args):
             "final_residual": RMX["res"], "tol": RMX["tol"], "gpu_launches": RMX["launches"],
             "speedup_vs_fp64": (RMX["value"] / R64["value"]) if R64 else None},
         "its": its_list, "rel_residual": rel_res, "max_nodal_error_vs_exact": err_inf,
+        "mixed_vs_fp64_max_rel": mixed_vs_fp64,
         "setup_s": t_setup,
         "e2e": {"value": e2e_value, "unit": "DOF/s", "h2d_bytes_per_step": dofs * 8,
                 "d2h_bytes_per_step": dofs * 8, "api": "DGSolver.solve(mode=%r) (pinned host f -> x)" % mode},
         "roofline": roof(rooflines[0]),
         "roofline_other": [roof(e) for e in rooflines[1:]],
+        "mixed_iteration_breakdown": breakdown,
         "gpu_launches": launches,
         "clocks": clk,
     }
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and kappa is not None:
+        out["cpu_baseline"] = {"value": None, "unit": "DOF/s",
+                               "skipped": "the CPU restatement is timed on the kappa = 1 workloads only "
+                                          "(its set-up at this size takes minutes)"}
+    elif rank == 0 and not args.no_cpu_baseline:
         try:
             out["cpu_baseline"] = cpu_baseline_sample(m, order, el, int(np.median(its_list)),
                                                       rar=s.rar_values().cpu().numpy(), smooth=args.smooth)
@@ -429,7 +482,7 @@ def run_reference(args):
     ws, rank, local = dist_env()
     if ws > 1 and rank != 0:
         return
-    m, order, el, f, u = workload(args)
+    m, order, el, f, u, kappa = workload(args)
     # iteration count of this solve: the CPU restatement follows the same
     # algorithm, which matches the GPU path iteration for iteration on every
     # pinned case; the count for this workload is measured by the GPU arm

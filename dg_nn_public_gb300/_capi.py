@@ -53,6 +53,7 @@ _SIGNATURES = {
     "dg_info": (_I, [_P, _P, C.c_int32]),
     "dg_launch_count": (C.c_longlong, []),
     "dg_set_kappa": (_I, [_P, _P]),
+    "dg_set_face_kappa": (_I, [_P, C.c_int32]),
     "dg_build_operator": (_I, [_P, _P]),
     "dg_get_bdiag": (_I, [_P, _P, _P, _P]),
     "dg_get_rar": (_I, [_P, _P, _P]),
@@ -65,6 +66,7 @@ _SIGNATURES = {
     "dg_solve_mixed": (_I, [_P, _P, _P, C.c_double, C.c_int32, C.c_int32, C.c_double, _P, _P, _P, _P]),
     "dg_apply_f32": (_I, [_P, _P, _P, _P]),
     "dg_smooth_pc": (_I, [_P, _P, _P, _P, _P]),
+    "dg_precond_f32": (_I, [_P, _P, _P, _P]),
     "dg_set_mixed_options": (_I, [_P, C.c_int32, C.c_double, C.c_int32, C.c_int32]),
     "dg_residual_norm_noalloc": (_I, [_P, _P, _P, _P, _P, _P]),
     "dg_p1cg_sparsity": (_I, [C.c_int64, C.c_int32, _P, C.c_int64, _P, _P, C.c_int64, _P]),

@@ -40,6 +40,7 @@ struct BuildParams {
   double eta, mu;
   int64_t B;
   int* err;               // error word: 1 = non-positive Jacobian
+  int face_kappa;         // interior-face kappa: 0 = (ke + kn) / 2, 1 = 2 ke kn / (ke + kn)
 };
 
 // ---------------------------------------------------------------------------
@@ -233,7 +234,8 @@ __global__ void __launch_bounds__(N* N) build_blocks_kernel(BuildParams p) {
     double ke = p.kappa[e];
     if (s.bct[f] < 0) {
       int nb = s.nbi[f];
-      s.kf[f] = p.mu * 0.5 * (ke + (nb >= 0 ? p.kappa[nb] : ke));
+      const double kn = nb >= 0 ? p.kappa[nb] : ke;
+      s.kf[f] = p.mu * (p.face_kappa ? 2.0 * ke * kn / (ke + kn) : 0.5 * (ke + kn));
     } else if (s.bct[f] == 0) {
       s.kf[f] = p.mu * ke;
     } else {

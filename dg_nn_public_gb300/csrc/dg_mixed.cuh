@@ -4,15 +4,19 @@
 //
 //   outer (FP64):  r = b - A x;  stop when ||r|| <= tol
 //   inner (FP32):  solve A d = r / ||r|| with right-preconditioned flexible
-//                  GMRES(m): z_j = M v_j, w = A z_j, CGS2 (FP64 accumulated
-//                  dot products), Hessenberg least squares in FP64 on the
-//                  host; stops when the Hessenberg residual estimate falls
-//                  below inner_rtol (checked every `chunk` steps)
+//                  GMRES(m): z_j = M v_j, w = A z_j, classical Gram-Schmidt
+//                  (one pass by default, CGS2 optional; FP64 partial sums),
+//                  Hessenberg least squares in FP64 on the host; stops when
+//                  the Hessenberg residual estimate falls below the inner
+//                  target (checked every `chunk` steps)
 //   x += ||r|| * d  (FP64)
 //
-// The FP32 operator, smoother matrices and SFC level values are copies of
-// the FP64 ones (the smoother is the same three-sweep block-Jacobi map), so
-// the inner solve runs the reference's preconditioner in single precision.
+// M is the reference's DG->CG SFC V-cycle in reduced precision: FP32 copies
+// of the operator blocks (FGMRES apply) and of the SFC level values, BF16
+// copies of the blocks and smoother matrices for the preconditioner's
+// smoothing steps, the damped block inverse w A_ee^-1 as smoother (the
+// three-sweep Jacobi map as an option) and an exact dense inverse on the
+// first SFC level small enough.
 
 namespace {
 
@@ -68,6 +72,137 @@ __global__ void dense_matvec_kernel(const float* __restrict__ Ainv, const float*
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if (lane == 0) e[row] = s;
+}
+
+// ---------------------------------------------------------------------------
+// BF16 blocks of P3 tetrahedra (20x20) in a chunked layout for wide loads:
+// the block's columns 0-7, 8-15 and 16-19 form three chunks, each stored as
+// [row m][column within the chunk] (8, 8 and 4 wide).  Row m of a block is
+// then two 16-byte loads and one 8-byte load instead of twenty 2-byte ones,
+// which is what keeps enough bytes in flight to stream the blocks at HBM
+// rate.  Chunk offsets (in elements): 0, 160, 320; a block is 400 elements
+// (800 bytes), so every block and chunk starts on a 16-byte boundary.
+constexpr int kC20Off1 = 160, kC20Off2 = 320;
+
+// destination index of entry (row m, column n) of a block in that layout
+__host__ __device__ __forceinline__ int chunk20_index(int m, int n) {
+  return n < 8 ? m * 8 + n : (n < 16 ? kC20Off1 + m * 8 + (n - 8) : kC20Off2 + m * 4 + (n - 16));
+}
+
+// a: nblock column-major FP64 blocks [blk][n][m] -> chunked BF16 blocks
+__global__ void convert_f64_bf16_chunk20_kernel(const double* __restrict__ a, __nv_bfloat16* __restrict__ b,
+                                                int64_t nblock) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nblock * 400) return;
+  const int64_t blk = k / 400;
+  const int rem = (int)(k - blk * 400);
+  const int n = rem / 20, m = rem % 20;
+  b[blk * 400 + chunk20_index(m, n)] = __float2bfloat16_rn((float)a[k]);
+}
+
+struct Row20 {
+  uint4 a, b;
+  uint2 c;
+};
+
+__device__ __forceinline__ Row20 load_row20(const __nv_bfloat16* __restrict__ blk, int m) {
+  Row20 q;
+  q.a = __ldg(reinterpret_cast<const uint4*>(blk) + m);
+  q.b = __ldg(reinterpret_cast<const uint4*>(blk + kC20Off1) + m);
+  q.c = __ldg(reinterpret_cast<const uint2*>(blk + kC20Off2) + m);
+  return q;
+}
+
+__device__ __forceinline__ Row20 zero_row20() {
+  Row20 q;
+  q.a = make_uint4(0u, 0u, 0u, 0u);
+  q.b = q.a;
+  q.c = make_uint2(0u, 0u);
+  return q;
+}
+
+// the two BF16 values of a 32-bit word (low half = lower column), exactly
+__device__ __forceinline__ float bf_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+
+// acc + sum_n row[n] * v[n], n = 0..19 in order (one FMA chain)
+__device__ __forceinline__ float dot_row20(const Row20& q, const float* v, float acc) {
+  const uint32_t w[10] = {q.a.x, q.a.y, q.a.z, q.a.w, q.b.x, q.b.y, q.b.z, q.b.w, q.c.x, q.c.y};
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    acc = fmaf(bf_lo(w[i]), v[2 * i], acc);
+    acc = fmaf(bf_hi(w[i]), v[2 * i + 1], acc);
+  }
+  return acc;
+}
+
+// residual_kernel<20, 4, EPB, bf16, float, float> on the chunked layout
+// (same flags, same per-thread summation order, so the same results): the
+// block rows (and the smoother row) are loaded into registers before the
+// CTA waits for its x gather, so all of an element's loads are in flight
+// together.
+template <int EPB>
+__global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
+    const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
+    const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
+    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1) {
+  constexpr int N = 20, F = 4;
+  __shared__ float xs[EPB][F + 1][N];
+  __shared__ float rs[EPB][N];
+  __shared__ int nbs[EPB][F];
+  const int le = threadIdx.x / N, m = threadIdx.x % N;
+  const int64_t e = (int64_t)blockIdx.x * EPB + le;
+  const bool valid = e < B;
+  const bool zerox = flags & RF_ZEROX;
+  const bool smooth = flags & RF_SMOOTH;
+  if (valid && m < F) nbs[le][m] = nbe[e * F + m];
+  __syncthreads();
+  Row20 q[F + 1];
+  Row20 wq = zero_row20();
+  const __nv_bfloat16* A = blk + (size_t)e * (F + 1) * N * N;
+  if (valid && !zerox) {
+    q[0] = load_row20(A, m);
+#pragma unroll
+    for (int f = 0; f < F; ++f) q[1 + f] = nbs[le][f] >= 0 ? load_row20(A + (1 + f) * N * N, m) : zero_row20();
+  }
+  if (valid && smooth) wq = load_row20(W + (size_t)e * N * N, m);
+  if (valid && !zerox) {
+    xs[le][0][m] = x[e * N + m];
+#pragma unroll
+    for (int f = 0; f < F; ++f) {
+      const int nb = nbs[le][f];
+      xs[le][1 + f][m] = nb >= 0 ? x[(int64_t)nb * N + m] : 0.0f;
+    }
+  }
+  __syncthreads();
+  float acc = 0.0f;
+  if (valid && !zerox) {
+    acc = dot_row20(q[0], xs[le][0], acc);
+#pragma unroll
+    for (int f = 0; f < F; ++f)
+      if (nbs[le][f] >= 0) acc = dot_row20(q[1 + f], xs[le][1 + f], acc);
+  }
+  float res = 0.0f;
+  if (valid) {
+    res = (b ? b[e * N + m] : 0.0f) - acc;
+    if (r) r[e * N + m] = (flags & RF_NEG) ? -res : res;
+  }
+  if (flags & RF_RESTRICT) {
+    rs[le][m] = res;
+    __syncthreads();
+    constexpr int NC = F;
+    if (valid && m < NC) {
+      float s = 0.0f;
+#pragma unroll
+      for (int n = 0; n < N; ++n) s += (float)P[n * NC + m] * rs[le][n];
+      r1[e * NC + m] = s;
+    }
+  }
+  if (smooth) {
+    rs[le][m] = res;
+    __syncthreads();
+    if (valid) x_out[e * N + m] = (zerox ? 0.0f : xs[le][0][m]) + dot_row20(wq, rs[le], 0.0f);
+  }
 }
 
 // Gauss-Jordan inverse with partial pivoting (host, FP64); false if singular
@@ -171,9 +306,19 @@ int launch_residual16(dg_ctx* c, const float* x, const float* b, float* r, float
 
 // residual in the preconditioner: BF16 blocks when enabled, FP32 otherwise
 int residual_pc(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags, cudaStream_t st) {
-  if (c->precond_bf16)
-    return c->D == 3 ? launch_residual16<3>(c, x, b, r, x_out, flags, st)
-                     : launch_residual16<2>(c, x, b, r, x_out, flags, st);
+  if (c->precond_bf16) {
+    if (c->D == 3) {
+      Mixed& M = mixed_of(c);
+      unsigned g = nblk(c->B, 8);
+      if (g)
+        residual_bf16c20_kernel<8><<<g, 8 * 20, 0, st>>>(M.blk16, M.W16, c->d_nbe, x, b, r, x_out, c->B, flags,
+                                                          c->T.P, M.r1);
+      bump();
+      CKL(c);
+      return DG_OK;
+    }
+    return launch_residual16<2>(c, x, b, r, x_out, flags, st);
+  }
   return residual32(c, x, b, r, x_out, flags, st);
 }
 
@@ -379,10 +524,18 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
       if ((rc = dalloc(c, &M.blk16, nb))) return rc;
       if ((rc = dalloc(c, &M.W16, nw))) return rc;
     }
-    convert_f64_bf16_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk16, (int64_t)nb);
-    bump();
-    convert_f64_bf16_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W16, (int64_t)nw);
-    bump();
+    if (c->D == 3) {   // chunked layout read by residual_bf16c20_kernel
+      convert_f64_bf16_chunk20_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk16,
+                                                                             (int64_t)c->B * (c->F + 1));
+      bump();
+      convert_f64_bf16_chunk20_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W16, (int64_t)c->B);
+      bump();
+    } else {
+      convert_f64_bf16_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk16, (int64_t)nb);
+      bump();
+      convert_f64_bf16_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W16, (int64_t)nw);
+      bump();
+    }
   }
   if (Winv) {
     int herr = 0;
@@ -459,11 +612,179 @@ int ensure_krylov32(dg_ctx* c, int m) {
 
 int norm32(dg_ctx* c, const float* z, double* out, cudaStream_t st) { return norm_t<float>(c, z, out, st); }
 
-// CGS2 of w against V[0..j] (FP32 vectors, FP64 accumulation); writes the
-// FP64 Hessenberg column j and V[j+1].
+// ---------------------------------------------------------------------------
+// FP32 Gram-Schmidt kernels on float4 (vector length a multiple of 4, every
+// vector 16-byte aligned).  Each thread keeps one float4 of z and the same
+// float4 of up to 8 basis vectors in flight per step; per-thread sums are
+// FP32, the block and grid sums FP64, in a fixed order (deterministic).
+
+// partial[bx * KMAXV + i0 + q] = sum over this block's slice of V[i0+q] . z,
+// i0 = 8 * blockIdx.y
+template <int TB>
+__global__ void __launch_bounds__(TB) mdot8_f32_kernel(const float* __restrict__ V, int64_t ld, int nv,
+                                                       const float* __restrict__ z, int64_t n4,
+                                                       double* __restrict__ partial) {
+  __shared__ double red[TB / 32][8];
+  const int i0 = blockIdx.y * 8;
+  const int cnt = min(8, nv - i0);
+  float acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
+  const float4* z4 = reinterpret_cast<const float4*>(z);
+  for (int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x; k < n4; k += (int64_t)gridDim.x * TB) {
+    const float4 zv = z4[k];
+    float4 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      v[q] = q < cnt ? reinterpret_cast<const float4*>(V + (size_t)(i0 + q) * ld)[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      acc[q] = fmaf(v[q].x, zv.x, acc[q]);
+      acc[q] = fmaf(v[q].y, zv.y, acc[q]);
+      acc[q] = fmaf(v[q].z, zv.z, acc[q]);
+      acc[q] = fmaf(v[q].w, zv.w, acc[q]);
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const double a = warp_sum((double)acc[q]);
+    if (lane == 0) red[wid][q] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x < cnt) {
+    double s = 0.0;
+    for (int w = 0; w < TB / 32; ++w) s += red[w][threadIdx.x];
+    partial[(int64_t)blockIdx.x * KMAXV + i0 + threadIdx.x] = s;
+  }
+}
+
+// z -= sum_i V[i] h[i] (nv <= 256); with want_norm also
+// partial[bx * KMAXV] = this block's slice of |z_new|^2
+template <int TB>
+__global__ void __launch_bounds__(TB) axpy8_f32_kernel(const float* __restrict__ V, int64_t ld, int nv,
+                                                       const double* __restrict__ h, float* __restrict__ z,
+                                                       int64_t n4, double* __restrict__ partial, int want_norm) {
+  __shared__ float hs[256];
+  __shared__ double red[TB / 32];
+  for (int i = threadIdx.x; i < nv; i += TB) hs[i] = (float)h[i];
+  __syncthreads();
+  float acc = 0.0f;
+  float4* z4 = reinterpret_cast<float4*>(z);
+  for (int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x; k < n4; k += (int64_t)gridDim.x * TB) {
+    float4 zv = z4[k];
+    for (int i0 = 0; i0 < nv; i0 += 8) {
+      float4 v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        v[q] = (i0 + q < nv) ? reinterpret_cast<const float4*>(V + (size_t)(i0 + q) * ld)[k]
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float hq = (i0 + q < nv) ? hs[i0 + q] : 0.0f;
+        zv.x -= v[q].x * hq;
+        zv.y -= v[q].y * hq;
+        zv.z -= v[q].z * hq;
+        zv.w -= v[q].w * hq;
+      }
+    }
+    z4[k] = zv;
+    if (want_norm) {
+      acc = fmaf(zv.x, zv.x, acc);
+      acc = fmaf(zv.y, zv.y, acc);
+      acc = fmaf(zv.z, zv.z, acc);
+      acc = fmaf(zv.w, zv.w, acc);
+    }
+  }
+  if (!want_norm) return;
+  const double a = warp_sum((double)acc);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < TB / 32; ++w) s += red[w];
+    partial[(int64_t)blockIdx.x * KMAXV] = s;
+  }
+}
+
+// Hessenberg column j: Hc[i] = h1[i] (+ h2[i] when h2) for i < nv;
+// Hc[nv] = |z| = sqrt(sum of the norm partials); *inv = 1 / |z| in FP32.
+// One block, fixed summation order.
+__global__ void cgs_finish_kernel(const double* __restrict__ partial, int nblk, const double* __restrict__ h1,
+                                  const double* __restrict__ h2, int nv, double* __restrict__ Hc,
+                                  float* __restrict__ inv) {
+  __shared__ double red[32];
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) Hc[i] = h2 ? h1[i] + h2[i] : h1[i];
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) s += partial[(int64_t)b * KMAXV];
+  s = warp_sum(s);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) t += red[w];
+    t = sqrt(t);
+    Hc[nv] = t;
+    *inv = (float)(1.0 / t);
+  }
+}
+
+// v = z * (*inv), float4
+__global__ void scale4_f32_kernel(const float* __restrict__ z, const float* __restrict__ inv, float* __restrict__ v,
+                                  int64_t n4) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n4) return;
+  const float s = *inv;
+  float4 a = reinterpret_cast<const float4*>(z)[k];
+  a.x *= s;
+  a.y *= s;
+  a.z *= s;
+  a.w *= s;
+  reinterpret_cast<float4*>(v)[k] = a;
+}
+
+// h[0..nv) = V^T z with the float4 kernels (nv <= KMAXV per call)
+int mdot4_f32(dg_ctx* c, const float* V, int nv, const float* z, double* h, cudaStream_t st) {
+  const int64_t n4 = c->nonods / 4;
+  for (int off = 0; off < nv; off += KMAXV) {
+    const int cnt = std::min(KMAXV, nv - off);
+    dim3 grid(c->nred, (cnt + 7) / 8);
+    mdot8_f32_kernel<RED_TB><<<grid, RED_TB, 0, st>>>(V + (size_t)off * c->nonods, c->nonods, cnt, z, n4, c->d_part);
+    bump();
+    reduce_partial_kernel<<<cnt, 128, 0, st>>>(c->d_part, c->nred, cnt, h + off, 0, 0);
+    bump();
+  }
+  return DG_OK;
+}
+
+// Gram-Schmidt of w against V[0..j] (FP32 vectors; CGS2 or, with
+// mixed_cgs_passes = 1, one classical pass); writes the FP64 Hessenberg
+// column j and V[j+1] = w / |w|.
 int cgs2_32(dg_ctx* c, int j, float* w, int m, cudaStream_t st) {
   Mixed& M = mixed_of(c);
-  return cgs2_t<float>(c, M.V, M.H, j, w, m, st);
+  if (c->nonods % 4 != 0) return cgs2_t<float>(c, M.V, M.H, j, w, m, st);
+  const int nv = j + 1;
+  const int64_t n4 = c->nonods / 4;
+  double* Hc = M.H + (size_t)j * (m + 1);
+  const bool two = c->mixed_cgs_passes != 1;
+  float* inv = reinterpret_cast<float*>(c->d_scal + 1);
+  int rc;
+  if ((rc = mdot4_f32(c, M.V, nv, w, c->d_h1, st))) return rc;
+  axpy8_f32_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(M.V, c->nonods, nv, c->d_h1, w, n4, c->d_part, two ? 0 : 1);
+  bump();
+  if (two) {
+    if ((rc = mdot4_f32(c, M.V, nv, w, c->d_h2, st))) return rc;
+    axpy8_f32_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(M.V, c->nonods, nv, c->d_h2, w, n4, c->d_part, 1);
+    bump();
+  }
+  cgs_finish_kernel<<<1, 256, 0, st>>>(c->d_part, c->nred, c->d_h1, two ? c->d_h2 : nullptr, nv, Hc, inv);
+  bump();
+  scale4_f32_kernel<<<nblk(n4, 256), 256, 0, st>>>(w, inv, M.V + (size_t)nv * c->nonods, n4);
+  bump();
+  CKL(c);
+  return DG_OK;
 }
 
 // inner Arnoldi steps j0 .. j0+cnt-1: z_j = M v_j (kept), w = A z_j, CGS2
@@ -669,6 +990,24 @@ extern "C" int dg_apply_f32(dg_ctx* c, const float* x, float* y, void* stream) {
     c->mixed_version = c->build_version;
   }
   return residual32(c, x, nullptr, y, nullptr, RF_NEG, st);
+}
+
+// z = the mixed preconditioner (FP32 V-cycle with the BF16/FP32 block copies)
+// applied once to r, FP32 vectors -- the reduced-precision counterpart of
+// _um_left_precond.
+extern "C" int dg_precond_f32(dg_ctx* c, const float* r, float* z, void* stream) {
+  if (!c || !r || !z) return set_thread_error(DG_ERR_ARG, "dg_precond_f32: null argument");
+  if (r == z) return fail(c, DG_ERR_ARG, "dg_precond_f32: z must not alias r");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_precond_f32: operator not built");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  CK(c, cudaSetDevice(c->dev));
+  Mixed& M = mixed_of(c);
+  int rc;
+  if (!M.built || c->mixed_version != c->build_version) {
+    if ((rc = build_mixed(c, st))) return rc;
+    c->mixed_version = c->build_version;
+  }
+  return precond32(c, r, z, st);
 }
 
 // One smoothing step of the mixed preconditioner on FP32 vectors:

@@ -49,6 +49,7 @@ struct dg_ctx {
   // host copies
   std::vector<int64_t> p1cg, sfc;      // (B*NC), (ncg) 1-based
   std::vector<double> kappa;
+  int face_kappa = 0;   // interior-face kappa: 0 arithmetic mean (reference), 1 harmonic mean
   std::vector<int> bf_elem, bf_face, bf_type;
   // device allocations (released in dg_destroy)
   std::vector<void*> allocs;
@@ -103,6 +104,10 @@ struct dg_ctx {
   // sweeps, 1 = damped exact block inverse w_b * A_ee^{-1}
   int mixed_smoother = 1;
   double mixed_smooth_w = 0.8;
+  // Gram-Schmidt passes of the FP32 inner Arnoldi (1 = classical GS with
+  // FP64 partial sums; 2 = CGS2).  One pass: the FP64 refinement bounds the
+  // result, and c2 / c3 need the same inner iterations either way.
+  int mixed_cgs_passes = 1;
   // captured Arnoldi cycle (GMRES(m) inner loop) replayed as one CUDA graph
   bool use_graph = true;
   cudaStream_t cap_stream = nullptr;
@@ -189,6 +194,7 @@ int launch_build(dg_ctx* c, cudaStream_t st) {
   p.mu = c->cfg.mu_f;
   p.B = c->B;
   p.err = c->d_err;
+  p.face_kappa = c->face_kappa;
   auto k = build_blocks_kernel<D, E::N, E::F, E::VG, E::SG>;
   CK(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm)));
   if (c->B > 0) k<<<(unsigned)c->B, E::N * E::N, sizeof(Sm), st>>>(p);
@@ -666,6 +672,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (mw && mw[0]) c->mixed_smooth_w = std::atof(mw);
     const char* pb = std::getenv("DG_PRECOND_BF16");
     if (pb && pb[0]) c->precond_bf16 = pb[0] != '0';
+    const char* mc = std::getenv("DG_MIXED_CGS");
+    if (mc && mc[0]) c->mixed_cgs_passes = std::atoi(mc) == 1 ? 1 : 2;
   }
   {
     const char* ng = std::getenv("DG_NO_GRAPH");
@@ -817,6 +825,14 @@ int dg_set_kappa(dg_ctx* c, const double* kappa) {
   CK(c, cudaSetDevice(c->dev));
   CK(c, cudaMemcpy(c->d_kappa, c->kappa.data(), sizeof(double) * c->B, cudaMemcpyHostToDevice));
   c->built = false;
+  return DG_OK;
+}
+
+int dg_set_face_kappa(dg_ctx* c, int32_t mode) {
+  if (!c) return set_thread_error(DG_ERR_ARG, "dg_set_face_kappa: null context");
+  if (mode != 0 && mode != 1) return fail(c, DG_ERR_ARG, "dg_set_face_kappa: mode 0 (mean) or 1 (harmonic)");
+  if (c->face_kappa != mode) c->built = false;
+  c->face_kappa = mode;
   return DG_OK;
 }
 

@@ -138,6 +138,13 @@ class DGSolver:
         self._chk(self._lib.dg_set_kappa(self._ctx, None if k is None else k.ctypes.data))
         self.built = False
 
+    def set_face_kappa(self, mode: str):
+        """Interior-face diffusivity: 'mean' = (k_e + k_nb)/2 (the reference's
+        variable-property convention) or 'harmonic' = 2 k_e k_nb/(k_e + k_nb)
+        (weighted-average SIP, coercive under large jumps).  Rebuild after."""
+        self._chk(self._lib.dg_set_face_kappa(self._ctx, {"mean": 0, "harmonic": 1}[mode]))
+        self.built = False
+
     def build_operator(self):
         self._chk(self._lib.dg_build_operator(self._ctx, self._stream()))
         self.built = True
@@ -195,6 +202,15 @@ class DGSolver:
         y = torch.empty_like(x) if y is None else y
         self._chk(self._lib.dg_apply_f32(self._ctx, x.data_ptr(), y.data_ptr(), self._stream()))
         return y
+
+    def precond_f32(self, r, z=None):
+        """z = the mixed preconditioner applied once to r (FP32 CUDA tensors)."""
+        torch = _torch()
+        if not (r.is_cuda and r.dtype == torch.float32 and r.is_contiguous() and r.numel() == self.nonods):
+            raise ValueError("expected a contiguous FP32 CUDA tensor with %d entries" % self.nonods)
+        z = torch.empty_like(r) if z is None else z
+        self._chk(self._lib.dg_precond_f32(self._ctx, r.data_ptr(), z.data_ptr(), self._stream()))
+        return z
 
     def smooth_pc(self, x, b, x_out=None):
         """One smoothing step of the mixed preconditioner, x_out = x + W (b - A x),

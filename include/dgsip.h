@@ -97,6 +97,14 @@ long long dg_launch_count(void);
 /* Per-element diffusivity (z05-ns/volume_mf_um_diff_varprop.py:422-426,
  * 567, 682); NULL restores kappa = 1. */
 int dg_set_kappa(dg_ctx* ctx, const double* kappa /* [host] (nele) or NULL */);
+/* Interior-face diffusivity of the SIP form: mode 0 = (kappa_e + kappa_nb)/2
+ * on all three face terms, the reference's variable-property convention
+ * (z05-ns/volume_mf_um_diff_varprop.py:422-426); mode 1 = the harmonic mean
+ * 2 kappa_e kappa_nb / (kappa_e + kappa_nb), the weighted-average SIP of Ern,
+ * Stephansen and Zunino (IMA J. Numer. Anal. 29, 2009), which stays coercive
+ * under large kappa jumps (no counterpart in the reference).  Takes effect
+ * at the next dg_build_operator. */
+int dg_set_face_kappa(dg_ctx* ctx, int32_t mode);
 /* Assemble the stored element blocks, the block diagonal, the colour-probe
  * Galerkin P1CG operator and the SFC levels.  Replaces get_bdiag_diag()
  * (z06/get_bdiag_diag.py:30-62) and _get_RAR_and_sfc_data_Um()
@@ -150,6 +158,11 @@ int dg_solve_mixed(dg_ctx* ctx, double* x, const double* b, double tol, int32_t 
                    double inner_rtol, int32_t* its, double* res_norm, int32_t* outer, void* stream);
 /* y = A x with the FP32 copy of the operator blocks (FP32 vectors). */
 int dg_apply_f32(dg_ctx* ctx, const float* x, float* y, void* stream);
+/* z = the mixed-precision preconditioner applied once to r (FP32 vectors):
+ * the DG->CG SFC V-cycle of dg_precond with the FP32/BF16 block copies and
+ * the options of dg_set_mixed_options -- the reduced-precision counterpart
+ * of _um_left_precond (z06/volume_mf_diff.py:1934-2029).  z must not alias r. */
+int dg_precond_f32(dg_ctx* ctx, const float* r, float* z, void* stream);
 /* One smoothing step of the mixed preconditioner on FP32 vectors,
  * x_out = x + W (b - A x) with the preconditioner's block copies (BF16 when
  * precond_bf16) -- the reduced-precision counterpart of

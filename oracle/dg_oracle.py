@@ -26,6 +26,9 @@ Per-element diffusivity kappa follows the reference's variable-property
 convention (z05-ns/volume_mf_um_diff_varprop.py:422-426, 567, 682): the
 volume term uses kappa_e, interior faces use (kappa_e + kappa_nb) / 2 on all
 three face terms, Dirichlet faces use kappa_e.  kappa = 1 reproduces z06.
+face_kappa="harmonic" replaces the interior-face value by the harmonic mean
+2 kappa_e kappa_nb / (kappa_e + kappa_nb): the weighted-average SIP of Ern,
+Stephansen and Zunino (IMA J. Numer. Anal. 29, 2009), not in the reference.
 """
 from __future__ import annotations
 
@@ -76,7 +79,7 @@ class OracleDG:
     """
 
     def __init__(self, mesh, el, drst, eta_e=90.0, mu_f=1.0, kappa=None, jac_wei=2.0 / 3.0,
-                 pre_smooth_its=3, post_smooth_its=3):
+                 pre_smooth_its=3, post_smooth_its=3, face_kappa="mean"):
         self.m, self.el = mesh, el
         self.D = mesh.ndim
         self.F = self.D + 1
@@ -86,6 +89,9 @@ class OracleDG:
         self.pre_smooth_its, self.post_smooth_its = pre_smooth_its, post_smooth_its
         self.drst = np.asarray(drst, dtype=np.float64)
         self.kappa = np.ones(self.B) if kappa is None else np.asarray(kappa, dtype=np.float64)
+        if face_kappa not in ("mean", "harmonic"):
+            raise ValueError("face_kappa: 'mean' or 'harmonic'")
+        self.face_kappa = face_kappa
         self._geometry()
         self._faces()
 
@@ -141,7 +147,8 @@ class OracleDG:
         self.E_b, self.f_b = self.F_b // F, self.F_b % F
         aln = np.asarray(m.alnmt)[self.F_i]
         self.align = np.asarray(self.el.gi_align)[aln]        # (S_int, SG)
-        self.kface = 0.5 * (self.kappa[self.E_i] + self.kappa[self.E_inb])
+        ke, kn = self.kappa[self.E_i], self.kappa[self.E_inb]
+        self.kface = 2.0 * ke * kn / (ke + kn) if self.face_kappa == "harmonic" else 0.5 * (ke + kn)
 
     # ------------------------------------------------------------------
     # operator apply (volume_mf_diff.py:403-617, 909-1369, 1459-1639)

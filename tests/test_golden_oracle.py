@@ -111,3 +111,34 @@ def test_upsample_index_matches_torch():
         src = torch.arange(nc, dtype=torch.float64).view(1, 1, -1)
         got = up(src).view(-1).numpy().astype(np.int64)
         assert np.array_equal(got, upsample_index(nf, nc)), nf
+
+
+def test_face_kappa_coercivity_under_a_kappa_jump():
+    """kappa = 1 except one neighbour of an interior element at 1000: with the
+    reference's arithmetic face mean, that face's consistency terms carry
+    kappa ~ 500 against the element's volume term of 1, and its diagonal
+    block is indefinite; the harmonic face mean (weighted-average SIP) keeps
+    every diagonal block positive definite (smallest/largest eigenvalue
+    ~0.056) and the operator symmetric."""
+    from dg_nn_public_gb300 import element, mesh
+    from oracle.dg_oracle import OracleDG
+    m = mesh.build_mesh("tet", 3, seed=0)
+    nbf = np.asarray(m.nbf).reshape(m.nele, 4)
+    t = np.asarray(m.glb_bcface_type).reshape(m.nele, 4)
+    e = [k for k in range(m.nele) if (t[k] < 0).all()][0]
+    kappa = np.ones(m.nele)
+    kappa[int(nbf[e, 0]) // 4] = 1000.0
+    el = element.p3_element(3)
+    lo = {}
+    for mode in ("mean", "harmonic"):
+        O = OracleDG(m, el, element.drst_duv(3), kappa=kappa, face_kappa=mode)
+        K = O.bdiag()[0]
+        ev = np.linalg.eigvalsh(K[e])
+        lo[mode] = ev[0] / ev[-1]
+        if mode == "harmonic":
+            assert all(np.linalg.eigvalsh(K[k])[0] > 0 for k in range(m.nele))
+            rng = np.random.default_rng(0)
+            x, y = rng.standard_normal((2, m.nele * m.nloc))
+            xAy, yAx = x @ O.apply_Ax(y).reshape(-1), y @ O.apply_Ax(x).reshape(-1)
+            assert abs(xAy - yAx) <= 1e-12 * abs(xAy)
+    assert lo["mean"] < 0 < 0.05 < lo["harmonic"], lo

@@ -125,15 +125,17 @@ def test_tet8_against_oracle(tet8):
     assert rel(N(s.precond(T(b))), O.precond(b, ctx)) < 1e-11
 
 
-def test_kappa_operator_against_oracle(tet8):
+@pytest.mark.parametrize("face_kappa", ["mean", "harmonic"])
+def test_kappa_operator_against_oracle(tet8, face_kappa):
     m, order, s0, _ = tet8
     rng = np.random.default_rng(5)
     kappa = np.exp(rng.standard_normal(m.nele))
     el = element.p3_element(3)
     s = DGSolver(m, order, SolverConfig(), el)
     s.set_kappa(kappa)
+    s.set_face_kappa(face_kappa)
     s.build_operator()
-    O = OracleDG(m, el, element.drst_duv(3), kappa=kappa)
+    O = OracleDG(m, el, element.drst_duv(3), kappa=kappa, face_kappa=face_kappa)
     x = rng.standard_normal(s.nonods)
     b = rng.standard_normal(s.nonods)
     assert rel(N(s.residual(T(x), T(b))), O.residual(x, b)) < STAGE_TOL
