@@ -205,6 +205,202 @@ __global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same smoothing / residual step as a persistent kernel that streams the
+// blocks with the Tensor Memory Accelerator: MINB CTAs per SM walk the
+// element groups g = blockIdx.x, blockIdx.x + gridDim.x, ...; a group's EPB
+// elements are consecutive, so their BF16 blocks (EPB * 4000 bytes) and
+// smoother matrices (EPB * 800 bytes) are two contiguous bulk copies
+// (cp.async.bulk, completion on an mbarrier) into a ring of S shared-memory
+// stages.  While group k is
+// computed, groups k+1 .. k+S-1 are in flight, and the x / b
+// gathers of group k+1 (ordinary loads, from L2) are issued before group k's
+// wait, so neither the block stream nor the gathers stall on a per-CTA
+// round trip.  Every mbarrier wait is bounded: on time-out the kernel sets
+// *err = 3, waits (bounded) for its own copies in flight and returns.
+// A group of EPB elements needs EPB * 4000 bytes of blocks and EPB * 800
+// bytes of smoother matrices per stage.
+template <int EPB>
+struct TmaGroup {
+  static constexpr int ABytes = EPB * 5 * 400 * 2;
+  static constexpr int WBytes = EPB * 400 * 2;
+  static constexpr int StageBytes = ABytes + WBytes;
+};
+constexpr uint32_t kTmaSpinLimit = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  uint64_t state;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+               : "=l"(state)
+               : "r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+  (void)state;
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait; false on time-out
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kTmaSpinLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ Row20 lds_row20(const unsigned char* blk, int m) {
+  Row20 q;
+  q.a = *reinterpret_cast<const uint4*>(blk + 16 * m);
+  q.b = *reinterpret_cast<const uint4*>(blk + 2 * kC20Off1 + 16 * m);
+  q.c = *reinterpret_cast<const uint2*>(blk + 2 * kC20Off2 + 8 * m);
+  return q;
+}
+
+template <int EPB, int S, int MINB>
+__global__ void __launch_bounds__(EPB * 20, MINB) residual_bf16_tma_kernel(
+    const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
+    const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
+    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err) {
+  constexpr int N = 20, F = 4;
+  constexpr int kTmaABytes = TmaGroup<EPB>::ABytes, kTmaStageBytes = TmaGroup<EPB>::StageBytes;
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  __shared__ __align__(8) uint64_t bar[S];
+  __shared__ float xs[EPB][F + 1][N];
+  __shared__ float rs[EPB][N];
+  __shared__ float Ps[N][F];
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x;
+  const int le = tid / N, m = tid % N;
+  const bool zerox = flags & RF_ZEROX;
+  const bool smooth = flags & RF_SMOOTH;
+  const bool restrict_ = flags & RF_RESTRICT;
+  const int64_t ngroups = (B + EPB - 1) / EPB;
+  const int64_t stride = gridDim.x;
+  if (tid < N * F) Ps[tid / F][tid % F] = (float)P[tid];
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // copies of the CTA's k-th group go to stage k % S, phase parity (k / S) & 1
+  auto issue = [&](int64_t k) {
+    const int64_t g = blockIdx.x + k * stride;
+    if (g >= ngroups) return;
+    const int64_t e0 = g * EPB;
+    const uint32_t ne = (uint32_t)((B - e0) < EPB ? (B - e0) : EPB);
+    const uint32_t ba = zerox ? 0u : ne * 4000u, bw = smooth ? ne * 800u : 0u;
+    unsigned char* st = tma_smem + (size_t)(k % S) * kTmaStageBytes;
+    mbar_expect_tx(&bar[k % S], ba + bw);
+    if (ba) bulk_copy_g2s(st, blk + e0 * 2000, ba, &bar[k % S]);
+    if (bw) bulk_copy_g2s(st + kTmaABytes, W + e0 * 400, bw, &bar[k % S]);
+  };
+  if (tid == 0)
+    for (int k = 0; k < S; ++k) issue(k);
+  // register prefetch of the gathers of the next group
+  auto load_nb = [&](int64_t g) {
+    const int64_t e = g * EPB + le;
+    return (g < ngroups && e < B) ? reinterpret_cast<const int4*>(nbe)[e] : make_int4(-1, -1, -1, -1);
+  };
+  int4 nb_cur = load_nb(blockIdx.x);
+  float x_own = 0.0f, x_nb[F] = {0.0f, 0.0f, 0.0f, 0.0f}, b_cur = 0.0f;
+  auto load_x = [&](int64_t g, const int4& nb) {
+    const int64_t e = g * EPB + le;
+    const bool ok = g < ngroups && e < B;
+    x_own = (ok && !zerox) ? x[e * N + m] : 0.0f;
+    const int nbv[F] = {nb.x, nb.y, nb.z, nb.w};
+#pragma unroll
+    for (int f = 0; f < F; ++f) x_nb[f] = (ok && !zerox && nbv[f] >= 0) ? x[(int64_t)nbv[f] * N + m] : 0.0f;
+    b_cur = (ok && b) ? b[e * N + m] : 0.0f;
+  };
+  load_x(blockIdx.x, nb_cur);
+  int4 nb_next = load_nb(blockIdx.x + stride);
+  int64_t k = 0;
+  for (int64_t g = blockIdx.x; g < ngroups; g += stride, ++k) {
+    const int64_t e = g * EPB + le;
+    const bool valid = e < B;
+    const int nbv[F] = {nb_cur.x, nb_cur.y, nb_cur.z, nb_cur.w};
+    xs[le][0][m] = x_own;
+#pragma unroll
+    for (int f = 0; f < F; ++f) xs[le][1 + f][m] = x_nb[f];
+    const float bb = b_cur;
+    // gathers of the next group, in flight during this group's work
+    nb_cur = nb_next;
+    load_x(g + stride, nb_cur);
+    nb_next = load_nb(g + 2 * stride);
+    const int s = (int)(k % S);
+    if (!mbar_wait_bounded(&bar[s], (uint32_t)((k / S) & 1))) {
+      atomicExch(err, 3);
+      abort_flag = 1;
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    const unsigned char* st = tma_smem + (size_t)s * kTmaStageBytes;
+    float acc = 0.0f;
+    if (valid && !zerox) {
+      const unsigned char* Ae = st + (size_t)le * 4000;
+      acc = dot_row20(lds_row20(Ae, m), xs[le][0], acc);
+#pragma unroll
+      for (int f = 0; f < F; ++f)
+        if (nbv[f] >= 0) acc = dot_row20(lds_row20(Ae + (1 + f) * 800, m), xs[le][1 + f], acc);
+    }
+    float res = 0.0f;
+    if (valid) {
+      res = bb - acc;
+      if (r) r[e * N + m] = (flags & RF_NEG) ? -res : res;
+    }
+    if (restrict_ || smooth) {
+      rs[le][m] = res;
+      __syncthreads();
+      if (restrict_ && valid && m < F) {
+        float t = 0.0f;
+#pragma unroll
+        for (int n = 0; n < N; ++n) t += Ps[n][m] * rs[le][n];
+        r1[e * F + m] = t;
+      }
+      if (smooth && valid)
+        x_out[e * N + m] = (zerox ? 0.0f : xs[le][0][m]) +
+                           dot_row20(lds_row20(st + kTmaABytes + (size_t)le * 800, m), rs[le], 0.0f);
+    }
+    __syncthreads();   // stage s and xs / rs free again
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(k + S);
+    }
+  }
+  if (abort_flag && tid == 0) {
+    // drain this CTA's copies still in flight (groups k .. k+S-1), bounded
+    for (int64_t j = k; j < k + S; ++j) {
+      if (blockIdx.x + j * stride >= ngroups) break;
+      (void)mbar_wait_bounded(&bar[j % S], (uint32_t)((j / S) & 1));
+    }
+  }
+}
+
 // Gauss-Jordan inverse with partial pivoting (host, FP64); false if singular
 bool invert_dense(std::vector<double>& A, int n, std::vector<double>& inv) {
   inv.assign((size_t)n * n, 0.0);
@@ -304,9 +500,42 @@ int launch_residual16(dg_ctx* c, const float* x, const float* b, float* r, float
   return DG_OK;
 }
 
+template <int EPB, int S, int MINB>
+int launch_bf16_tma(dg_ctx* c, Mixed& M, const float* x, const float* b, float* r, float* x_out, int flags,
+                    cudaStream_t st) {
+  const int64_t ngroups = (c->B + EPB - 1) / EPB;
+  const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
+  if (g)
+    residual_bf16_tma_kernel<EPB, S, MINB><<<g, EPB * 20, S * TmaGroup<EPB>::StageBytes, st>>>(
+        M.blk16, M.W16, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, M.r1, c->d_err);
+  bump();
+  CKL(c);
+  return DG_OK;
+}
+
+template <int EPB, int S, int MINB>
+int set_tma_smem(dg_ctx* c) {
+  CK(c, cudaFuncSetAttribute(residual_bf16_tma_kernel<EPB, S, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             S * TmaGroup<EPB>::StageBytes));
+  return DG_OK;
+}
+
 // residual in the preconditioner: BF16 blocks when enabled, FP32 otherwise
 int residual_pc(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags, cudaStream_t st) {
   if (c->precond_bf16) {
+    if (c->D == 3 && c->bf16_tma) {
+      Mixed& M = mixed_of(c);
+      // launch shapes (elements per group, stages, CTAs per SM); c2 sweep:
+      // (8,5,1) 49.3 us, (8,3,1) 49.2, (8,2,2) 41.2, (4,2,4) 41.3,
+      // (4,2,5) 41.6, (4,1,8) 41.5, (6,2,3) 40.7 -- several CTAs per SM hide
+      // the per-group round trip that one CTA per SM cannot
+      switch (c->tma_variant) {
+        case 1: return launch_bf16_tma<8, 2, 2>(c, M, x, b, r, x_out, flags, st);
+        case 2: return launch_bf16_tma<4, 2, 4>(c, M, x, b, r, x_out, flags, st);
+        case 3: return launch_bf16_tma<8, 5, 1>(c, M, x, b, r, x_out, flags, st);
+        default: return launch_bf16_tma<6, 2, 3>(c, M, x, b, r, x_out, flags, st);
+      }
+    }
     if (c->D == 3) {
       Mixed& M = mixed_of(c);
       unsigned g = nblk(c->B, 8);
@@ -492,6 +721,9 @@ __global__ void convert_f64_bf16_kernel(const double* __restrict__ a, __nv_bfloa
 int build_mixed(dg_ctx* c, cudaStream_t st) {
   Mixed& M = mixed_of(c);
   int rc;
+  if ((rc = set_tma_smem<6, 2, 3>(c)) || (rc = set_tma_smem<8, 2, 2>(c)) || (rc = set_tma_smem<4, 2, 4>(c)) ||
+      (rc = set_tma_smem<8, 5, 1>(c)))
+    return rc;
   const size_t nb = (size_t)c->B * (c->F + 1) * c->N * c->N;
   const size_t nw = (size_t)c->B * c->N * c->N;
   if (!M.blk) {
@@ -884,6 +1116,7 @@ extern "C" int dg_solve_mixed(dg_ctx* c, double* x, const double* b, double tol,
     c->mixed_version = c->build_version;
   }
   if ((rc = ensure_krylov32(c, m))) return rc;
+  CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));   // bulk-copy wait time-outs land here
   const int chunk = std::min(10, m);
   const int64_t n = c->nonods;
   double* r64 = c->d_t2;
@@ -970,6 +1203,15 @@ extern "C" int dg_solve_mixed(dg_ctx* c, double* x, const double* b, double tol,
   if (its_out) *its_out = its;
   if (res_out) *res_out = rn;
   if (outer_out) *outer_out = outer;
+  {
+    int herr = 0;
+    CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    if (herr == 3) {
+      c->err = "mixed solve: a bulk-copy wait of the preconditioner timed out";
+      return DG_ERR_CUDA;
+    }
+  }
   if (status == DG_OK && rn > tol) {
     c->err = "mixed solve reached the iteration limit";
     return DG_ERR_NOCONV;

@@ -99,6 +99,9 @@ struct dg_ctx {
   int dense_n = 0;
   // mixed preconditioner reads BF16 copies of the blocks / smoother matrices
   bool precond_bf16 = true;
+  // ... streamed by the persistent bulk-copy (TMA) kernel (3D)
+  bool bf16_tma = true;
+  int tma_variant = 0;   // elements per group / stages / CTAs per SM of that kernel
   bool verbose = false;
   // mixed preconditioner smoother: 0 = the reference's three point-Jacobi
   // sweeps, 1 = damped exact block inverse w_b * A_ee^{-1}
@@ -672,6 +675,10 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (mw && mw[0]) c->mixed_smooth_w = std::atof(mw);
     const char* pb = std::getenv("DG_PRECOND_BF16");
     if (pb && pb[0]) c->precond_bf16 = pb[0] != '0';
+    const char* bt = std::getenv("DG_BF16_TMA");
+    if (bt && bt[0]) c->bf16_tma = bt[0] != '0';
+    const char* tv = std::getenv("DG_TMA_VARIANT");
+    if (tv && tv[0]) c->tma_variant = std::atoi(tv);
     const char* mc = std::getenv("DG_MIXED_CGS");
     if (mc && mc[0]) c->mixed_cgs_passes = std::atoi(mc) == 1 ? 1 : 2;
   }
