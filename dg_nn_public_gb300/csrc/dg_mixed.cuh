@@ -206,24 +206,86 @@ __global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
 }
 
 // ---------------------------------------------------------------------------
-// The same smoothing / residual step as a persistent kernel that streams the
-// blocks with the Tensor Memory Accelerator: MINB CTAs per SM walk the
-// element groups g = blockIdx.x, blockIdx.x + gridDim.x, ...; a group's EPB
-// elements are consecutive, so their BF16 blocks (EPB * 4000 bytes) and
-// smoother matrices (EPB * 800 bytes) are two contiguous bulk copies
-// (cp.async.bulk, completion on an mbarrier) into a ring of S shared-memory
-// stages.  While group k is
-// computed, groups k+1 .. k+S-1 are in flight, and the x / b
+// FP32 blocks of P3 tetrahedra in the matching chunked layout: five chunks
+// of four columns, each [row m][column within the chunk], so row m of a
+// block is five 16-byte loads (chunk c at byte 320 c + 16 m).
+__host__ __device__ __forceinline__ int chunk20f_index(int m, int n) { return (n >> 2) * 80 + m * 4 + (n & 3); }
+
+__global__ void convert_f64_f32_chunk20_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t nblock) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nblock * 400) return;
+  const int64_t blk = k / 400;
+  const int rem = (int)(k - blk * 400);
+  const int n = rem / 20, m = rem % 20;
+  b[blk * 400 + chunk20f_index(m, n)] = (float)a[k];
+}
+
+struct Row20f {
+  float4 c[5];
+};
+
+// one block row in shared memory, per storage type, and its dot product with
+// v[0..19] as one FMA chain in column order (the order of residual_kernel)
+template <typename MT>
+struct Chunk20;
+
+template <>
+struct Chunk20<__nv_bfloat16> {
+  using Row = Row20;
+  static constexpr int BlockBytes = 800;
+  static __device__ __forceinline__ Row lds(const unsigned char* blk, int m) {
+    Row q;
+    q.a = *reinterpret_cast<const uint4*>(blk + 16 * m);
+    q.b = *reinterpret_cast<const uint4*>(blk + 2 * kC20Off1 + 16 * m);
+    q.c = *reinterpret_cast<const uint2*>(blk + 2 * kC20Off2 + 8 * m);
+    return q;
+  }
+  static __device__ __forceinline__ float dot(const Row& q, const float* v, float acc) {
+    return dot_row20(q, v, acc);
+  }
+};
+
+template <>
+struct Chunk20<float> {
+  using Row = Row20f;
+  static constexpr int BlockBytes = 1600;
+  static __device__ __forceinline__ Row lds(const unsigned char* blk, int m) {
+    Row q;
+#pragma unroll
+    for (int c = 0; c < 5; ++c) q.c[c] = *reinterpret_cast<const float4*>(blk + 320 * c + 16 * m);
+    return q;
+  }
+  static __device__ __forceinline__ float dot(const Row& q, const float* v, float acc) {
+#pragma unroll
+    for (int c = 0; c < 5; ++c) {
+      acc = fmaf(q.c[c].x, v[4 * c], acc);
+      acc = fmaf(q.c[c].y, v[4 * c + 1], acc);
+      acc = fmaf(q.c[c].z, v[4 * c + 2], acc);
+      acc = fmaf(q.c[c].w, v[4 * c + 3], acc);
+    }
+    return acc;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// The residual / smoothing step of residual_kernel<20, 4, ., MT, float,
+// float> as a persistent kernel that streams the blocks with the Tensor
+// Memory Accelerator: MINB CTAs per SM walk the element groups
+// g = blockIdx.x, blockIdx.x + gridDim.x, ...; a group's EPB elements are
+// consecutive, so their blocks (EPB * 5 blocks) and, with WITH_W, their
+// smoother matrices are two contiguous bulk copies (cp.async.bulk,
+// completion on an mbarrier) into a ring of S shared-memory stages.  While
+// group k is computed, groups k+1 .. k+S-1 are in flight, and the x / b
 // gathers of group k+1 (ordinary loads, from L2) are issued before group k's
-// wait, so neither the block stream nor the gathers stall on a per-CTA
-// round trip.  Every mbarrier wait is bounded: on time-out the kernel sets
+// wait, so neither the block stream nor the gathers stall on a per-CTA round
+// trip.  Same arithmetic in the same order as residual_kernel, so the same
+// results.  Every mbarrier wait is bounded: on time-out the kernel sets
 // *err = 3, waits (bounded) for its own copies in flight and returns.
-// A group of EPB elements needs EPB * 4000 bytes of blocks and EPB * 800
-// bytes of smoother matrices per stage.
-template <int EPB>
+template <typename MT, int EPB, bool WITH_W>
 struct TmaGroup {
-  static constexpr int ABytes = EPB * 5 * 400 * 2;
-  static constexpr int WBytes = EPB * 400 * 2;
+  static constexpr int BlockBytes = Chunk20<MT>::BlockBytes;
+  static constexpr int ABytes = EPB * 5 * BlockBytes;
+  static constexpr int WBytes = WITH_W ? EPB * BlockBytes : 0;
   static constexpr int StageBytes = ABytes + WBytes;
 };
 constexpr uint32_t kTmaSpinLimit = 1u << 20;
@@ -272,21 +334,14 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
       : "memory");
 }
 
-__device__ __forceinline__ Row20 lds_row20(const unsigned char* blk, int m) {
-  Row20 q;
-  q.a = *reinterpret_cast<const uint4*>(blk + 16 * m);
-  q.b = *reinterpret_cast<const uint4*>(blk + 2 * kC20Off1 + 16 * m);
-  q.c = *reinterpret_cast<const uint2*>(blk + 2 * kC20Off2 + 8 * m);
-  return q;
-}
-
-template <int EPB, int S, int MINB>
-__global__ void __launch_bounds__(EPB * 20, MINB) residual_bf16_tma_kernel(
-    const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
-    const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
-    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err) {
+template <typename MT, int EPB, int S, int MINB, bool WITH_W>
+__global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
+    const MT* __restrict__ blk, const MT* __restrict__ W, const int* __restrict__ nbe, const float* __restrict__ x,
+    const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out, int64_t B, int flags,
+    const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err) {
   constexpr int N = 20, F = 4;
-  constexpr int kTmaABytes = TmaGroup<EPB>::ABytes, kTmaStageBytes = TmaGroup<EPB>::StageBytes;
+  using G = TmaGroup<MT, EPB, WITH_W>;
+  using C = Chunk20<MT>;
   extern __shared__ __align__(128) unsigned char tma_smem[];
   __shared__ __align__(8) uint64_t bar[S];
   __shared__ float xs[EPB][F + 1][N];
@@ -296,11 +351,11 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_bf16_tma_kernel(
   const int tid = threadIdx.x;
   const int le = tid / N, m = tid % N;
   const bool zerox = flags & RF_ZEROX;
-  const bool smooth = flags & RF_SMOOTH;
+  const bool smooth = WITH_W && (flags & RF_SMOOTH);
   const bool restrict_ = flags & RF_RESTRICT;
   const int64_t ngroups = (B + EPB - 1) / EPB;
   const int64_t stride = gridDim.x;
-  if (tid < N * F) Ps[tid / F][tid % F] = (float)P[tid];
+  for (int t = tid; t < N * F; t += EPB * N) Ps[t / F][t % F] = P ? (float)P[t] : 0.0f;
   if (tid == 0) {
     abort_flag = 0;
     for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
@@ -313,11 +368,12 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_bf16_tma_kernel(
     if (g >= ngroups) return;
     const int64_t e0 = g * EPB;
     const uint32_t ne = (uint32_t)((B - e0) < EPB ? (B - e0) : EPB);
-    const uint32_t ba = zerox ? 0u : ne * 4000u, bw = smooth ? ne * 800u : 0u;
-    unsigned char* st = tma_smem + (size_t)(k % S) * kTmaStageBytes;
+    const uint32_t ba = zerox ? 0u : ne * 5u * G::BlockBytes;
+    const uint32_t bw = smooth ? ne * (uint32_t)G::BlockBytes : 0u;
+    unsigned char* sp = tma_smem + (size_t)(k % S) * G::StageBytes;
     mbar_expect_tx(&bar[k % S], ba + bw);
-    if (ba) bulk_copy_g2s(st, blk + e0 * 2000, ba, &bar[k % S]);
-    if (bw) bulk_copy_g2s(st + kTmaABytes, W + e0 * 400, bw, &bar[k % S]);
+    if (ba) bulk_copy_g2s(sp, blk + e0 * 2000, ba, &bar[k % S]);
+    if (bw) bulk_copy_g2s(sp + G::ABytes, W + e0 * 400, bw, &bar[k % S]);
   };
   if (tid == 0)
     for (int k = 0; k < S; ++k) issue(k);
@@ -359,14 +415,14 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_bf16_tma_kernel(
     }
     __syncthreads();
     if (abort_flag) break;
-    const unsigned char* st = tma_smem + (size_t)s * kTmaStageBytes;
+    const unsigned char* sp = tma_smem + (size_t)s * G::StageBytes;
     float acc = 0.0f;
     if (valid && !zerox) {
-      const unsigned char* Ae = st + (size_t)le * 4000;
-      acc = dot_row20(lds_row20(Ae, m), xs[le][0], acc);
+      const unsigned char* Ae = sp + (size_t)le * 5 * G::BlockBytes;
+      acc = C::dot(C::lds(Ae, m), xs[le][0], acc);
 #pragma unroll
       for (int f = 0; f < F; ++f)
-        if (nbv[f] >= 0) acc = dot_row20(lds_row20(Ae + (1 + f) * 800, m), xs[le][1 + f], acc);
+        if (nbv[f] >= 0) acc = C::dot(C::lds(Ae + (1 + f) * G::BlockBytes, m), xs[le][1 + f], acc);
     }
     float res = 0.0f;
     if (valid) {
@@ -384,7 +440,7 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_bf16_tma_kernel(
       }
       if (smooth && valid)
         x_out[e * N + m] = (zerox ? 0.0f : xs[le][0][m]) +
-                           dot_row20(lds_row20(st + kTmaABytes + (size_t)le * 800, m), rs[le], 0.0f);
+                           C::dot(C::lds(sp + G::ABytes + (size_t)le * G::BlockBytes, m), rs[le], 0.0f);
     }
     __syncthreads();   // stage s and xs / rs free again
     if (tid == 0) {
@@ -398,6 +454,41 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_bf16_tma_kernel(
       if (blockIdx.x + j * stride >= ngroups) break;
       (void)mbar_wait_bounded(&bar[j % S], (uint32_t)((j / S) & 1));
     }
+  }
+}
+
+template <typename MT, int EPB, int S, int MINB, bool WITH_W>
+int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out,
+               int flags, float* r1, cudaStream_t st) {
+  const int64_t ngroups = (c->B + EPB - 1) / EPB;
+  const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
+  if (g)
+    residual_tma_kernel<MT, EPB, S, MINB, WITH_W><<<g, EPB * 20, S * TmaGroup<MT, EPB, WITH_W>::StageBytes, st>>>(
+        blk, W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, r1, c->d_err);
+  bump();
+  CKL(c);
+  return DG_OK;
+}
+
+template <typename MT, int EPB, int S, int MINB, bool WITH_W>
+int set_tma_smem(dg_ctx* c) {
+  CK(c, cudaFuncSetAttribute(residual_tma_kernel<MT, EPB, S, MINB, WITH_W>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             S * TmaGroup<MT, EPB, WITH_W>::StageBytes));
+  return DG_OK;
+}
+
+// BF16 preconditioner step (3D) through the bulk-copy kernel.  Launch shapes
+// (elements per group, stages, CTAs per SM); c2 sweep: (8,5,1) 49.3 us,
+// (8,3,1) 49.2, (8,2,2) 41.2, (4,2,4) 41.3, (4,2,5) 41.6, (4,1,8) 41.5,
+// (6,2,3) 40.7 -- several CTAs per SM hide the per-group round trip that
+// one CTA per SM cannot.
+int launch_bf16_tma(dg_ctx* c, Mixed& M, const float* x, const float* b, float* r, float* x_out, int flags,
+                    cudaStream_t st) {
+  switch (c->tma_variant) {
+    case 1: return launch_tma<__nv_bfloat16, 8, 2, 2, true>(c, M.blk16, M.W16, x, b, r, x_out, flags, M.r1, st);
+    case 2: return launch_tma<__nv_bfloat16, 4, 2, 4, true>(c, M.blk16, M.W16, x, b, r, x_out, flags, M.r1, st);
+    default: return launch_tma<__nv_bfloat16, 6, 2, 3, true>(c, M.blk16, M.W16, x, b, r, x_out, flags, M.r1, st);
   }
 }
 
@@ -471,6 +562,10 @@ int launch_residual32(dg_ctx* c, const float* x, const float* b, float* r, float
                       cudaStream_t st) {
   using E = Elem<D>;
   Mixed& M = mixed_of(c);
+  if (D == 3 && c->f32_tma) {   // chunked FP32 copy, bulk-copy kernel
+    if (flags & RF_SMOOTH) return launch_tma<float, 4, 2, 2, true>(c, M.blk, M.W, x, b, r, x_out, flags, M.r1, st);
+    return launch_tma<float, 4, 2, 3, false>(c, M.blk, M.W, x, b, r, x_out, flags, M.r1, st);
+  }
   unsigned g = nblk(c->B, E::EPB);
   if (g)
     residual_kernel<E::N, E::F, E::EPB, float, float, float><<<g, E::EPB * E::N, 0, st>>>(
@@ -500,41 +595,12 @@ int launch_residual16(dg_ctx* c, const float* x, const float* b, float* r, float
   return DG_OK;
 }
 
-template <int EPB, int S, int MINB>
-int launch_bf16_tma(dg_ctx* c, Mixed& M, const float* x, const float* b, float* r, float* x_out, int flags,
-                    cudaStream_t st) {
-  const int64_t ngroups = (c->B + EPB - 1) / EPB;
-  const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
-  if (g)
-    residual_bf16_tma_kernel<EPB, S, MINB><<<g, EPB * 20, S * TmaGroup<EPB>::StageBytes, st>>>(
-        M.blk16, M.W16, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, M.r1, c->d_err);
-  bump();
-  CKL(c);
-  return DG_OK;
-}
-
-template <int EPB, int S, int MINB>
-int set_tma_smem(dg_ctx* c) {
-  CK(c, cudaFuncSetAttribute(residual_bf16_tma_kernel<EPB, S, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             S * TmaGroup<EPB>::StageBytes));
-  return DG_OK;
-}
-
 // residual in the preconditioner: BF16 blocks when enabled, FP32 otherwise
 int residual_pc(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags, cudaStream_t st) {
   if (c->precond_bf16) {
     if (c->D == 3 && c->bf16_tma) {
       Mixed& M = mixed_of(c);
-      // launch shapes (elements per group, stages, CTAs per SM); c2 sweep:
-      // (8,5,1) 49.3 us, (8,3,1) 49.2, (8,2,2) 41.2, (4,2,4) 41.3,
-      // (4,2,5) 41.6, (4,1,8) 41.5, (6,2,3) 40.7 -- several CTAs per SM hide
-      // the per-group round trip that one CTA per SM cannot
-      switch (c->tma_variant) {
-        case 1: return launch_bf16_tma<8, 2, 2>(c, M, x, b, r, x_out, flags, st);
-        case 2: return launch_bf16_tma<4, 2, 4>(c, M, x, b, r, x_out, flags, st);
-        case 3: return launch_bf16_tma<8, 5, 1>(c, M, x, b, r, x_out, flags, st);
-        default: return launch_bf16_tma<6, 2, 3>(c, M, x, b, r, x_out, flags, st);
-      }
+      return launch_bf16_tma(c, M, x, b, r, x_out, flags, st);
     }
     if (c->D == 3) {
       Mixed& M = mixed_of(c);
@@ -721,8 +787,9 @@ __global__ void convert_f64_bf16_kernel(const double* __restrict__ a, __nv_bfloa
 int build_mixed(dg_ctx* c, cudaStream_t st) {
   Mixed& M = mixed_of(c);
   int rc;
-  if ((rc = set_tma_smem<6, 2, 3>(c)) || (rc = set_tma_smem<8, 2, 2>(c)) || (rc = set_tma_smem<4, 2, 4>(c)) ||
-      (rc = set_tma_smem<8, 5, 1>(c)))
+  if ((rc = set_tma_smem<__nv_bfloat16, 6, 2, 3, true>(c)) || (rc = set_tma_smem<__nv_bfloat16, 8, 2, 2, true>(c)) ||
+      (rc = set_tma_smem<__nv_bfloat16, 4, 2, 4, true>(c)) || (rc = set_tma_smem<float, 4, 2, 3, false>(c)) ||
+      (rc = set_tma_smem<float, 4, 2, 2, true>(c)))
     return rc;
   const size_t nb = (size_t)c->B * (c->F + 1) * c->N * c->N;
   const size_t nw = (size_t)c->B * c->N * c->N;
@@ -734,7 +801,11 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
     if ((rc = dalloc(c, &M.cg1, (size_t)c->ncg))) return rc;
     if ((rc = dalloc(c, &M.r1, (size_t)c->B * c->NC))) return rc;
   }
-  convert_f64_f32_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk, (int64_t)nb);
+  if (c->D == 3 && c->f32_tma)
+    convert_f64_f32_chunk20_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk,
+                                                                          (int64_t)c->B * (c->F + 1));
+  else
+    convert_f64_f32_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk, (int64_t)nb);
   bump();
   // smoother matrices of the mixed preconditioner
   const double* Wsrc = c->d_W;
@@ -749,7 +820,10 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
     bump();
     Wsrc = Winv;
   }
-  convert_f64_f32_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W, (int64_t)nw);
+  if (c->D == 3 && c->f32_tma)
+    convert_f64_f32_chunk20_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W, (int64_t)c->B);
+  else
+    convert_f64_f32_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W, (int64_t)nw);
   bump();
   if (c->precond_bf16) {
     if (!M.blk16) {

@@ -101,6 +101,8 @@ struct dg_ctx {
   bool precond_bf16 = true;
   // ... streamed by the persistent bulk-copy (TMA) kernel (3D)
   bool bf16_tma = true;
+  // FP32 operator copy (3D) in the chunked layout, read by the bulk-copy kernel
+  bool f32_tma = true;
   int tma_variant = 0;   // elements per group / stages / CTAs per SM of that kernel
   bool verbose = false;
   // mixed preconditioner smoother: 0 = the reference's three point-Jacobi
@@ -677,6 +679,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (pb && pb[0]) c->precond_bf16 = pb[0] != '0';
     const char* bt = std::getenv("DG_BF16_TMA");
     if (bt && bt[0]) c->bf16_tma = bt[0] != '0';
+    const char* ft = std::getenv("DG_F32_TMA");
+    if (ft && ft[0]) c->f32_tma = ft[0] != '0';
     const char* tv = std::getenv("DG_TMA_VARIANT");
     if (tv && tv[0]) c->tma_variant = std::atoi(tv);
     const char* mc = std::getenv("DG_MIXED_CGS");

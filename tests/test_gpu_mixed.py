@@ -103,19 +103,25 @@ def test_smooth_pc_matches_fp64_smoothing(smoother, bf16, tol):
 
 
 @pytest.mark.parametrize("n", [6, 7])
-def test_bulk_copy_kernel_matches_plain_loads(n, monkeypatch):
-    """The persistent bulk-copy (TMA) smoothing kernel and the plain-load
-    kernel run the same arithmetic in the same order: the preconditioner's
-    smoothing step and the whole FP32 preconditioner agree bit for bit
-    (7^3 * 6 = 2058 tets leaves a partial last group of elements)."""
+def test_bulk_copy_kernels_match_plain_loads(n, monkeypatch):
+    """The persistent bulk-copy (TMA) kernels and the plain-load kernels run
+    the same arithmetic in the same order: the preconditioner's smoothing
+    step (BF16 and FP32 block copies), the whole FP32 preconditioner and the
+    FP32 apply agree bit for bit (7^3 * 6 = 2058 tets leaves partial last
+    groups of elements)."""
     outs = {}
     for tma in ("1", "0"):
         monkeypatch.setenv("DG_BF16_TMA", tma)
+        monkeypatch.setenv("DG_F32_TMA", tma)
         m, s, f, u = _setup("tet", n, 2)
         g = torch.Generator(device="cuda:0").manual_seed(8)
         x = torch.randn(s.nonods, dtype=torch.float32, device="cuda:0", generator=g)
         b = torch.randn(s.nonods, dtype=torch.float32, device="cuda:0", generator=g)
-        outs[tma] = (s.smooth_pc(x, b), s.precond_f32(b))
+        res = [s.smooth_pc(x, b), s.precond_f32(b), s.apply_f32(x)]
+        s.set_mixed_options(precond_bf16=False)
+        s.build_operator()
+        res += [s.smooth_pc(x, b), s.precond_f32(b)]
         torch.cuda.synchronize()
-    assert torch.equal(outs["1"][0], outs["0"][0])
-    assert torch.equal(outs["1"][1], outs["0"][1])
+        outs[tma] = res
+    for a, c in zip(outs["1"], outs["0"]):
+        assert torch.equal(a, c)
