@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(N* N) block_inverse_kernel(const double* __res
 //   res = b - A x            (b = 0 when null; x = 0 when ZEROX)
 //   r  <- sgn * res          (when r != null)
 //   SMOOTH: x_out = x + W_e res  (the three-sweep block-Jacobi step)
-enum { RF_ZEROX = 1, RF_SMOOTH = 2, RF_NEG = 4, RF_RESTRICT = 8 };
+enum { RF_ZEROX = 1, RF_SMOOTH = 2, RF_NEG = 4, RF_RESTRICT = 8, RF_STREAM_HINT = 16 };
 
 // MT: stored matrix type; VT: vector type; AT: accumulation type.
 template <int N, int F, int EPB, typename MT = double, typename VT = double, typename AT = double>

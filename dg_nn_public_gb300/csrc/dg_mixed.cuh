@@ -334,6 +334,23 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
       : "memory");
 }
 
+// L2 policy "evict first" for data read once per pass (the block stream), so
+// that it does not push the vectors and the SFC level matrices out of L2
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+__device__ __forceinline__ void bulk_copy_g2s_hint(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                                   uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
+      : "memory");
+}
+
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
 __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     const MT* __restrict__ blk, const MT* __restrict__ W, const int* __restrict__ nbe, const float* __restrict__ x,
@@ -362,6 +379,8 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  const uint64_t pol = l2_evict_first_policy();
+  const bool hint = flags & RF_STREAM_HINT;
   // copies of the CTA's k-th group go to stage k % S, phase parity (k / S) & 1
   auto issue = [&](int64_t k) {
     const int64_t g = blockIdx.x + k * stride;
@@ -372,8 +391,13 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     const uint32_t bw = smooth ? ne * (uint32_t)G::BlockBytes : 0u;
     unsigned char* sp = tma_smem + (size_t)(k % S) * G::StageBytes;
     mbar_expect_tx(&bar[k % S], ba + bw);
-    if (ba) bulk_copy_g2s(sp, blk + e0 * 2000, ba, &bar[k % S]);
-    if (bw) bulk_copy_g2s(sp + G::ABytes, W + e0 * 400, bw, &bar[k % S]);
+    if (hint) {
+      if (ba) bulk_copy_g2s_hint(sp, blk + e0 * 2000, ba, &bar[k % S], pol);
+      if (bw) bulk_copy_g2s_hint(sp + G::ABytes, W + e0 * 400, bw, &bar[k % S], pol);
+    } else {
+      if (ba) bulk_copy_g2s(sp, blk + e0 * 2000, ba, &bar[k % S]);
+      if (bw) bulk_copy_g2s(sp + G::ABytes, W + e0 * 400, bw, &bar[k % S]);
+    }
   };
   if (tid == 0)
     for (int k = 0; k < S; ++k) issue(k);
@@ -460,6 +484,7 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
 int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out,
                int flags, float* r1, cudaStream_t st) {
+  if (c->l2_hint) flags |= RF_STREAM_HINT;
   const int64_t ngroups = (c->B + EPB - 1) / EPB;
   const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
   if (g)
