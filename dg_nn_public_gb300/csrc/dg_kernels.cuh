@@ -368,6 +368,16 @@ __global__ void __launch_bounds__(N* N) block_inverse_kernel(const double* __res
 //   SMOOTH: x_out = x + W_e res  (the three-sweep block-Jacobi step)
 enum { RF_ZEROX = 1, RF_SMOOTH = 2, RF_NEG = 4, RF_RESTRICT = 8, RF_STREAM_HINT = 16 };
 
+// Programmatic dependent launch: wait until the preceding kernel of the
+// stream has completed (its writes visible), then let the next kernel start
+// its launch.  Triggering only after the wait means a kernel's pre-wait
+// part can read anything produced two or more kernels back.  Both are
+// no-ops for a kernel launched without the programmatic attribute.
+__device__ __forceinline__ void pdl_wait_then_trigger() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // MT: stored matrix type; VT: vector type; AT: accumulation type.
 template <int N, int F, int EPB, typename MT = double, typename VT = double, typename AT = double>
 __global__ void __launch_bounds__(EPB* N) residual_kernel(const MT* __restrict__ blk,

@@ -149,6 +149,7 @@ template <typename T>
 __global__ void gather_cg_kernel(const T* __restrict__ r1, const int* __restrict__ gptr,
                                  const int* __restrict__ gent, const double* __restrict__ wdg,
                                  const int* __restrict__ pos, T* __restrict__ out, int ncg) {
+  pdl_wait_then_trigger();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ncg) return;
   T acc = 0;
@@ -166,6 +167,7 @@ __global__ void prolong_cg_kernel(T* __restrict__ x, const T* __restrict__ ecg,
                                   const int* __restrict__ pos, const int* __restrict__ p1cg,
                                   const double* __restrict__ wdg, const double* __restrict__ P,
                                   const int* __restrict__ whichc, int color, int64_t B, int add) {
+  pdl_wait_then_trigger();
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= B * N) return;
   const int64_t e = t / N;
@@ -195,7 +197,8 @@ __global__ void rar_scatter_kernel(double* __restrict__ value, const double* __r
 // ---------------------------------------------------------------------------
 // SFC levels (multigrid_linearelastic.py:25-172)
 
-// rr = b - A e_in;  e_out = e_in + w * rr / diag   (mg_smooth_one_level).
+// rr = b - A e_in;  e_out = e_in + w * rr / diag   (mg_smooth_one_level);
+// e_in = NULL stands for a zero initial guess.
 // LPR lanes share a row (strided over its entries, shuffle-reduced) so the
 // dependent loads of a row are spread over lanes instead of chained.
 constexpr int LPR = 8;
@@ -205,16 +208,17 @@ __global__ void lev_jacobi_kernel(const int* __restrict__ rowptr, const int* __r
                                   const T* __restrict__ e_in, const T* __restrict__ b,
                                   T* __restrict__ e_out, T* __restrict__ rr_out, int n,
                                   double w) {
+  pdl_wait_then_trigger();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / LPR, lane = t % LPR;
   T s = 0;
-  if (i < n)
+  if (i < n && e_in)
     for (int k = rowptr[i] + lane; k < rowptr[i + 1]; k += LPR) s += val[k] * e_in[col[k]];
 #pragma unroll
   for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
   if (i >= n || lane != 0) return;
   const T rr = b[i] - s;
-  e_out[i] = e_in[i] + rr / diag[i] * (T)w;
+  e_out[i] = (e_in ? e_in[i] : (T)0) + rr / diag[i] * (T)w;
   if (rr_out) rr_out[i] = rr;
 }
 
@@ -223,6 +227,7 @@ template <typename T = double>
 __global__ void lev_restrict_kernel(const T* __restrict__ rr, const T* __restrict__ e,
                                     T* __restrict__ r_next, T* __restrict__ e_next,
                                     int n, int nn) {
+  pdl_wait_then_trigger();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nn) return;
   const int a = 2 * i, b = 2 * i + 1;
@@ -234,6 +239,7 @@ __global__ void lev_restrict_kernel(const T* __restrict__ rr, const T* __restric
 template <typename T = double>
 __global__ void lev_prolong_kernel(T* __restrict__ e, const T* __restrict__ e_next,
                                    const int* __restrict__ up, int n) {
+  pdl_wait_then_trigger();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) e[i] += e_next[up[i]];
 }
@@ -320,6 +326,7 @@ __global__ void __launch_bounds__(TB) axpy_multi_kernel(const VT* __restrict__ V
 // sqrt.  One block per vector i (gridDim.x = nv), a fixed-order tree sum.
 __global__ void reduce_partial_kernel(const double* __restrict__ partial, int nblk, int nv,
                                       double* __restrict__ out, int accumulate, int take_sqrt) {
+  pdl_wait_then_trigger();
   __shared__ double red[32];
   const int i = blockIdx.x;
   if (i >= nv) return;

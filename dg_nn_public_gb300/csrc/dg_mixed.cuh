@@ -53,6 +53,10 @@ struct Mixed {
   float* dense_inv = nullptr;
   int g_m = 0, g_chunk = 0;
   const float* g_vptr = nullptr;
+  // Gram-Schmidt partial sums: one float4 of the vectors per thread,
+  // nblk4 = ceil(nonods / 4 / 256) blocks, KMAXV sums per block
+  double* part = nullptr;
+  int nblk4 = 0;
 };
 
 __global__ void f64_to_f32_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t n, double scale) {
@@ -60,9 +64,52 @@ __global__ void f64_to_f32_kernel(const double* __restrict__ a, float* __restric
   if (k < n) b[k] = (float)(a[k] * scale);
 }
 
+// Launch on st, as a programmatic dependent launch when c->use_pdl (the
+// kernel's launch overlaps the tail of the preceding kernel; its
+// pdl_wait_then_trigger() keeps the data order).  Used for the chain of
+// kernels of one inner Arnoldi step.
+template <typename... KArgs, typename... Args>
+int launch_k(dg_ctx* c, void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+             Args... args) {
+  if (grid == 0) return DG_OK;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = c->use_pdl ? 1 : 0;
+  CK(c, cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+  bump();
+  return DG_OK;
+}
+
+template <typename... KArgs, typename... Args>
+int launch_k2(dg_ctx* c, void (*kern)(KArgs...), dim3 grid, unsigned block, size_t smem, cudaStream_t st,
+              Args... args) {
+  if (grid.x == 0 || grid.y == 0) return DG_OK;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = c->use_pdl ? 1 : 0;
+  CK(c, cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...));
+  bump();
+  return DG_OK;
+}
+
 // e = Ainv r for a small dense level matrix: one warp per row
 __global__ void dense_matvec_kernel(const float* __restrict__ Ainv, const float* __restrict__ r,
                                     float* __restrict__ e, int n) {
+  pdl_wait_then_trigger();
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
@@ -407,6 +454,9 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     return (g < ngroups && e < B) ? reinterpret_cast<const int4*>(nbe)[e] : make_int4(-1, -1, -1, -1);
   };
   int4 nb_cur = load_nb(blockIdx.x);
+  // blocks, smoother matrices and neighbour table are fixed during a solve:
+  // the copies above may run ahead of the preceding kernel; x and b may not
+  pdl_wait_then_trigger();
   float x_own = 0.0f, x_nb[F] = {0.0f, 0.0f, 0.0f, 0.0f}, b_cur = 0.0f;
   auto load_x = [&](int64_t g, const int4& nb) {
     const int64_t e = g * EPB + le;
@@ -487,12 +537,9 @@ int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const floa
   if (c->l2_hint) flags |= RF_STREAM_HINT;
   const int64_t ngroups = (c->B + EPB - 1) / EPB;
   const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
-  if (g)
-    residual_tma_kernel<MT, EPB, S, MINB, WITH_W><<<g, EPB * 20, S * TmaGroup<MT, EPB, WITH_W>::StageBytes, st>>>(
-        blk, W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, r1, c->d_err);
-  bump();
-  CKL(c);
-  return DG_OK;
+  return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W>, g, EPB * 20,
+                  (size_t)S * TmaGroup<MT, EPB, WITH_W>::StageBytes, st, blk, W, (const int*)c->d_nbe, x, b, r,
+                  x_out, (int64_t)c->B, flags, (const double*)c->T.P, r1, (int*)c->d_err);
 }
 
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
@@ -651,9 +698,10 @@ int launch_transfer32(dg_ctx* c, const float* r, float* cg_out, float* x_add, co
         r, c->T.P, c->d_gptr, c->d_gent, c->d_wdg, c->d_pos, cg_out, (int)c->ncg);
     bump();
   } else {
-    prolong_cg_kernel<E::N, E::NC, float><<<nblk(c->B * E::N, 256), 256, 0, st>>>(
-        x_add, e_sfc, c->d_pos, c->d_p1cg, c->d_wdg, c->T.P, nullptr, 0, c->B, 1);
-    bump();
+    int rc = launch_k(c, prolong_cg_kernel<E::N, E::NC, float>, nblk(c->B * E::N, 256), 256, 0, st, x_add, e_sfc,
+                      (const int*)c->d_pos, (const int*)c->d_p1cg, (const double*)c->d_wdg, (const double*)c->T.P,
+                      (const int*)nullptr, 0, (int64_t)c->B, 1);
+    if (rc) return rc;
   }
   CKL(c);
   return DG_OK;
@@ -674,42 +722,51 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
   const double w = c->cfg.jac_wei;
   const int TB = 128;
   if (M.dense_l >= 0) {
+    // kernels only (no copy / memset nodes), so that the whole chain can be
+    // linked by programmatic dependent launches: the residual arrives in
+    // lev[0].r (gathered there directly when r_sfc is lev[0].r) and level 0
+    // starts from a zero guess (e_in = NULL in its first sweep)
     const int lc = M.dense_l;
-    if (lc == 0) {
+    int rc;
+    if (r_sfc != M.lev[0].r)
       CK(c, cudaMemcpyAsync(M.lev[0].r, r_sfc, sizeof(float) * M.lev[0].n, cudaMemcpyDeviceToDevice, st));
-    } else {
-      CK(c, cudaMemcpyAsync(M.lev[0].r, r_sfc, sizeof(float) * M.lev[0].n, cudaMemcpyDeviceToDevice, st));
-      CK(c, cudaMemsetAsync(M.lev[0].e, 0, sizeof(float) * M.lev[0].n, st));
-    }
     for (int l = 0; l < lc; ++l) {
       Lev32& L = M.lev[l];
+      const unsigned gj = nblk((int64_t)L.n * LPR, TB);
       for (int it = 0; it < c->cfg.pre_smooth_its; ++it) {
-        lev_jacobi_kernel<float><<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag,
-                                                                             L.e, L.r, L.e2, nullptr, L.n, w);
-        bump();
+        const float* ein = (l == 0 && it == 0) ? nullptr : L.e;
+        if ((rc = launch_k(c, lev_jacobi_kernel<float>, gj, TB, 0, st, (const int*)L.rowptr, (const int*)L.col,
+                           (const float*)L.val, (const float*)L.diag, ein, (const float*)L.r, L.e2,
+                           (float*)nullptr, L.n, w)))
+          return rc;
         std::swap(L.e, L.e2);
       }
-      lev_jacobi_kernel<float><<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag, L.e,
-                                                                           L.r, L.e2, L.rr, L.n, w);
-      bump();
+      const float* ein = (l == 0 && c->cfg.pre_smooth_its == 0) ? nullptr : L.e;
+      if ((rc = launch_k(c, lev_jacobi_kernel<float>, gj, TB, 0, st, (const int*)L.rowptr, (const int*)L.col,
+                         (const float*)L.val, (const float*)L.diag, ein, (const float*)L.r, L.e2, L.rr, L.n, w)))
+        return rc;
       std::swap(L.e, L.e2);
       Lev32& Nx = M.lev[l + 1];
-      lev_restrict_kernel<float><<<nblk(Nx.n, TB), TB, 0, st>>>(L.rr, L.e, Nx.r, Nx.e, L.n, Nx.n);
-      bump();
+      if ((rc = launch_k(c, lev_restrict_kernel<float>, nblk(Nx.n, TB), TB, 0, st, (const float*)L.rr,
+                         (const float*)L.e, Nx.r, Nx.e, L.n, Nx.n)))
+        return rc;
     }
     {
       Lev32& L = M.lev[lc];
-      dense_matvec_kernel<<<nblk(L.n, 8), 256, 0, st>>>(M.dense_inv, L.r, L.e, L.n);
-      bump();
+      if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, 0, st, (const float*)M.dense_inv,
+                         (const float*)L.r, L.e, L.n)))
+        return rc;
     }
     for (int l = lc - 1; l >= 0; --l) {
       Lev32& L = M.lev[l];
-      lev_prolong_kernel<float><<<nblk(L.n, TB), TB, 0, st>>>(L.e, M.lev[l + 1].e, L.up, L.n);
-      bump();
+      if ((rc = launch_k(c, lev_prolong_kernel<float>, nblk(L.n, TB), TB, 0, st, L.e, (const float*)M.lev[l + 1].e,
+                         (const int*)L.up, L.n)))
+        return rc;
       for (int it = 0; it < c->cfg.post_smooth_its; ++it) {
-        lev_jacobi_kernel<float><<<nblk((int64_t)L.n * LPR, TB), TB, 0, st>>>(L.rowptr, L.col, L.val, L.diag,
-                                                                             L.e, L.r, L.e2, nullptr, L.n, w);
-        bump();
+        if ((rc = launch_k(c, lev_jacobi_kernel<float>, nblk((int64_t)L.n * LPR, TB), TB, 0, st,
+                           (const int*)L.rowptr, (const int*)L.col, (const float*)L.val, (const float*)L.diag,
+                           (const float*)L.e, (const float*)L.r, L.e2, (float*)nullptr, L.n, w)))
+          return rc;
         std::swap(L.e, L.e2);
       }
     }
@@ -786,8 +843,12 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
     CK(c, cudaMemsetAsync(cur, 0, sizeof(float) * c->nonods, st));
   }
   if ((rc = residual_pc(c, cur, r, nullptr, nullptr, RF_RESTRICT, st))) return rc;   // -> M.r1
-  if ((rc = gather_cg<float>(c, M.r1, M.cg1, true, st))) return rc;
-  if ((rc = vcycle32(c, M.cg1, st))) return rc;
+  float* cg_dst = M.dense_l > 0 ? M.lev[0].r : M.cg1;
+  if ((rc = launch_k(c, gather_cg_kernel<float>, nblk(c->ncg, 128), 128, 0, st, (const float*)M.r1,
+                     (const int*)c->d_gptr, (const int*)c->d_gent, (const double*)c->d_wdg, (const int*)c->d_pos,
+                     cg_dst, (int)c->ncg)))
+    return rc;
+  if ((rc = vcycle32(c, cg_dst, st))) return rc;
   if ((rc = transfer32(c, nullptr, nullptr, cur, M.lev[0].e, st))) return rc;
   for (int it = 0; it < nsm; ++it) {
     float* out = (it == nsm - 1) ? z : other;
@@ -937,6 +998,10 @@ int ensure_krylov32(dg_ctx* c, int m) {
   if ((rc = dalloc(c, &M.V, (size_t)(m + 1) * c->nonods))) return rc;
   if ((rc = dalloc(c, &M.Z, (size_t)m * c->nonods))) return rc;
   if ((rc = dalloc(c, &M.H, (size_t)(m + 1) * m))) return rc;
+  if (!M.part) {
+    M.nblk4 = (int)((c->nonods / 4 + RED_TB - 1) / RED_TB);
+    if ((rc = dalloc(c, &M.part, (size_t)std::max(M.nblk4, 1) * KMAXV))) return rc;
+  }
   M.vcap = m + 1;
   return DG_OK;
 }
@@ -949,13 +1014,25 @@ int norm32(dg_ctx* c, const float* z, double* out, cudaStream_t st) { return nor
 // float4 of up to 8 basis vectors in flight per step; per-thread sums are
 // FP32, the block and grid sums FP64, in a fixed order (deterministic).
 
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // partial[bx * KMAXV + i0 + q] = sum over this block's slice of V[i0+q] . z,
-// i0 = 8 * blockIdx.y
+// i0 = 8 * blockIdx.y.  The grid covers the vectors once (one float4 per
+// thread when gridDim.x * TB >= n4), so all nine loads of a thread are in
+// flight together; per-thread and in-warp sums are FP32 (a warp sums at most
+// a few hundred products), the warps of a block and the blocks are combined
+// in FP64.  GB300's FP64 pipe is narrow: FP64 shuffle trees per thread cost
+// more than the memory traffic here.
 template <int TB>
 __global__ void __launch_bounds__(TB) mdot8_f32_kernel(const float* __restrict__ V, int64_t ld, int nv,
                                                        const float* __restrict__ z, int64_t n4,
                                                        double* __restrict__ partial) {
-  __shared__ double red[TB / 32][8];
+  pdl_wait_then_trigger();
+  __shared__ float red[TB / 32][8];
   const int i0 = blockIdx.y * 8;
   const int cnt = min(8, nv - i0);
   float acc[8];
@@ -979,25 +1056,27 @@ __global__ void __launch_bounds__(TB) mdot8_f32_kernel(const float* __restrict__
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
-    const double a = warp_sum((double)acc[q]);
+    const float a = warp_sum_f(acc[q]);
     if (lane == 0) red[wid][q] = a;
   }
   __syncthreads();
   if (threadIdx.x < cnt) {
     double s = 0.0;
-    for (int w = 0; w < TB / 32; ++w) s += red[w][threadIdx.x];
+    for (int w = 0; w < TB / 32; ++w) s += (double)red[w][threadIdx.x];
     partial[(int64_t)blockIdx.x * KMAXV + i0 + threadIdx.x] = s;
   }
 }
 
 // z -= sum_i V[i] h[i] (nv <= 256); with want_norm also
-// partial[bx * KMAXV] = this block's slice of |z_new|^2
+// partial[bx * KMAXV] = this block's slice of |z_new|^2 (FP32 within a warp,
+// FP64 across warps)
 template <int TB>
 __global__ void __launch_bounds__(TB) axpy8_f32_kernel(const float* __restrict__ V, int64_t ld, int nv,
                                                        const double* __restrict__ h, float* __restrict__ z,
                                                        int64_t n4, double* __restrict__ partial, int want_norm) {
+  pdl_wait_then_trigger();
   __shared__ float hs[256];
-  __shared__ double red[TB / 32];
+  __shared__ float red[TB / 32];
   for (int i = threadIdx.x; i < nv; i += TB) hs[i] = (float)h[i];
   __syncthreads();
   float acc = 0.0f;
@@ -1028,13 +1107,13 @@ __global__ void __launch_bounds__(TB) axpy8_f32_kernel(const float* __restrict__
     }
   }
   if (!want_norm) return;
-  const double a = warp_sum((double)acc);
+  const float a = warp_sum_f(acc);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) red[wid] = a;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;
-    for (int w = 0; w < TB / 32; ++w) s += red[w];
+    for (int w = 0; w < TB / 32; ++w) s += (double)red[w];
     partial[(int64_t)blockIdx.x * KMAXV] = s;
   }
 }
@@ -1045,6 +1124,7 @@ __global__ void __launch_bounds__(TB) axpy8_f32_kernel(const float* __restrict__
 __global__ void cgs_finish_kernel(const double* __restrict__ partial, int nblk, const double* __restrict__ h1,
                                   const double* __restrict__ h2, int nv, double* __restrict__ Hc,
                                   float* __restrict__ inv) {
+  pdl_wait_then_trigger();
   __shared__ double red[32];
   for (int i = threadIdx.x; i < nv; i += blockDim.x) Hc[i] = h2 ? h1[i] + h2[i] : h1[i];
   double s = 0.0;
@@ -1065,6 +1145,7 @@ __global__ void cgs_finish_kernel(const double* __restrict__ partial, int nblk, 
 // v = z * (*inv), float4
 __global__ void scale4_f32_kernel(const float* __restrict__ z, const float* __restrict__ inv, float* __restrict__ v,
                                   int64_t n4) {
+  pdl_wait_then_trigger();
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n4) return;
   const float s = *inv;
@@ -1081,11 +1162,14 @@ int mdot4_f32(dg_ctx* c, const float* V, int nv, const float* z, double* h, cuda
   const int64_t n4 = c->nonods / 4;
   for (int off = 0; off < nv; off += KMAXV) {
     const int cnt = std::min(KMAXV, nv - off);
-    dim3 grid(c->nred, (cnt + 7) / 8);
-    mdot8_f32_kernel<RED_TB><<<grid, RED_TB, 0, st>>>(V + (size_t)off * c->nonods, c->nonods, cnt, z, n4, c->d_part);
-    bump();
-    reduce_partial_kernel<<<cnt, 128, 0, st>>>(c->d_part, c->nred, cnt, h + off, 0, 0);
-    bump();
+    int rc;
+    Mixed& M = mixed_of(c);
+    if ((rc = launch_k2(c, mdot8_f32_kernel<RED_TB>, dim3(M.nblk4, (cnt + 7) / 8), RED_TB, 0, st,
+                        (const float*)(V + (size_t)off * c->nonods), (int64_t)c->nonods, cnt, z, n4, M.part)))
+      return rc;
+    if ((rc = launch_k(c, reduce_partial_kernel, cnt, 256, 0, st, (const double*)M.part, M.nblk4, cnt, h + off, 0,
+                       0)))
+      return rc;
   }
   return DG_OK;
 }
@@ -1103,17 +1187,21 @@ int cgs2_32(dg_ctx* c, int j, float* w, int m, cudaStream_t st) {
   float* inv = reinterpret_cast<float*>(c->d_scal + 1);
   int rc;
   if ((rc = mdot4_f32(c, M.V, nv, w, c->d_h1, st))) return rc;
-  axpy8_f32_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(M.V, c->nonods, nv, c->d_h1, w, n4, c->d_part, two ? 0 : 1);
-  bump();
+  if ((rc = launch_k(c, axpy8_f32_kernel<RED_TB>, M.nblk4, RED_TB, 0, st, (const float*)M.V, (int64_t)c->nonods, nv,
+                     (const double*)c->d_h1, w, n4, M.part, two ? 0 : 1)))
+    return rc;
   if (two) {
     if ((rc = mdot4_f32(c, M.V, nv, w, c->d_h2, st))) return rc;
-    axpy8_f32_kernel<RED_TB><<<c->nred, RED_TB, 0, st>>>(M.V, c->nonods, nv, c->d_h2, w, n4, c->d_part, 1);
-    bump();
+    if ((rc = launch_k(c, axpy8_f32_kernel<RED_TB>, M.nblk4, RED_TB, 0, st, (const float*)M.V, (int64_t)c->nonods,
+                       nv, (const double*)c->d_h2, w, n4, M.part, 1)))
+      return rc;
   }
-  cgs_finish_kernel<<<1, 256, 0, st>>>(c->d_part, c->nred, c->d_h1, two ? c->d_h2 : nullptr, nv, Hc, inv);
-  bump();
-  scale4_f32_kernel<<<nblk(n4, 256), 256, 0, st>>>(w, inv, M.V + (size_t)nv * c->nonods, n4);
-  bump();
+  if ((rc = launch_k(c, cgs_finish_kernel, 1, 256, 0, st, (const double*)M.part, M.nblk4, (const double*)c->d_h1,
+                     two ? (const double*)c->d_h2 : (const double*)nullptr, nv, Hc, inv)))
+    return rc;
+  if ((rc = launch_k(c, scale4_f32_kernel, nblk(n4, 256), 256, 0, st, (const float*)w, (const float*)inv,
+                     M.V + (size_t)nv * c->nonods, n4)))
+    return rc;
   CKL(c);
   return DG_OK;
 }

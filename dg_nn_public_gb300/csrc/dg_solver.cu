@@ -105,6 +105,8 @@ struct dg_ctx {
   bool f32_tma = true;
   // bulk-copy block streams read with an L2 evict-first policy
   bool l2_hint = true;
+  // link the kernels of an inner Arnoldi step by programmatic dependent launch
+  bool use_pdl = true;
   int tma_variant = 0;   // elements per group / stages / CTAs per SM of that kernel
   bool verbose = false;
   // mixed preconditioner smoother: 0 = the reference's three point-Jacobi
@@ -683,6 +685,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (bt && bt[0]) c->bf16_tma = bt[0] != '0';
     const char* ft = std::getenv("DG_F32_TMA");
     if (ft && ft[0]) c->f32_tma = ft[0] != '0';
+    const char* pd = std::getenv("DG_PDL");
+    if (pd && pd[0]) c->use_pdl = pd[0] != '0';
     const char* lh = std::getenv("DG_L2_HINT");
     if (lh && lh[0]) c->l2_hint = lh[0] != '0';
     const char* tv = std::getenv("DG_TMA_VARIANT");
