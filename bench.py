@@ -382,6 +382,9 @@ def run_ours(args):
     F = m.ndim + 1                                   # faces per simplex
 
     def time_launch(fn, reps=20):
+        # back-to-back launches of one kernel would overlap each other's
+        # prologue under programmatic dependent launch; time them plain
+        s.set_launch_options(use_graph=True, use_pdl=False)
         for _ in range(3):
             fn()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -391,6 +394,7 @@ def run_ours(args):
             fn()
         e1.record(stream)
         torch.cuda.synchronize()
+        s.set_launch_options(use_graph=True, use_pdl=True)
         return e0.elapsed_time(e1) / reps / 1e3
 
     peaks, kind = load_peaks()

@@ -1481,3 +1481,24 @@ extern "C" int dg_set_mixed_options(dg_ctx* c, int32_t smoother, double smooth_w
   M.g_m = 0;
   return DG_OK;
 }
+
+// Launch options: use_graph != 0 replays the Arnoldi cycles / chunks as CUDA
+// graphs, use_pdl != 0 links the kernels of a mixed inner step by
+// programmatic dependent launch.  Cached graphs are dropped and captured
+// again with the new options at the next solve.
+extern "C" int dg_set_launch_options(dg_ctx* c, int32_t use_graph, int32_t use_pdl) {
+  if (!c) return set_thread_error(DG_ERR_ARG, "dg_set_launch_options: null context");
+  CK(c, cudaSetDevice(c->dev));
+  c->use_graph = use_graph != 0;
+  c->use_pdl = use_pdl != 0;
+  if (c->arnoldi_exec) {
+    cudaGraphExecDestroy(c->arnoldi_exec);
+    c->arnoldi_exec = nullptr;
+  }
+  Mixed& M = mixed_of(c);
+  for (auto& g : M.graphs)
+    if (g) cudaGraphExecDestroy(g);
+  M.graphs.clear();
+  M.g_m = 0;
+  return DG_OK;
+}

@@ -293,6 +293,11 @@ class DGSolver:
         self.mixed_options = dict(smoother=smoother, smooth_w=float(smooth_w), precond_bf16=bool(precond_bf16),
                                   dense_max=int(dense_max))
 
+    def set_launch_options(self, use_graph=True, use_pdl=True):
+        """CUDA-graph replay of Arnoldi cycles and programmatic dependent
+        launches inside a mixed inner step (both on by default)."""
+        self._chk(self._lib.dg_set_launch_options(self._ctx, 1 if use_graph else 0, 1 if use_pdl else 0))
+
     # library defaults of the mixed preconditioner (dg_create)
     mixed_options = dict(smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=1200)
 

@@ -178,6 +178,13 @@ int dg_smooth_pc(dg_ctx* ctx, const float* x, const float* b, float* x_out, void
 int dg_set_mixed_options(dg_ctx* ctx, int32_t smoother, double smooth_w, int32_t precond_bf16,
                          int32_t dense_max);
 
+/* Launch options (no counterpart in the reference): use_graph != 0 replays
+ * GMRES Arnoldi cycles and mixed inner chunks as CUDA graphs (default on);
+ * use_pdl != 0 links the kernels of a mixed inner Arnoldi step by
+ * programmatic dependent launch (default on).  Cached graphs are captured
+ * again at the next solve. */
+int dg_set_launch_options(dg_ctx* ctx, int32_t use_graph, int32_t use_pdl);
+
 /* Allocation-free residual norm (no counterpart in the reference):
  * r = b - A x and *norm_out = ||r||_2, both written on the device (r may be
  * NULL for the norm alone; b NULL means b = 0).  It allocates nothing: its
