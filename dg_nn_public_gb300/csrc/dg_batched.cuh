@@ -1,0 +1,1088 @@
+// Batched mixed-precision solve: up to kNR right-hand sides on one operator
+// (P3 tetrahedra), in lockstep.  Included into dg_solver.cu after
+// dg_mixed.cuh; it reuses the mixed-precision operator copies (chunked FP32
+// and BF16 blocks, BF16 smoother matrices, FP32 SFC levels, dense coarse
+// inverse) and adds batched kernels on RHS-interleaved vectors:
+//
+//   X[(e * 20 + n) * kNR + r]      (element-major, then node, then RHS)
+//
+// so that one node of an element is a contiguous run of kNR values and every
+// kernel reads the stored blocks once for all right-hand sides.
+//
+//   outer (FP64, per RHS):  r_k = b_k - A x_k with the FP64 blocks; stop the
+//                           RHS when ||r_k|| <= tol_k
+//   inner (FP32, batched):  right-preconditioned flexible GMRES(m) on
+//                           A d_k = r_k / ||r_k|| for all active k together,
+//                           one Hessenberg matrix per RHS (host, FP64);
+//                           classical Gram-Schmidt per RHS
+//   x_k += ||r_k|| d_k
+#pragma once
+
+namespace {
+
+constexpr int kNR = 64;   // right-hand sides per batch (lanes of the batched kernels)
+
+// ---------------------------------------------------------------------------
+// r = b - A x (FP32 sums) for kNR right-hand sides, one CTA per element
+// (128 threads): warp w owns rows 5w .. 5w+4, lane l owns RHS 2l, 2l+1.
+// The element's five blocks (chunked row layout, FP32 or BF16), its
+// smoother matrix (with RF_SMOOTH) and the gathered x of the element and its
+// four face neighbours (5 x 20 x kNR FP32) are staged in shared memory;
+// four columns of a block row are one 16-byte (FP32) or 8-byte (BF16) word.
+// Flags as residual_kernel: RF_ZEROX (x = 0), RF_NEG (r = A x - b),
+// RF_RESTRICT (r1 = P^T res per corner), RF_SMOOTH (x_out = x + W res).
+template <typename MT>
+struct BRow4;
+
+template <>
+struct BRow4<float> {
+  // columns n .. n+3 (n a multiple of 4) of row m of a chunked FP32 block
+  static __device__ __forceinline__ float4 get(const float* blk, int m, int n) {
+    return *reinterpret_cast<const float4*>(blk + (n >> 2) * 80 + m * 4);
+  }
+};
+
+template <>
+struct BRow4<__nv_bfloat16> {
+  static __device__ __forceinline__ float4 get(const __nv_bfloat16* blk, int m, int n) {
+    const int off = n < 8 ? m * 8 + n : (n < 16 ? kC20Off1 + m * 8 + (n - 8) : kC20Off2 + m * 4);
+    const uint2 w = *reinterpret_cast<const uint2*>(blk + off);
+    return make_float4(bf_lo(w.x), bf_hi(w.x), bf_lo(w.y), bf_hi(w.y));
+  }
+};
+
+template <typename MT>
+__global__ void __launch_bounds__(128) bres_kernel(const MT* __restrict__ blk, const MT* __restrict__ W,
+                                                   const int* __restrict__ nbe, const float* __restrict__ x,
+                                                   const float* __restrict__ b, float* __restrict__ r,
+                                                   float* __restrict__ x_out, int64_t B, int flags,
+                                                   const double* __restrict__ P, float* __restrict__ r1) {
+  constexpr int N = 20, F = 4;
+  constexpr int BLK = N * N;                     // entries per block
+  constexpr int EL_BYTES = (F + 1) * BLK * (int)sizeof(MT);
+  constexpr int W_BYTES = BLK * (int)sizeof(MT);
+  __shared__ __align__(16) unsigned char As[EL_BYTES];
+  __shared__ __align__(16) unsigned char Ws[W_BYTES];
+  __shared__ __align__(16) float xs[F + 1][N][kNR];
+  __shared__ __align__(16) float rs[N][kNR];
+  __shared__ int nbs[F];
+  const int64_t e = blockIdx.x;
+  if (e >= B) return;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool zerox = flags & RF_ZEROX;
+  const bool smooth = flags & RF_SMOOTH;
+  if (tid < F) nbs[tid] = nbe[e * F + tid];
+  if (!zerox) {
+    const uint4* src = reinterpret_cast<const uint4*>(blk + e * (F + 1) * BLK);
+    for (int i = tid; i < EL_BYTES / 16; i += 128) reinterpret_cast<uint4*>(As)[i] = src[i];
+  }
+  if (smooth) {
+    const uint4* src = reinterpret_cast<const uint4*>(W + e * BLK);
+    for (int i = tid; i < W_BYTES / 16; i += 128) reinterpret_cast<uint4*>(Ws)[i] = src[i];
+  }
+  __syncthreads();
+  if (!zerox) {
+    // 5 blocks x 20 nodes x kNR values = 5 * 20 * 16 float4; loads first
+    constexpr int kItems = (F + 1) * N * (kNR / 4);
+    constexpr int kPer = (kItems + 127) / 128;
+    float4 v[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int i = tid + u * 128;
+      v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i < kItems) {
+        const int bb = i / (N * (kNR / 4)), rem = i - (i / (N * (kNR / 4))) * (N * (kNR / 4));
+        const int64_t src_e = bb == 0 ? e : (int64_t)nbs[bb - 1];
+        if (src_e >= 0) v[u] = reinterpret_cast<const float4*>(x + src_e * N * kNR)[rem];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int i = tid + u * 128;
+      if (i < kItems) reinterpret_cast<float4*>(&xs[0][0][0])[i] = v[u];
+    }
+  }
+  __syncthreads();
+  const int m0 = warp * 5, r0 = lane * 2;
+  float acc[5][2];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) acc[i][0] = acc[i][1] = 0.0f;
+  if (!zerox) {
+    const MT* A = reinterpret_cast<const MT*>(As);
+#pragma unroll 1
+    for (int bb = 0; bb <= F; ++bb) {
+      if (bb > 0 && nbs[bb - 1] < 0) continue;
+      const MT* Ab = A + bb * BLK;
+#pragma unroll
+      for (int n = 0; n < N; n += 4) {
+        float4 a[5];
+#pragma unroll
+        for (int i = 0; i < 5; ++i) a[i] = BRow4<MT>::get(Ab, m0 + i, n);
+        const float2 x0 = *reinterpret_cast<const float2*>(&xs[bb][n][r0]);
+        const float2 x1 = *reinterpret_cast<const float2*>(&xs[bb][n + 1][r0]);
+        const float2 x2 = *reinterpret_cast<const float2*>(&xs[bb][n + 2][r0]);
+        const float2 x3 = *reinterpret_cast<const float2*>(&xs[bb][n + 3][r0]);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+          acc[i][0] = fmaf(a[i].x, x0.x, acc[i][0]);
+          acc[i][1] = fmaf(a[i].x, x0.y, acc[i][1]);
+          acc[i][0] = fmaf(a[i].y, x1.x, acc[i][0]);
+          acc[i][1] = fmaf(a[i].y, x1.y, acc[i][1]);
+          acc[i][0] = fmaf(a[i].z, x2.x, acc[i][0]);
+          acc[i][1] = fmaf(a[i].z, x2.y, acc[i][1]);
+          acc[i][0] = fmaf(a[i].w, x3.x, acc[i][0]);
+          acc[i][1] = fmaf(a[i].w, x3.y, acc[i][1]);
+        }
+      }
+    }
+  }
+  float res[5][2];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const int64_t o = (e * N + m0 + i) * kNR + r0;
+    float2 bv = make_float2(0.f, 0.f);
+    if (b) bv = *reinterpret_cast<const float2*>(b + o);
+    res[i][0] = bv.x - acc[i][0];
+    res[i][1] = bv.y - acc[i][1];
+    if (r) {
+      const float s = (flags & RF_NEG) ? -1.0f : 1.0f;
+      *reinterpret_cast<float2*>(r + o) = make_float2(s * res[i][0], s * res[i][1]);
+    }
+  }
+  if (flags & (RF_RESTRICT | RF_SMOOTH)) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) *reinterpret_cast<float2*>(&rs[m0 + i][r0]) = make_float2(res[i][0], res[i][1]);
+    __syncthreads();
+    if (flags & RF_RESTRICT) {
+      // r1[(e*4 + c) * kNR + q] = sum_n P[n][c] rs[n][q]; 4 x kNR outputs, 2 per thread
+      for (int o = tid; o < F * kNR; o += 128) {
+        const int cc = o / kNR, q = o % kNR;
+        float t = 0.0f;
+#pragma unroll
+        for (int n = 0; n < N; ++n) t += (float)P[n * F + cc] * rs[n][q];
+        r1[(e * F + cc) * kNR + q] = t;
+      }
+    }
+    if (smooth) {
+      const MT* Wm = reinterpret_cast<const MT*>(Ws);
+      float c[5][2];
+#pragma unroll
+      for (int i = 0; i < 5; ++i) c[i][0] = c[i][1] = 0.0f;
+#pragma unroll
+      for (int n = 0; n < N; n += 4) {
+        const float2 q0 = *reinterpret_cast<const float2*>(&rs[n][r0]);
+        const float2 q1 = *reinterpret_cast<const float2*>(&rs[n + 1][r0]);
+        const float2 q2 = *reinterpret_cast<const float2*>(&rs[n + 2][r0]);
+        const float2 q3 = *reinterpret_cast<const float2*>(&rs[n + 3][r0]);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+          const float4 w = BRow4<MT>::get(Wm, m0 + i, n);
+          c[i][0] = fmaf(w.x, q0.x, c[i][0]);
+          c[i][1] = fmaf(w.x, q0.y, c[i][1]);
+          c[i][0] = fmaf(w.y, q1.x, c[i][0]);
+          c[i][1] = fmaf(w.y, q1.y, c[i][1]);
+          c[i][0] = fmaf(w.z, q2.x, c[i][0]);
+          c[i][1] = fmaf(w.z, q2.y, c[i][1]);
+          c[i][0] = fmaf(w.w, q3.x, c[i][0]);
+          c[i][1] = fmaf(w.w, q3.y, c[i][1]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+        const int64_t o = (e * N + m0 + i) * kNR + r0;
+        float2 xo = make_float2(c[i][0], c[i][1]);
+        if (!zerox) {
+          xo.x += xs[0][m0 + i][r0];
+          xo.y += xs[0][m0 + i][r0 + 1];
+        }
+        *reinterpret_cast<float2*>(x_out + o) = xo;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The same step with BF16 blocks on the tensor cores (warp-level
+// mma.sync m16n8k16 / m16n8k8, BF16 inputs, FP32 accumulation).  Per element
+// Y (20 x kNR) = A_stack (20 x 100) X_stack (100 x kNR): the A operand is the
+// element's BF16 blocks in the chunked row layout, read directly as
+// fragments (columns 0-15 of a block = one k16 step over chunks 0 and 1,
+// columns 16-19 = one k8 step over chunk 2 with the upper half zeroed); the
+// B operand is X_stack in shared memory as [k][RHS] BF16 rows (k = 24 *
+// block + node, nodes 20..23 zero; 144-byte rows, so the eight rows an
+// ldmatrix reads fall in distinct banks), loaded with ldmatrix.trans.  x is
+// split into BF16 hi + lo parts (two MMAs each), so x keeps ~16 bits through
+// the product.  One CTA per element, 4 warps; warp w owns RHS 16w .. 16w+15.
+// The smoothing product W res goes through the tensor cores the same way.
+constexpr int kXK = 120;        // k slots (5 blocks x 24)
+constexpr int kXRow = 144;      // bytes per k slot row (64 BF16 + 16 bytes pad)
+
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                               uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ void mma_bf16_1688(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t b0) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a0), "r"(a1), "r"(b0));
+}
+
+__device__ __forceinline__ void ldm_x2_trans(uint32_t& r0, uint32_t& r1, const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0, %1}, [%2];"
+               : "=r"(r0), "=r"(r1)
+               : "r"(smem_addr(p)));
+}
+
+__device__ __forceinline__ void ldm_x1_trans(uint32_t& r0, const void* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x1.trans.shared.b16 {%0}, [%1];" : "=r"(r0) : "r"(smem_addr(p)));
+}
+
+// hi / lo BF16 parts of four consecutive values, stored at two 8-byte words
+__device__ __forceinline__ void store_split4(unsigned char* hi, unsigned char* lo, float4 v) {
+  const __nv_bfloat16 h0 = __float2bfloat16_rn(v.x), h1 = __float2bfloat16_rn(v.y), h2 = __float2bfloat16_rn(v.z),
+                      h3 = __float2bfloat16_rn(v.w);
+  const __nv_bfloat16 l0 = __float2bfloat16_rn(v.x - __bfloat162float(h0)),
+                      l1 = __float2bfloat16_rn(v.y - __bfloat162float(h1)),
+                      l2 = __float2bfloat16_rn(v.z - __bfloat162float(h2)),
+                      l3 = __float2bfloat16_rn(v.w - __bfloat162float(h3));
+  uint2 H, L;
+  H.x = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+  H.y = (uint32_t)__bfloat16_as_ushort(h2) | ((uint32_t)__bfloat16_as_ushort(h3) << 16);
+  L.x = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+  L.y = (uint32_t)__bfloat16_as_ushort(l2) | ((uint32_t)__bfloat16_as_ushort(l3) << 16);
+  *reinterpret_cast<uint2*>(hi) = H;
+  *reinterpret_cast<uint2*>(lo) = L;
+}
+
+// one block (20x20 BF16, chunked) times the slab of k slots kb .. kb+23 of
+// Xs (hi or lo): accumulates into acc[mt][nt], m tiles mt = 0, 1 (rows 0-15,
+// 16-31), n tiles nt = 0, 1 (RHS rbase + 8 nt ..)
+__device__ __forceinline__ void mma_block(float (&acc)[2][2][4], const unsigned char* blk, const unsigned char* Xs,
+                                          int kb, int rbase, int lane) {
+  const int g = lane >> 2, t = lane & 3;
+  uint32_t a[2][4], a8[2][2];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt) {
+    const int r0 = mt * 16 + g, r1 = r0 + 8;
+    const bool v0 = r0 < 20, v1 = r1 < 20;
+    a[mt][0] = v0 ? *reinterpret_cast<const uint32_t*>(blk + r0 * 16 + 4 * t) : 0u;
+    a[mt][1] = v1 ? *reinterpret_cast<const uint32_t*>(blk + r1 * 16 + 4 * t) : 0u;
+    a[mt][2] = v0 ? *reinterpret_cast<const uint32_t*>(blk + 2 * kC20Off1 + r0 * 16 + 4 * t) : 0u;
+    a[mt][3] = v1 ? *reinterpret_cast<const uint32_t*>(blk + 2 * kC20Off1 + r1 * 16 + 4 * t) : 0u;
+    a8[mt][0] = (v0 && t < 2) ? *reinterpret_cast<const uint32_t*>(blk + 2 * kC20Off2 + r0 * 8 + 4 * t) : 0u;
+    a8[mt][1] = (v1 && t < 2) ? *reinterpret_cast<const uint32_t*>(blk + 2 * kC20Off2 + r1 * 8 + 4 * t) : 0u;
+  }
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt) {
+    const int q0 = rbase + nt * 8;
+    uint32_t b0, b1, b8;
+    // lanes 0-15: rows kb .. kb+15 (two 8x8 matrices); lanes 0-7: rows kb+16 .. kb+23
+    ldm_x2_trans(b0, b1, Xs + (size_t)(kb + (lane & 15)) * kXRow + q0 * 2);
+    ldm_x1_trans(b8, Xs + (size_t)(kb + 16 + (lane & 7)) * kXRow + q0 * 2);
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+      mma_bf16_16816(acc[mt][nt], a[mt][0], a[mt][1], a[mt][2], a[mt][3], b0, b1);
+      mma_bf16_1688(acc[mt][nt], a8[mt][0], a8[mt][1], b8);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __restrict__ blk,
+                                                       const __nv_bfloat16* __restrict__ W,
+                                                       const int* __restrict__ nbe, const float* __restrict__ x,
+                                                       const float* __restrict__ b, float* __restrict__ r,
+                                                       float* __restrict__ x_out, int64_t B, int flags,
+                                                       const double* __restrict__ P, float* __restrict__ r1) {
+  constexpr int N = 20, F = 4;
+  __shared__ __align__(16) unsigned char As[(F + 1) * 800];
+  __shared__ __align__(16) unsigned char Ws[800];
+  __shared__ __align__(16) unsigned char Xhi[kXK * kXRow];
+  __shared__ __align__(16) unsigned char Xlo[kXK * kXRow];
+  __shared__ __align__(16) float rs[N][kNR];
+  __shared__ int nbs[F];
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, t = lane & 3;
+  const bool zerox = flags & RF_ZEROX;
+  const bool smooth = flags & RF_SMOOTH;
+  if (tid < F) nbs[tid] = nbe[e * F + tid];
+  if (!zerox)
+    for (int i = tid; i < (F + 1) * 800 / 16; i += 128)
+      reinterpret_cast<uint4*>(As)[i] = reinterpret_cast<const uint4*>(blk + e * 2000)[i];
+  if (smooth)
+    for (int i = tid; i < 800 / 16; i += 128) reinterpret_cast<uint4*>(Ws)[i] = reinterpret_cast<const uint4*>(W + e * 400)[i];
+  // zero pad slots (nodes 20..23 of every block): 5 x 4 rows x 64 RHS, hi and lo
+  for (int i = tid; i < (F + 1) * 4 * (kNR / 4); i += 128) {
+    const int bb = i / (4 * (kNR / 4)), rem = i % (4 * (kNR / 4));
+    const int row = bb * 24 + 20 + rem / (kNR / 4), q4 = rem % (kNR / 4);
+    *reinterpret_cast<uint2*>(Xhi + row * kXRow + q4 * 8) = make_uint2(0u, 0u);
+    *reinterpret_cast<uint2*>(Xlo + row * kXRow + q4 * 8) = make_uint2(0u, 0u);
+  }
+  __syncthreads();
+  const int rbase = warp * 16;
+  float acc[2][2][4];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[mt][nt][i] = 0.0f;
+  if (!zerox) {
+    // X_stack rows: slot 24 bb + n = x[nb_bb][n][:] (hi / lo), coalesced
+    // float4 reads; all of a thread's loads are issued before the first
+    // conversion, so the gather costs one round trip, not thirteen
+    constexpr int kItems = (F + 1) * N * (kNR / 4);          // 1600 float4
+    constexpr int kPer = (kItems + 127) / 128;               // 13 per thread
+    float4 v[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int i = tid + u * 128;
+      v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i < kItems) {
+        const int bb = i / (N * (kNR / 4)), rem = i % (N * (kNR / 4));
+        const int64_t src_e = bb == 0 ? e : (int64_t)nbs[bb - 1];
+        if (src_e >= 0) v[u] = reinterpret_cast<const float4*>(x + src_e * N * kNR)[rem];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int i = tid + u * 128;
+      if (i < kItems) {
+        const int bb = i / (N * (kNR / 4)), rem = i % (N * (kNR / 4));
+        const int n = rem / (kNR / 4), q4 = rem % (kNR / 4);
+        const int row = bb * 24 + n;
+        store_split4(Xhi + row * kXRow + q4 * 8, Xlo + row * kXRow + q4 * 8, v[u]);
+      }
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int bb = 0; bb <= F; ++bb) {
+      if (bb > 0 && nbs[bb - 1] < 0) continue;
+      mma_block(acc, As + bb * 800, Xhi, bb * 24, rbase, lane);
+      mma_block(acc, As + bb * 800, Xlo, bb * 24, rbase, lane);
+    }
+  }
+  // epilogue: rows (mt*16 + g [+8]), RHS rbase + nt*8 + 2t (+1)
+  const float sgn = (flags & RF_NEG) ? -1.0f : 1.0f;
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+      const int row = mt * 16 + g + 8 * hh;
+      if (row >= N) continue;
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        const int q = rbase + nt * 8 + 2 * t;
+        const int64_t o = (e * N + row) * kNR + q;
+        float2 bv = make_float2(0.f, 0.f);
+        if (b) bv = *reinterpret_cast<const float2*>(b + o);
+        const float2 res = make_float2(bv.x - acc[mt][nt][2 * hh], bv.y - acc[mt][nt][2 * hh + 1]);
+        if (r) *reinterpret_cast<float2*>(r + o) = make_float2(sgn * res.x, sgn * res.y);
+        *reinterpret_cast<float2*>(&rs[row][q]) = res;
+      }
+    }
+  if (!(flags & (RF_RESTRICT | RF_SMOOTH))) return;
+  __syncthreads();
+  if (flags & RF_RESTRICT) {
+    for (int o = tid; o < F * kNR; o += 128) {
+      const int cc = o / kNR, q = o % kNR;
+      float s = 0.0f;
+#pragma unroll
+      for (int n = 0; n < N; ++n) s += (float)P[n * F + cc] * rs[n][q];
+      r1[(e * F + cc) * kNR + q] = s;
+    }
+  }
+  if (smooth) {
+    // res rows into slots 0..19 (slots 20..23 are still zero)
+    for (int i = tid; i < N * (kNR / 4); i += 128) {
+      const int n = i / (kNR / 4), q4 = i % (kNR / 4);
+      store_split4(Xhi + n * kXRow + q4 * 8, Xlo + n * kXRow + q4 * 8, reinterpret_cast<const float4*>(&rs[n][0])[q4]);
+    }
+    __syncthreads();
+    float c2[2][2][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) c2[mt][nt][i] = 0.0f;
+    mma_block(c2, Ws, Xhi, 0, rbase, lane);
+    mma_block(c2, Ws, Xlo, 0, rbase, lane);
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int row = mt * 16 + g + 8 * hh;
+        if (row >= N) continue;
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) {
+          const int q = rbase + nt * 8 + 2 * t;
+          const int64_t o = (e * N + row) * kNR + q;
+          float2 xo = make_float2(c2[mt][nt][2 * hh], c2[mt][nt][2 * hh + 1]);
+          if (!zerox) {
+            const float2 xv = *reinterpret_cast<const float2*>(x + o);
+            xo.x += xv.x;
+            xo.y += xv.y;
+          }
+          *reinterpret_cast<float2*>(x_out + o) = xo;
+        }
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// DG <-> CG P1 transfers and SFC levels on kNR columns (thread per (row, RHS))
+
+// out[pos(i)][q] = sum over DG copies (e, c) of vertex i of w_ec * r1[(e, c)][q]
+__global__ void bgather_kernel(const float* __restrict__ r1, const int* __restrict__ gptr,
+                               const int* __restrict__ gent, const double* __restrict__ wdg,
+                               const int* __restrict__ pos, float* __restrict__ out, int ncg) {
+  const int i = blockIdx.x;
+  const int q = threadIdx.x;
+  if (i >= ncg) return;
+  float acc = 0.0f;
+  for (int k = gptr[i]; k < gptr[i + 1]; ++k) {
+    const int ent = gent[k];
+    acc += (float)wdg[ent] * r1[(int64_t)ent * kNR + q];
+  }
+  out[(int64_t)pos[i] * kNR + q] = acc;
+}
+
+// x[(e, n)][q] += sum_c P[n][c] * w_ec * ecg[pos(p1cg[e][c])][q]; one CTA of
+// 320 threads per element: thread (n, quad of 4 RHS)
+__global__ void __launch_bounds__(320) bprolong_kernel(float* __restrict__ x, const float* __restrict__ ecg,
+                                                       const int* __restrict__ pos, const int* __restrict__ p1cg,
+                                                       const double* __restrict__ wdg, const double* __restrict__ P,
+                                                       int64_t B) {
+  __shared__ int vp[4];
+  __shared__ float wc[4];
+  __shared__ float Ps[20][4];
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x;
+  if (tid < 4) {
+    vp[tid] = pos[p1cg[e * 4 + tid]];
+    wc[tid] = (float)wdg[e * 4 + tid];
+  }
+  if (tid < 80) Ps[tid / 4][tid % 4] = (float)P[tid];
+  __syncthreads();
+  const int n = tid / (kNR / 4), q4 = tid % (kNR / 4);
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float4 ev = reinterpret_cast<const float4*>(ecg + (int64_t)vp[c] * kNR)[q4];
+    const float f = Ps[n][c] * wc[c];
+    v.x += f * ev.x;
+    v.y += f * ev.y;
+    v.z += f * ev.z;
+    v.w += f * ev.w;
+  }
+  float4* xp = reinterpret_cast<float4*>(x + (e * 20 + n) * kNR) + q4;
+  float4 xv = *xp;
+  xv.x += v.x;
+  xv.y += v.y;
+  xv.z += v.z;
+  xv.w += v.w;
+  *xp = xv;
+}
+
+// rr = b - A e_in;  e_out = e_in + w rr / diag (e_in = NULL: zero guess)
+__global__ void bjacobi_kernel(const int* __restrict__ rowptr, const int* __restrict__ col,
+                               const float* __restrict__ val, const float* __restrict__ diag,
+                               const float* __restrict__ e_in, const float* __restrict__ b,
+                               float* __restrict__ e_out, float* __restrict__ rr_out, int n, float w) {
+  const int i = blockIdx.x * (blockDim.x / kNR) + threadIdx.x / kNR;
+  const int q = threadIdx.x % kNR;
+  if (i >= n) return;
+  float s = 0.0f;
+  if (e_in)
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += val[k] * e_in[(int64_t)col[k] * kNR + q];
+  const int64_t o = (int64_t)i * kNR + q;
+  const float rr = b[o] - s;
+  e_out[o] = (e_in ? e_in[o] : 0.0f) + rr / diag[i] * w;
+  if (rr_out) rr_out[o] = rr;
+}
+
+__global__ void brestrict_kernel(const float* __restrict__ rr, const float* __restrict__ e, float* __restrict__ r_next,
+                                 float* __restrict__ e_next, int n, int nn) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nn * kNR) return;
+  const int i = (int)(t / kNR), q = (int)(t % kNR);
+  const int a = 2 * i, bq = 2 * i + 1;
+  r_next[t] = rr[(int64_t)a * kNR + q] + (bq < n ? rr[(int64_t)bq * kNR + q] : 0.0f);
+  e_next[t] = e[(int64_t)a * kNR + q] + (bq < n ? e[(int64_t)bq * kNR + q] : 0.0f);
+}
+
+__global__ void bprolong_lev_kernel(float* __restrict__ e, const float* __restrict__ e_next, const int* __restrict__ up,
+                                    int n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * kNR) return;
+  const int i = (int)(t / kNR), q = (int)(t % kNR);
+  e[t] += e_next[(int64_t)up[i] * kNR + q];
+}
+
+// E = Ainv R on the dense coarse level: 8-row tiles (enough CTAs for the
+// GPU at ~1,000 rows), k in tiles of 64 staged in shared memory; 128
+// threads, each 1 row x 4 RHS
+__global__ void __launch_bounds__(128) bdense_kernel(const float* __restrict__ Ainv, const float* __restrict__ R,
+                                                     float* __restrict__ E, int n) {
+  __shared__ float As[8][65];
+  __shared__ __align__(16) float Rs[64][kNR];
+  const int row0 = blockIdx.x * 8;
+  const int tid = threadIdx.x;
+  const int rr = tid / 16, q4 = tid % 16;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k0 = 0; k0 < n; k0 += 64) {
+    for (int i = tid; i < 8 * 64; i += 128) {
+      const int r = i / 64, k = i % 64;
+      As[r][k] = (row0 + r < n && k0 + k < n) ? Ainv[(int64_t)(row0 + r) * n + k0 + k] : 0.0f;
+    }
+    for (int i = tid; i < 64 * (kNR / 4); i += 128) {
+      const int k = i / (kNR / 4), qq = i % (kNR / 4);
+      reinterpret_cast<float4*>(&Rs[k][0])[qq] =
+          k0 + k < n ? reinterpret_cast<const float4*>(R + (int64_t)(k0 + k) * kNR)[qq] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int k = 0; k < 64; ++k) {
+      const float4 rv = reinterpret_cast<const float4*>(&Rs[k][0])[q4];
+      const float a = As[rr][k];
+      acc.x = fmaf(a, rv.x, acc.x);
+      acc.y = fmaf(a, rv.y, acc.y);
+      acc.z = fmaf(a, rv.z, acc.z);
+      acc.w = fmaf(a, rv.w, acc.w);
+    }
+    __syncthreads();
+  }
+  if (row0 + rr < n) reinterpret_cast<float4*>(E + (int64_t)(row0 + rr) * kNR)[q4] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// Gram-Schmidt per RHS on interleaved vectors.  A block is 256 threads =
+// 4 row lanes x kNR RHS; per-thread sums FP32, the 4 lanes and the blocks
+// combined in FP64 (fixed order).
+
+// partial[(blk * 32 + j) * kNR + q] = sum over the block's rows of V_j[row][q] z[row][q],
+// j = 8 blockIdx.y .. +7; 256 threads = 16 row lanes x 16 RHS quads
+__global__ void __launch_bounds__(256) bmdot_kernel(const float* __restrict__ V, int64_t ld, int nv,
+                                                    const float* __restrict__ z, int64_t n,
+                                                    double* __restrict__ partial) {
+  __shared__ float4 red[16][8][kNR / 4];
+  const int q4 = threadIdx.x % 16, lane = threadIdx.x / 16;
+  const int j0 = blockIdx.y * 8;
+  const int cnt = min(8, nv - j0);
+  float4 acc[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t row = (int64_t)blockIdx.x * 16 + lane; row < n; row += (int64_t)gridDim.x * 16) {
+    const float4 zv = reinterpret_cast<const float4*>(z + row * kNR)[q4];
+    float4 v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      v[j] = j < cnt ? reinterpret_cast<const float4*>(V + (size_t)(j0 + j) * ld + row * kNR)[q4]
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      acc[j].x = fmaf(v[j].x, zv.x, acc[j].x);
+      acc[j].y = fmaf(v[j].y, zv.y, acc[j].y);
+      acc[j].z = fmaf(v[j].z, zv.z, acc[j].z);
+      acc[j].w = fmaf(v[j].w, zv.w, acc[j].w);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) red[lane][j][q4] = acc[j];
+  __syncthreads();
+  for (int o = threadIdx.x; o < cnt * kNR; o += 256) {
+    const int j = o / kNR, q = o % kNR;
+    double s = 0.0;
+    for (int l = 0; l < 16; ++l) s += (double)reinterpret_cast<const float*>(&red[l][j][0])[q];
+    partial[((int64_t)blockIdx.x * 32 + j0 + j) * kNR + q] = s;
+  }
+}
+
+// h[j * kNR + q] = sum over blocks of partial[(blk * 32 + j) * kNR + q]
+__global__ void breduce_kernel(const double* __restrict__ partial, int nblk, int nv, double* __restrict__ h) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= nv * kNR) return;
+  const int j = o / kNR, q = o % kNR;
+  double s = 0.0;
+  for (int bk = 0; bk < nblk; ++bk) s += partial[((int64_t)bk * 32 + j) * kNR + q];
+  h[o] = s;
+}
+
+// z[row][q] -= sum_j V_j[row][q] h[j][q]; partial[blk * kNR + q] = slice of |z_new[:, q]|^2
+__global__ void __launch_bounds__(256) baxpy_kernel(const float* __restrict__ V, int64_t ld, int nv,
+                                                    const double* __restrict__ h, float* __restrict__ z, int64_t n,
+                                                    double* __restrict__ partial) {
+  __shared__ float4 hs[32][kNR / 4];
+  __shared__ float4 red[16][kNR / 4];
+  const int q4 = threadIdx.x % 16, lane = threadIdx.x / 16;
+  for (int o = threadIdx.x; o < 32 * kNR; o += 256)
+    reinterpret_cast<float*>(&hs[0][0])[o] = o < nv * kNR ? (float)h[o] : 0.0f;
+  __syncthreads();
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t row = (int64_t)blockIdx.x * 16 + lane; row < n; row += (int64_t)gridDim.x * 16) {
+    float4* zp = reinterpret_cast<float4*>(z + row * kNR) + q4;
+    float4 zv = *zp;
+    for (int j0 = 0; j0 < nv; j0 += 8) {
+      float4 v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        v[j] = j0 + j < nv ? reinterpret_cast<const float4*>(V + (size_t)(j0 + j) * ld + row * kNR)[q4]
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float4 hv = hs[(j0 + j) & 31][q4];
+        zv.x -= v[j].x * hv.x;
+        zv.y -= v[j].y * hv.y;
+        zv.z -= v[j].z * hv.z;
+        zv.w -= v[j].w * hv.w;
+      }
+    }
+    *zp = zv;
+    acc.x = fmaf(zv.x, zv.x, acc.x);
+    acc.y = fmaf(zv.y, zv.y, acc.y);
+    acc.z = fmaf(zv.z, zv.z, acc.z);
+    acc.w = fmaf(zv.w, zv.w, acc.w);
+  }
+  red[lane][q4] = acc;
+  __syncthreads();
+  if (threadIdx.x < kNR) {
+    const int q = threadIdx.x;
+    double s = 0.0;
+    for (int l = 0; l < 16; ++l) s += (double)reinterpret_cast<const float*>(&red[l][0])[q];
+    partial[(int64_t)blockIdx.x * kNR + q] = s;
+  }
+}
+
+// Hessenberg column j of every RHS q (H[q][(m+1) * m], column-major):
+// H_q[i][j] = h[i][q] for i < nv, H_q[nv][j] = |z_q|; inv[q] = 1/|z_q| (0 if 0)
+__global__ void bfinish_kernel(const double* __restrict__ partial, int nblk, const double* __restrict__ h, int nv,
+                               int j, int m, double* __restrict__ H, float* __restrict__ inv) {
+  const int q = threadIdx.x;
+  if (q >= kNR) return;
+  double* Hq = H + (size_t)q * (m + 1) * m + (size_t)j * (m + 1);
+  for (int i = 0; i < nv; ++i) Hq[i] = h[i * kNR + q];
+  double s = 0.0;
+  for (int bk = 0; bk < nblk; ++bk) s += partial[(int64_t)bk * kNR + q];
+  const double t = sqrt(s);
+  Hq[nv] = t;
+  inv[q] = t > 0.0 ? (float)(1.0 / t) : 0.0f;
+}
+
+// v[row][q] = z[row][q] * inv[q]  (float4; total a multiple of kNR)
+__global__ void bscale_kernel(const float* __restrict__ z, const float* __restrict__ inv, float* __restrict__ v,
+                              int64_t total) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;   // float4 index
+  if (t * 4 >= total) return;
+  const int q = (int)((t * 4) % kNR);
+  float4 a = reinterpret_cast<const float4*>(z)[t];
+  a.x *= inv[q];
+  a.y *= inv[q + 1];
+  a.z *= inv[q + 2];
+  a.w *= inv[q + 3];
+  reinterpret_cast<float4*>(v)[t] = a;
+}
+
+// d[row][q] += sum_j Z_j[row][q] y[j][q]
+__global__ void bcombine_kernel(const float* __restrict__ Z, int64_t ld, int k, const double* __restrict__ y,
+                                float* __restrict__ d, int64_t total) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int q = (int)(t % kNR);
+  float s = d[t];
+  for (int j = 0; j < k; ++j) s += Z[(size_t)j * ld + t] * (float)y[j * kNR + q];
+  d[t] = s;
+}
+
+// column norms^2 of an interleaved vector: partial[blk * kNR + q]
+__global__ void __launch_bounds__(256) bnorm_kernel(const float* __restrict__ z, int64_t n,
+                                                    double* __restrict__ partial) {
+  __shared__ float red[4][kNR];
+  const int q = threadIdx.x % kNR, lane4 = threadIdx.x / kNR;
+  float acc = 0.0f;
+  for (int64_t row = (int64_t)blockIdx.x * 4 + lane4; row < n; row += (int64_t)gridDim.x * 4) {
+    const float v = z[row * kNR + q];
+    acc = fmaf(v, v, acc);
+  }
+  red[lane4][q] = acc;
+  __syncthreads();
+  if (threadIdx.x < kNR) {
+    double s = 0.0;
+    for (int l = 0; l < 4; ++l) s += (double)red[l][threadIdx.x];
+    partial[(int64_t)blockIdx.x * kNR + threadIdx.x] = s;
+  }
+}
+
+// out[q] = sqrt(sum_blk partial[blk * kNR + q]); inv[q] = 1/out (0 if 0)
+__global__ void bnorm_finish_kernel(const double* __restrict__ partial, int nblk, double* __restrict__ out,
+                                    float* __restrict__ inv) {
+  const int q = threadIdx.x;
+  if (q >= kNR) return;
+  double s = 0.0;
+  for (int bk = 0; bk < nblk; ++bk) s += partial[(int64_t)bk * kNR + q];
+  const double t = sqrt(s);
+  out[q] = t;
+  if (inv) inv[q] = t > 0.0 ? (float)(1.0 / t) : 0.0f;
+}
+
+// interleave: out[row][q] = (float)(in_q[row] * s[q]) for q < nrhs (in_q = in + q * n), 0 beyond
+__global__ void binterleave_kernel(const double* __restrict__ in, int64_t n, int nrhs, const double* __restrict__ s,
+                                   float* __restrict__ out) {
+  __shared__ float tile[32][33];
+  const int64_t row0 = (int64_t)blockIdx.x * 32;
+  const int q0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;   // 32 x 8
+  for (int k = ty; k < 32; k += 8) {
+    const int q = q0 + k;
+    const int64_t row = row0 + tx;
+    float v = 0.0f;
+    if (q < nrhs && row < n) v = (float)(in[(int64_t)q * n + row] * s[q]);
+    tile[k][tx] = v;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t row = row0 + k;
+    if (row < n) out[row * kNR + q0 + tx] = tile[tx][k];
+  }
+}
+
+// de-interleave and update: x_q[row] += a[q] * d[row][q] (FP64) for q < nrhs
+__global__ void bupdate_kernel(double* __restrict__ x, int64_t n, int nrhs, const double* __restrict__ a,
+                               const float* __restrict__ d) {
+  __shared__ float tile[32][33];
+  const int64_t row0 = (int64_t)blockIdx.x * 32;
+  const int q0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t row = row0 + k;
+    tile[k][tx] = row < n ? d[row * kNR + q0 + tx] : 0.0f;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int q = q0 + k;
+    const int64_t row = row0 + tx;
+    if (q < nrhs && row < n && a[q] != 0.0) x[(int64_t)q * n + row] += a[q] * (double)tile[tx][k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+struct BatchState {
+  int m = 0;
+  float *V = nullptr, *Z = nullptr;
+  float *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t6 = nullptr;
+  float* r1 = nullptr;                      // (B * 4, kNR)
+  std::vector<float*> lr, le, le2, lrr;     // per SFC level (n_l, kNR)
+  double *H = nullptr, *part = nullptr, *h = nullptr, *nrm = nullptr, *scl = nullptr, *y = nullptr;
+  float* inv = nullptr;
+  double* r64 = nullptr;                    // (kNR, nonods) FP64 residuals, RHS-major
+  int nblk = 0;
+};
+
+void destroy_batch(void* batch) { delete static_cast<BatchState*>(batch); }
+
+BatchState& batch_of(Mixed& M) {
+  if (!M.batch) M.batch = new BatchState();
+  return *static_cast<BatchState*>(M.batch);
+}
+
+int ensure_batch(dg_ctx* c, int m) {
+  Mixed& M = mixed_of(c);
+  BatchState& S = batch_of(M);
+  int rc;
+  const size_t nv = (size_t)c->nonods * kNR;
+  if (!S.t1) {
+    for (float** t : {&S.t1, &S.t2, &S.t3, &S.t4, &S.t6})
+      if ((rc = dalloc(c, t, nv))) return rc;
+    if ((rc = dalloc(c, &S.r1, (size_t)c->B * 4 * kNR))) return rc;
+    S.nblk = 2 * c->nsm;
+    if ((rc = dalloc(c, &S.part, (size_t)S.nblk * 32 * kNR))) return rc;
+    if ((rc = dalloc(c, &S.h, (size_t)32 * kNR))) return rc;
+    if ((rc = dalloc(c, &S.nrm, (size_t)kNR))) return rc;
+    if ((rc = dalloc(c, &S.scl, (size_t)kNR))) return rc;
+    if ((rc = dalloc(c, &S.y, (size_t)32 * kNR))) return rc;
+    if ((rc = dalloc(c, &S.inv, (size_t)kNR))) return rc;
+    if ((rc = dalloc(c, &S.r64, (size_t)c->nonods * kNR))) return rc;
+    S.lr.assign(M.lev.size(), nullptr);
+    S.le = S.le2 = S.lrr = S.lr;
+    for (size_t l = 0; l < M.lev.size(); ++l) {
+      const size_t n = (size_t)M.lev[l].n * kNR;
+      if ((rc = dalloc(c, &S.lr[l], n)) || (rc = dalloc(c, &S.le[l], n)) || (rc = dalloc(c, &S.le2[l], n)) ||
+          (rc = dalloc(c, &S.lrr[l], n)))
+        return rc;
+    }
+  }
+  if (S.m < m) {
+    if ((rc = dalloc(c, &S.V, (size_t)(m + 1) * nv))) return rc;
+    if ((rc = dalloc(c, &S.Z, (size_t)m * nv))) return rc;
+    if ((rc = dalloc(c, &S.H, (size_t)kNR * (m + 1) * m))) return rc;
+    S.m = m;
+  }
+  return DG_OK;
+}
+
+template <typename MT>
+int bres(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out, int flags,
+         float* r1, cudaStream_t st) {
+  if (c->B > 0)
+    bres_kernel<MT><<<(unsigned)c->B, 128, 0, st>>>(blk, W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, r1);
+  bump();
+  CKL(c);
+  return DG_OK;
+}
+
+// batched preconditioner (same schedule as precond32, dense coarse level)
+int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
+  Mixed& M = mixed_of(c);
+  BatchState& S = batch_of(M);
+  int rc;
+  const int nsm = c->cfg.pre_smooth_its;
+  const float w = (float)c->cfg.jac_wei;
+  float* cur = S.t3;
+  float* other = S.t4;
+  const bool bf = c->precond_bf16;
+  auto pc = [&](const float* xx, float* xo, int flags, float* rr1) -> int {
+    if (bf && c->batched_mma) {
+      if (c->B > 0)
+        bres_mma_kernel<<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B, flags,
+                                                        c->T.P, rr1);
+      bump();
+      CKL(c);
+      return (int)DG_OK;
+    }
+    return bf ? bres<__nv_bfloat16>(c, M.blk16, M.W16, xx, r, nullptr, xo, flags, rr1, st)
+              : bres<float>(c, M.blk, M.W, xx, r, nullptr, xo, flags, rr1, st);
+  };
+  if ((rc = pc(nullptr, cur, RF_ZEROX | RF_SMOOTH, nullptr))) return rc;
+  for (int it = 1; it < nsm; ++it) {
+    if ((rc = pc(cur, other, RF_SMOOTH, nullptr))) return rc;
+    std::swap(cur, other);
+  }
+  if ((rc = pc(cur, nullptr, RF_RESTRICT, S.r1))) return rc;
+  bgather_kernel<<<(unsigned)c->ncg, kNR, 0, st>>>(S.r1, c->d_gptr, c->d_gent, c->d_wdg, c->d_pos, S.lr[0],
+                                                   (int)c->ncg);
+  bump();
+  const int lc = M.dense_l;
+  for (int l = 0; l < lc; ++l) {
+    const int n = M.lev[l].n;
+    const unsigned g = nblk((int64_t)n, 4);
+    for (int it = 0; it <= c->cfg.pre_smooth_its; ++it) {
+      const bool last = it == c->cfg.pre_smooth_its;
+      const float* ein = (l == 0 && it == 0) ? nullptr : S.le[l];
+      bjacobi_kernel<<<g, 4 * kNR, 0, st>>>(M.lev[l].rowptr, M.lev[l].col, M.lev[l].val, M.lev[l].diag, ein, S.lr[l],
+                                            S.le2[l], last ? S.lrr[l] : nullptr, n, w);
+      bump();
+      std::swap(S.le[l], S.le2[l]);
+    }
+    const int nn = M.lev[l + 1].n;
+    brestrict_kernel<<<nblk((int64_t)nn * kNR, 256), 256, 0, st>>>(S.lrr[l], S.le[l], S.lr[l + 1], S.le[l + 1], n, nn);
+    bump();
+  }
+  bdense_kernel<<<nblk(M.lev[lc].n, 8), 128, 0, st>>>(M.dense_inv, S.lr[lc], S.le[lc], M.lev[lc].n);
+  bump();
+  for (int l = lc - 1; l >= 0; --l) {
+    const int n = M.lev[l].n;
+    bprolong_lev_kernel<<<nblk((int64_t)n * kNR, 256), 256, 0, st>>>(S.le[l], S.le[l + 1], M.lev[l].up, n);
+    bump();
+    for (int it = 0; it < c->cfg.post_smooth_its; ++it) {
+      bjacobi_kernel<<<nblk((int64_t)n, 4), 4 * kNR, 0, st>>>(M.lev[l].rowptr, M.lev[l].col, M.lev[l].val,
+                                                              M.lev[l].diag, S.le[l], S.lr[l], S.le2[l], nullptr, n, w);
+      bump();
+      std::swap(S.le[l], S.le2[l]);
+    }
+  }
+  bprolong_kernel<<<(unsigned)c->B, 20 * (kNR / 4), 0, st>>>(cur, S.le[0], c->d_pos, c->d_p1cg, c->d_wdg, c->T.P,
+                                                             c->B);
+  bump();
+  for (int it = 0; it < nsm; ++it) {
+    float* out = (it == nsm - 1) ? z : other;
+    if ((rc = pc(cur, out, RF_SMOOTH, nullptr))) return rc;
+    other = cur;
+    cur = out;
+  }
+  CKL(c);
+  return DG_OK;
+}
+
+// Gram-Schmidt of w against V[0..j] for every RHS; writes H_q column j and V[j+1]
+int bcgs(dg_ctx* c, int j, float* w, int m, cudaStream_t st) {
+  Mixed& M = mixed_of(c);
+  BatchState& S = batch_of(M);
+  const int nv = j + 1;
+  const int64_t ld = c->nonods * kNR;
+  bmdot_kernel<<<dim3(S.nblk, (nv + 7) / 8), 256, 0, st>>>(S.V, ld, nv, w, c->nonods, S.part);
+  breduce_kernel<<<nblk((int64_t)nv * kNR, 256), 256, 0, st>>>(S.part, S.nblk, nv, S.h);
+  baxpy_kernel<<<S.nblk, 256, 0, st>>>(S.V, ld, nv, S.h, w, c->nonods, S.part);
+  bfinish_kernel<<<1, kNR, 0, st>>>(S.part, S.nblk, S.h, nv, j, m, S.H, S.inv);
+  bscale_kernel<<<nblk(ld / 4, 256), 256, 0, st>>>(w, S.inv, S.V + (size_t)nv * ld, ld);
+  bump(5);
+  CKL(c);
+  return DG_OK;
+}
+
+}  // namespace
+
+// Batched mixed-precision solve of nrhs <= 64 systems A x_q = b_q on one
+// operator (P3 tetrahedra): x and b are (nrhs, nonods) FP64, RHS-major;
+// each x_q starts from its content and stops at ||b_q - A x_q|| <= tol[q]
+// (FP64 true residual).  its / res (per RHS, may be NULL) receive the inner
+// iterations run while q was active and the final residual norm.
+extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int32_t nrhs, const double* tol,
+                                      int32_t m, int32_t max_its, double inner_rtol, int32_t* its_out,
+                                      double* res_out, void* stream) {
+  if (!c || !x || !b || !tol) return set_thread_error(DG_ERR_ARG, "dg_solve_mixed_batched: null argument");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_solve_mixed_batched: operator not built");
+  if (c->D != 3) return fail(c, DG_ERR_ARG, "dg_solve_mixed_batched: P3 tetrahedra only");
+  if (nrhs < 1 || nrhs > kNR || m < 1 || m > 31 || max_its < 0 || !(inner_rtol > 0.0 && inner_rtol < 1.0))
+    return fail(c, DG_ERR_ARG, "dg_solve_mixed_batched: need 1 <= nrhs <= 64, 1 <= m <= 31, 0 < inner_rtol < 1");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  CK(c, cudaSetDevice(c->dev));
+  Mixed& M = mixed_of(c);
+  int rc;
+  if (!M.built || c->mixed_version != c->build_version) {
+    if ((rc = build_mixed(c, st))) return rc;
+    c->mixed_version = c->build_version;
+  }
+  if (M.dense_l < 0) return fail(c, DG_ERR_STATE, "dg_solve_mixed_batched: needs the dense coarse level");
+  if (!c->f32_tma) return fail(c, DG_ERR_STATE, "dg_solve_mixed_batched: needs the chunked FP32 block layout");
+  if ((rc = ensure_batch(c, m))) return rc;
+  BatchState& S = batch_of(M);
+  const int64_t n = c->nonods;
+  const int64_t ld = n * kNR;
+  const dim3 tgrid((unsigned)((n + 31) / 32), kNR / 32), tblock(32, 8);
+  std::vector<double> rn(kNR, 0.0), tolv(kNR, 0.0), target(kNR, 0.0), beta0(kNR, 0.0), a(kNR, 0.0);
+  std::vector<int32_t> its(kNR, 0);
+  std::vector<char> active(kNR, 0);
+  for (int q = 0; q < nrhs; ++q) tolv[q] = tol[q];
+  std::vector<double> Hh((size_t)kNR * (m + 1) * m), ybuf((size_t)32 * kNR), nrm(kNR);
+  auto outer_residuals = [&]() -> int {
+    int r2;
+    for (int q = 0; q < nrhs; ++q) {
+      if ((r2 = residual(c, x + (size_t)q * n, b + (size_t)q * n, S.r64 + (size_t)q * n, nullptr, 0, st))) return r2;
+      if ((r2 = norm2(c, S.r64 + (size_t)q * n, c->d_scal + q, st))) return r2;
+    }
+    CK(c, cudaMemcpyAsync(rn.data(), c->d_scal, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    return DG_OK;
+  };
+  if ((rc = outer_residuals())) return rc;
+  int total = 0, status = DG_OK;
+  while (total < max_its) {
+    int nact = 0;
+    for (int q = 0; q < kNR; ++q) {
+      active[q] = q < nrhs && std::isfinite(rn[q]) && rn[q] > tolv[q];
+      nact += active[q];
+      a[q] = active[q] ? 1.0 / rn[q] : 0.0;
+    }
+    for (int q = 0; q < nrhs; ++q)
+      if (!std::isfinite(rn[q])) status = DG_ERR_NUMERIC;
+    if (nact == 0 || status) break;
+    // rhs32 = r64 / |r| (inactive columns zero), d32 = 0
+    CK(c, cudaMemcpyAsync(S.scl, a.data(), sizeof(double) * kNR, cudaMemcpyHostToDevice, st));
+    binterleave_kernel<<<tgrid, tblock, 0, st>>>(S.r64, n, nrhs, S.scl, S.t2);
+    bump();
+    CK(c, cudaMemsetAsync(S.t6, 0, sizeof(float) * ld, st));
+    for (int q = 0; q < kNR; ++q) target[q] = active[q] ? std::max(inner_rtol, 0.5 * tolv[q] / rn[q]) : 0.0;
+    std::fill(beta0.begin(), beta0.end(), -1.0);
+    bool inner_done = false, first_cycle = true;
+    while (!inner_done && total < max_its) {
+      // V0 = rhs - A d (d = 0 on the first cycle); beta_q = |V0_q|
+      if (first_cycle) {
+        CK(c, cudaMemcpyAsync(S.V, S.t2, sizeof(float) * ld, cudaMemcpyDeviceToDevice, st));
+      } else if ((rc = bres<float>(c, M.blk, M.W, S.t6, S.t2, S.V, nullptr, 0, nullptr, st))) {
+        return rc;
+      }
+      bnorm_kernel<<<S.nblk, 256, 0, st>>>(S.V, n, S.part);
+      bnorm_finish_kernel<<<1, kNR, 0, st>>>(S.part, S.nblk, S.nrm, S.inv);
+      bscale_kernel<<<nblk(ld / 4, 256), 256, 0, st>>>(S.V, S.inv, S.V, ld);
+      bump(3);
+      CK(c, cudaMemcpyAsync(nrm.data(), S.nrm, sizeof(double) * kNR, cudaMemcpyDeviceToHost, st));
+      CK(c, cudaMemsetAsync(S.H, 0, sizeof(double) * kNR * (m + 1) * m, st));
+      CK(c, cudaStreamSynchronize(st));
+      bool any = false;
+      for (int q = 0; q < kNR; ++q) {
+        if (!active[q]) continue;
+        if (beta0[q] < 0.0) beta0[q] = nrm[q];
+        if (nrm[q] > target[q] * beta0[q]) any = true;
+      }
+      first_cycle = false;
+      if (!any) break;
+      int k = 0;
+      std::vector<char> conv(kNR, 0);
+      for (int j = 0; j < m && total < max_its; ++j) {
+        float* zj = S.Z + (size_t)j * ld;
+        if ((rc = bprecond(c, S.V + (size_t)j * ld, zj, st))) return rc;
+        if ((rc = bres<float>(c, M.blk, M.W, zj, nullptr, S.t1, nullptr, RF_NEG, nullptr, st))) return rc;
+        if ((rc = bcgs(c, j, S.t1, m, st))) return rc;
+        ++total;
+        k = j + 1;
+        for (int q = 0; q < kNR; ++q)
+          if (active[q]) ++its[q];
+        if (k % 5 == 0 || k == m) {
+          CK(c, cudaMemcpyAsync(Hh.data(), S.H, sizeof(double) * Hh.size(), cudaMemcpyDeviceToHost, st));
+          CK(c, cudaStreamSynchronize(st));
+          bool all = true;
+          for (int q = 0; q < kNR; ++q) {
+            if (!active[q] || nrm[q] <= target[q] * beta0[q]) continue;
+            std::vector<double> Hq(Hh.begin() + (size_t)q * (m + 1) * m, Hh.begin() + (size_t)(q + 1) * (m + 1) * m);
+            std::vector<double> yq;
+            bool ok = true;
+            const double est = hessenberg_ls(Hq, m, k, nrm[q], yq, ok);
+            if (!ok || !(est <= target[q] * beta0[q])) all = false;
+          }
+          if (all) break;
+        }
+      }
+      // per-RHS least squares over the k steps, d += Z y
+      CK(c, cudaMemcpyAsync(Hh.data(), S.H, sizeof(double) * Hh.size(), cudaMemcpyDeviceToHost, st));
+      CK(c, cudaStreamSynchronize(st));
+      std::fill(ybuf.begin(), ybuf.end(), 0.0);
+      bool alld = true;
+      for (int q = 0; q < kNR; ++q) {
+        if (!active[q] || nrm[q] <= target[q] * beta0[q]) continue;
+        std::vector<double> Hq(Hh.begin() + (size_t)q * (m + 1) * m, Hh.begin() + (size_t)(q + 1) * (m + 1) * m);
+        std::vector<double> yq;
+        bool ok = true;
+        const double est = hessenberg_ls(Hq, m, k, nrm[q], yq, ok);
+        if (!ok) {
+          active[q] = 0;   // breakdown of this RHS: keep its current iterate
+          continue;
+        }
+        for (int i = 0; i < k; ++i) ybuf[(size_t)i * kNR + q] = yq[i];
+        if (!(est <= target[q] * beta0[q])) alld = false;
+      }
+      CK(c, cudaMemcpyAsync(S.y, ybuf.data(), sizeof(double) * 32 * kNR, cudaMemcpyHostToDevice, st));
+      bcombine_kernel<<<nblk(ld, 256), 256, 0, st>>>(S.Z, ld, k, S.y, S.t6, ld);
+      bump();
+      CKL(c);
+      inner_done = alld;
+    }
+    // x_q += |r_q| d_q for the active RHS
+    for (int q = 0; q < kNR; ++q) a[q] = active[q] ? rn[q] : 0.0;
+    CK(c, cudaMemcpyAsync(S.scl, a.data(), sizeof(double) * kNR, cudaMemcpyHostToDevice, st));
+    bupdate_kernel<<<tgrid, tblock, 0, st>>>(x, n, nrhs, S.scl, S.t6);
+    bump();
+    CKL(c);
+    if ((rc = outer_residuals())) return rc;
+  }
+  bool all_conv = true;
+  for (int q = 0; q < nrhs; ++q) {
+    if (its_out) its_out[q] = its[q];
+    if (res_out) res_out[q] = rn[q];
+    if (!(rn[q] <= tolv[q])) all_conv = false;
+  }
+  if (status) {
+    c->err = "batched solve: non-finite residual";
+    return status;
+  }
+  if (!all_conv) {
+    c->err = "batched solve reached the iteration limit";
+    return DG_ERR_NOCONV;
+  }
+  return DG_OK;
+}

@@ -57,7 +57,11 @@ struct Mixed {
   // nblk4 = ceil(nonods / 4 / 256) blocks, KMAXV sums per block
   double* part = nullptr;
   int nblk4 = 0;
+  // batched (multi-RHS) solve state (dg_batched.cuh)
+  void* batch = nullptr;
 };
+
+void destroy_batch(void* batch);   // dg_batched.cuh
 
 __global__ void f64_to_f32_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t n, double scale) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -625,6 +629,7 @@ void destroy_mixed(dg_ctx* c) {
   Mixed* M = static_cast<Mixed*>(c->mixed_state);
   for (auto& g : M->graphs)
     if (g) cudaGraphExecDestroy(g);
+  destroy_batch(M->batch);   // host-side state only: device buffers are context allocations
   delete M;
   c->mixed_state = nullptr;
 }

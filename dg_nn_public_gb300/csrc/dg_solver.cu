@@ -107,6 +107,8 @@ struct dg_ctx {
   bool l2_hint = true;
   // link the kernels of an inner Arnoldi step by programmatic dependent launch
   bool use_pdl = true;
+  // batched solve: BF16 preconditioner steps on the tensor cores (mma.sync)
+  bool batched_mma = true;
   int tma_variant = 0;   // elements per group / stages / CTAs per SM of that kernel
   bool verbose = false;
   // mixed preconditioner smoother: 0 = the reference's three point-Jacobi
@@ -609,6 +611,7 @@ int read_scalar(dg_ctx* c, const double* d, double* h, cudaStream_t st) {
 }  // namespace
 
 #include "dg_mixed.cuh"
+#include "dg_batched.cuh"
 
 // ===========================================================================
 extern "C" {
@@ -685,6 +688,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (bt && bt[0]) c->bf16_tma = bt[0] != '0';
     const char* ft = std::getenv("DG_F32_TMA");
     if (ft && ft[0]) c->f32_tma = ft[0] != '0';
+    const char* bm = std::getenv("DG_BATCHED_MMA");
+    if (bm && bm[0]) c->batched_mma = bm[0] != '0';
     const char* pd = std::getenv("DG_PDL");
     if (pd && pd[0]) c->use_pdl = pd[0] != '0';
     const char* lh = std::getenv("DG_L2_HINT");

@@ -282,6 +282,31 @@ class DGSolver:
             return out, its, res
         return x, its, res
 
+    def solve_mixed_batched(self, X, Bm, tol, m=None, max_its=None, inner_rtol=1e-3, raise_noconv=False):
+        """Solve A X[q] = Bm[q] for up to 64 right-hand sides together (FP64
+        CUDA tensors of shape (nrhs, nonods), in place on X), each to
+        ||Bm[q] - A X[q]|| <= tol[q].  Returns (inner its, residual norms)
+        per RHS as numpy arrays."""
+        torch = _torch()
+        if X.dim() != 2 or X.shape != Bm.shape or X.shape[1] != self.nonods:
+            raise ValueError("X and Bm must be (nrhs, %d)" % self.nonods)
+        nrhs = X.shape[0]
+        for t in (X, Bm):
+            if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+                raise ValueError("expected contiguous FP64 CUDA tensors")
+        m = min(self.cfg.gmres_m if m is None else m, 31)
+        max_its = 100 * m if max_its is None else max_its
+        tolv = np.ascontiguousarray(np.broadcast_to(np.asarray(tol, dtype=np.float64), (nrhs,)))
+        its = np.zeros(nrhs, dtype=np.int32)
+        res = np.zeros(nrhs, dtype=np.float64)
+        rc = self._lib.dg_solve_mixed_batched(self._ctx, X.data_ptr(), Bm.data_ptr(), nrhs, tolv.ctypes.data, m,
+                                              max_its, float(inner_rtol), its.ctypes.data, res.ctypes.data,
+                                              self._stream())
+        if rc == _capi.DG_ERR_NOCONV and not raise_noconv:
+            return its, res
+        self._chk(rc)
+        return its, res
+
     def set_mixed_options(self, smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=1200):
         """Mixed preconditioner: smoother 'jacobi3' (three point-Jacobi sweeps,
         as the reference) or 'blockinv' (smooth_w * A_ee^-1); BF16 block copies

@@ -158,6 +158,15 @@ int dg_solve_mixed(dg_ctx* ctx, double* x, const double* b, double tol, int32_t 
                    double inner_rtol, int32_t* its, double* res_norm, int32_t* outer, void* stream);
 /* y = A x with the FP32 copy of the operator blocks (FP32 vectors). */
 int dg_apply_f32(dg_ctx* ctx, const float* x, float* y, void* stream);
+/* Batched mixed-precision solve (P3 tetrahedra): nrhs <= 64 systems
+ * A x_q = b_q on one operator, x and b (nrhs, nonods) FP64 [device],
+ * RHS-major; each stops at ||b_q - A x_q|| <= tol[q] [host] (FP64 true
+ * residual).  The inner flexible GMRES(m <= 31) runs all active RHS in
+ * lockstep on RHS-interleaved FP32 vectors, so every kernel reads the stored
+ * blocks once for all of them.  its / res_norm [host] (nrhs, may be NULL).
+ * The batched counterpart of _gmres_mg_solver (z06/volume_mf_diff.py:1757). */
+int dg_solve_mixed_batched(dg_ctx* ctx, double* x, const double* b, int32_t nrhs, const double* tol, int32_t m,
+                           int32_t max_its, double inner_rtol, int32_t* its, double* res_norm, void* stream);
 /* z = the mixed-precision preconditioner applied once to r (FP32 vectors):
  * the DG->CG SFC V-cycle of dg_precond with the FP32/BF16 block copies and
  * the options of dg_set_mixed_options -- the reduced-precision counterpart
