@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c2", "c3"],
+    ap.add_argument("--config", default="c2", choices=["c2", "c3", "c5"],
                     help="c2: 20^3 Kuhn cube, kappa = 1; c3: 40^3 (384,000 tets), log-normal kappa (sigma 1)")
     ap.add_argument("--n", type=int, default=None, help="cells per cube side (overrides --config)")
     ap.add_argument("--kappa-sigma", type=float, default=None,
@@ -61,10 +61,14 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-roofline", action="store_true", help="skip the isolated apply timing")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-RHS batched leg")
+    ap.add_argument("--requests", type=int, default=40, help="c5: requests in the served stream")
+    ap.add_argument("--rate", type=float, default=8.0, help="c5: Poisson arrival rate (requests / s)")
+    ap.add_argument("--nrhs", type=int, default=64, help="right-hand sides of the batched leg")
     ap.add_argument("--mode", default="both", choices=["both", "fp64", "mixed"],
                     help="which solver(s) to time; the faster converged one is the headline")
     a = ap.parse_args()
-    preset = {"c2": (20, 0.0, "mean"), "c3": (40, 1.0, "harmonic")}[a.config]
+    preset = {"c2": (20, 0.0, "mean"), "c3": (40, 1.0, "harmonic"), "c5": (20, 0.5, "harmonic")}[a.config]
     if a.n is None:
         a.n = preset[0]
     if a.kappa_sigma is None:
@@ -158,6 +162,28 @@ def workload(args):
         kappa = np.exp(args.kappa_sigma * np.random.default_rng(args.seed + 1).standard_normal(m.nele))
         f = f * kappa[:, None]
     return m, order, el, f.reshape(-1), u.reshape(-1), kappa
+
+
+def fourier_rhs(m, nrhs, seed):
+    """Sum of 8 Fourier modes per RHS: integer wavenumbers 1..4 per axis,
+    N(0,1) amplitudes, seeded; homogeneous Dirichlet data.  The exact
+    solution is sum a_k / (pi^2 |k|^2) prod sin(k_d pi x_d)."""
+    rng = np.random.default_rng(seed)
+    X = m.x_ref_in
+    F = np.zeros((nrhs, m.nele * m.nloc))
+    U = np.zeros((nrhs, m.nele * m.nloc))
+    for q in range(nrhs):
+        f = np.zeros((m.nele, m.nloc))
+        u = np.zeros((m.nele, m.nloc))
+        for _ in range(8):
+            k = rng.integers(1, 5, size=3)
+            a = rng.standard_normal()
+            mode = np.prod([np.sin(k[d] * np.pi * X[:, d]) for d in range(3)], axis=0)
+            f += a * np.pi ** 2 * float((k ** 2).sum()) * mode
+            u += a * mode
+        F[q] = f.reshape(-1)
+        U[q] = u.reshape(-1)
+    return F, U
 
 
 def config_block(args, m, extra=None):
@@ -466,6 +492,45 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk,
     }
+    # batched leg (c4): nrhs Fourier right-hand sides on the same operator,
+    # solved together; value = nrhs * DOFs * steps / time
+    if not args.no_batched and kappa is None and args.nrhs > 0:
+        Fb, Ub = fourier_rhs(m, args.nrhs, seed=args.seed + 2)
+        Bm = torch.stack([s.rhs(torch.tensor(Fb[q], device=dev)) for q in range(args.nrhs)]).contiguous()
+        tolb = 1e-10 * torch.linalg.norm(Bm, dim=1).cpu().numpy()
+        Xb = torch.zeros_like(Bm)
+        for _ in range(max(1, args.warmup)):
+            Xb.zero_()
+            s.solve_mixed_batched(Xb, Bm, tolb)
+        torch.cuda.synchronize()
+        l0 = _capi.launch_count()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        its_b = []
+        for _ in range(args.steps):
+            Xb.zero_()
+            itb, resb = s.solve_mixed_batched(Xb, Bm, tolb)
+            its_b.append(int(itb.max()))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        tb = e0.elapsed_time(e1) / 1e3
+        rel_b = max(float(torch.linalg.norm(s.residual(Xb[q].contiguous(), Bm[q].contiguous())) / tolb[q] * 1e-10)
+                    for q in range(args.nrhs))
+        err_b = float(np.abs(Xb.cpu().numpy() - Ub).max() / np.abs(Ub).max())
+        out["batched"] = {
+            "workload": "c4: the %s mesh with %d Fourier right-hand sides (8 modes each, wavenumbers 1..4, "
+                        "N(0,1) amplitudes, seed %d), solved together" % (
+                            "c2" if args.n == 20 else "n=%d" % args.n, args.nrhs, args.seed + 2),
+            "value": ws * args.nrhs * dofs * args.steps / tb, "unit": "DOF/s",
+            "ms_per_step": tb * 1e3 / args.steps, "nrhs": args.nrhs, "its_max": its_b,
+            "max_rel_residual": rel_b, "max_nodal_error_vs_exact_rel": err_b,
+            "gpu_launches": _capi.launch_count() - l0,
+            "speedup_vs_single_mixed": (ws * args.nrhs * dofs * args.steps / tb) / RMX["value"] if RMX else None,
+            "speedup_vs_fp64": (ws * args.nrhs * dofs * args.steps / tb) / R64["value"] if R64 else None,
+            "method": "lockstep flexible GMRES(30) on RHS-interleaved FP32 vectors; BF16 block smoothing on "
+                      "tensor cores (mma.sync m16n8k16, x split into BF16 hi+lo), FP32 apply on CUDA cores; "
+                      "per-RHS FP64 refinement"}
     if rank == 0 and not args.no_cpu_baseline and kappa is not None:
         out["cpu_baseline"] = {"value": None, "unit": "DOF/s",
                                "skipped": "the CPU restatement is timed on the kappa = 1 workloads only "
@@ -509,9 +574,56 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_serving(args):
+    """c5: a seeded Poisson stream of solves on resident Kuhn-cube meshes of
+    5 sizes (n = 8, 12, 20, 28, 36), per-request log-normal kappa (sigma 0.5,
+    harmonic face kappa) and 8-mode Fourier sources, mixed precision to 1e-10;
+    HBM admission with half the free device memory as the budget."""
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1 and rank != 0:
+        return
+    torch.cuda.set_device(local)
+    from dg_nn_public_gb300 import build, serving
+    build.build()
+    sizes = [8, 12, 20, 28, 36]
+    free, total = torch.cuda.mem_get_info(local)
+    t0 = time.perf_counter()
+    srv = serving.SolveServer(sizes, hbm_budget=0.5 * free, rtol=1e-10, smooth=args.smooth, device=local,
+                              seed=args.seed)
+    reqs = serving.make_requests(sizes, args.requests, args.rate, sigma=0.5, seed=args.seed + 5, meshes=srv.meshes)
+    # warm-up: one request per size sets up the first slot of every mesh
+    srv.run([serving.Request(1000 + k, n, np.ones(srv.meshes[n].nele), np.ones(srv.meshes[n].nele * 20), 0.0)
+             for k, n in enumerate(sizes)])
+    t_setup = time.perf_counter() - t0
+    clocks = ClockSampler(local)
+    clocks.start()
+    res = srv.run(reqs)
+    clk = clocks.stop()
+    st = serving.latency_stats(res)
+    worst = max(r.residual / r.tol for r in res)
+    out = {"metric": METRIC, "value": st["dofs_per_s"], "unit": "DOF/s", "n_gpus": 1, "steps": len(res),
+           "warmup": len(sizes), "ms_per_step": st["mean_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+           "config": {"workload": "c5: %d requests, Poisson arrivals at %.1f/s (seed %d), meshes n in %s drawn "
+                                  "uniformly, log-normal kappa sigma 0.5, 8-mode Fourier sources, mixed precision "
+                                  "to 1e-10, HBM admission budget %.1f GB" % (
+                                      len(res), args.rate, args.seed + 5, sizes, srv.hbm_budget / 1e9),
+                      "sizes": sizes, "requests": len(res), "rate_per_s": args.rate},
+           "latency": {"p50_s": st["p50_s"], "p99_s": st["p99_s"], "mean_s": st["mean_s"]},
+           "span_s": st["span_s"], "worst_residual_over_tol": worst,
+           "slots": {str(n): len(srv.slots[n]) for n in sizes},
+           "slot_footprint_gb": {str(n): srv.footprint.get(n, 0.0) / 1e9 for n in sizes},
+           "setup_s": t_setup, "clocks": clk}
+    srv.close()
+    print(json.dumps(out))
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.config == "c5":
+        run_serving(a)
     else:
         run_ours(a)

@@ -333,6 +333,20 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
     for (int nt = 0; nt < 2; ++nt)
 #pragma unroll
       for (int i = 0; i < 4; ++i) acc[mt][nt][i] = 0.0f;
+  // the epilogue's b and x values of this thread, loaded with the gather
+  float2 bpre[2][2][2], xpre[2][2][2];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        const int row = mt * 16 + g + 8 * hh;
+        const int64_t o = (e * N + row) * kNR + rbase + nt * 8 + 2 * t;
+        const bool ok = row < N;
+        bpre[mt][hh][nt] = (ok && b) ? *reinterpret_cast<const float2*>(b + o) : make_float2(0.f, 0.f);
+        xpre[mt][hh][nt] = (ok && smooth && !zerox) ? *reinterpret_cast<const float2*>(x + o) : make_float2(0.f, 0.f);
+      }
   if (!zerox) {
     // X_stack rows: slot 24 bb + n = x[nb_bb][n][:] (hi / lo), coalesced
     // float4 reads; all of a thread's loads are issued before the first
@@ -380,8 +394,7 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
       for (int nt = 0; nt < 2; ++nt) {
         const int q = rbase + nt * 8 + 2 * t;
         const int64_t o = (e * N + row) * kNR + q;
-        float2 bv = make_float2(0.f, 0.f);
-        if (b) bv = *reinterpret_cast<const float2*>(b + o);
+        const float2 bv = bpre[mt][hh][nt];
         const float2 res = make_float2(bv.x - acc[mt][nt][2 * hh], bv.y - acc[mt][nt][2 * hh + 1]);
         if (r) *reinterpret_cast<float2*>(r + o) = make_float2(sgn * res.x, sgn * res.y);
         *reinterpret_cast<float2*>(&rs[row][q]) = res;
@@ -424,13 +437,8 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
         for (int nt = 0; nt < 2; ++nt) {
           const int q = rbase + nt * 8 + 2 * t;
           const int64_t o = (e * N + row) * kNR + q;
-          float2 xo = make_float2(c2[mt][nt][2 * hh], c2[mt][nt][2 * hh + 1]);
-          if (!zerox) {
-            const float2 xv = *reinterpret_cast<const float2*>(x + o);
-            xo.x += xv.x;
-            xo.y += xv.y;
-          }
-          *reinterpret_cast<float2*>(x_out + o) = xo;
+          const float2 xv = xpre[mt][hh][nt];
+          *reinterpret_cast<float2*>(x_out + o) = make_float2(c2[mt][nt][2 * hh] + xv.x, c2[mt][nt][2 * hh + 1] + xv.y);
         }
       }
   }

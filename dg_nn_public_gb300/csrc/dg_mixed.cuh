@@ -568,44 +568,39 @@ int launch_bf16_tma(dg_ctx* c, Mixed& M, const float* x, const float* b, float* 
   }
 }
 
-// Gauss-Jordan inverse with partial pivoting (host, FP64); false if singular
-bool invert_dense(std::vector<double>& A, int n, std::vector<double>& inv) {
-  inv.assign((size_t)n * n, 0.0);
-  for (int i = 0; i < n; ++i) inv[(size_t)i * n + i] = 1.0;
-  for (int col = 0; col < n; ++col) {
-    int piv = col;
-    double best = std::fabs(A[(size_t)col * n + col]);
-    for (int r = col + 1; r < n; ++r) {
-      double v = std::fabs(A[(size_t)r * n + col]);
-      if (v > best) { best = v; piv = r; }
-    }
-    if (!(best > 0.0)) return false;
-    if (piv != col)
-      for (int k = 0; k < n; ++k) {
-        std::swap(A[(size_t)piv * n + k], A[(size_t)col * n + k]);
-        std::swap(inv[(size_t)piv * n + k], inv[(size_t)col * n + k]);
-      }
-    const double d = 1.0 / A[(size_t)col * n + col];
-    for (int k = 0; k < n; ++k) {
-      A[(size_t)col * n + k] *= d;
-      inv[(size_t)col * n + k] *= d;
-    }
-    for (int r = 0; r < n; ++r) {
-      if (r == col) continue;
-      const double f = A[(size_t)r * n + col];
-      if (f == 0.0) continue;
-      double* ar = &A[(size_t)r * n];
-      double* ir = &inv[(size_t)r * n];
-      const double* ac = &A[(size_t)col * n];
-      const double* ic = &inv[(size_t)col * n];
-      for (int k = 0; k < n; ++k) {
-        ar[k] -= f * ac[k];
-        ir[k] -= f * ic[k];
-      }
-    }
-  }
-  return true;
+// Gauss-Jordan inversion on the GPU (FP64, no pivoting: the coarse SFC level
+// matrix is a Galerkin product of an SPD operator, so every pivot is
+// positive; a non-positive pivot sets *err = 4).  G is the augmented n x 2n
+// matrix [A | I], row-major; step k eliminates column k from every row.
+// fcol[i] = G[i][k] and prow[j] = G[k][j] / G[k][k] are taken first so that
+// the update reads no element it writes.
+__global__ void gj_prep_kernel(const double* __restrict__ G, int n, int k, double* __restrict__ fcol,
+                               double* __restrict__ prow, int* __restrict__ err) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const double piv = G[(size_t)k * 2 * n + k];
+  if (t == 0 && !(piv > 0.0)) atomicExch(err, 4);
+  if (t < n) fcol[t] = G[(size_t)t * 2 * n + k];
+  const int j = k + t;
+  if (j < 2 * n) prow[j] = G[(size_t)k * 2 * n + j] / piv;
 }
+
+__global__ void gj_update_kernel(double* __restrict__ G, int n, int k, const double* __restrict__ fcol,
+                                 const double* __restrict__ prow) {
+  const int j = k + blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (j >= 2 * n) return;
+  double* row = G + (size_t)i * 2 * n;
+  row[j] = (i == k) ? prow[j] : row[j] - fcol[i] * prow[j];
+}
+
+// inv (n x n FP32) = right half of G
+__global__ void gj_extract_kernel(const double* __restrict__ G, int n, float* __restrict__ inv) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * n) return;
+  const int64_t i = t / n, j = t % n;
+  inv[t] = (float)G[i * 2 * n + n + j];
+}
+
 
 __global__ void zero_f32_kernel(float* __restrict__ a, int64_t n) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -951,7 +946,8 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
       L.col = D.col;
       L.up = D.up;
       int nnz = 0;
-      CK(c, cudaMemcpy(&nnz, D.rowptr + D.n, sizeof(int), cudaMemcpyDeviceToHost));
+      CK(c, cudaMemcpyAsync(&nnz, D.rowptr + D.n, sizeof(int), cudaMemcpyDeviceToHost, st));
+      CK(c, cudaStreamSynchronize(st));
       if ((rc = dalloc(c, &L.val, (size_t)nnz))) return rc;
       for (float** t : {&L.diag, &L.e, &L.e2, &L.r, &L.rr})
         if ((rc = dalloc(c, t, (size_t)L.n))) return rc;
@@ -961,7 +957,8 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
     Lev32& L = M.lev[l];
     const DevLevel& D = c->lev[l];
     int nnz = 0;
-    CK(c, cudaMemcpy(&nnz, D.rowptr + D.n, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(c, cudaMemcpyAsync(&nnz, D.rowptr + D.n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
     convert_f64_f32_kernel<<<nblk(nnz, 256), 256, 0, st>>>(D.val, L.val, nnz);
     bump();
     convert_f64_f32_kernel<<<nblk(D.n, 256), 256, 0, st>>>(D.diag, L.diag, D.n);
@@ -976,19 +973,38 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
       if (h.sizes[l] <= c->dense_max32) { lc = l; break; }
     if (lc >= 0) {
       const int n = (int)h.sizes[lc];
-      std::vector<double> A((size_t)n * n, 0.0), inv;
+      // augmented [A | I] assembled on the host from the level's CSR, inverted on the GPU
+      std::vector<double> Gh((size_t)n * 2 * n, 0.0);
       const int64_t r0 = h.start[lc];
-      for (int i = 0; i < n; ++i)
-        for (int64_t k = h.row_ptr[r0 + i]; k < h.row_ptr[r0 + i + 1]; ++k) A[(size_t)i * n + h.col[k]] += h.val[k];
-      if (invert_dense(A, n, inv)) {
-        std::vector<float> invf(inv.begin(), inv.end());
-        if (!M.dense_inv || c->dense_n != n) {
-          if ((rc = dalloc(c, &M.dense_inv, (size_t)n * n))) return rc;
-          c->dense_n = n;
-        }
-        CK(c, cudaMemcpy(M.dense_inv, invf.data(), sizeof(float) * invf.size(), cudaMemcpyHostToDevice));
-        M.dense_l = lc;
+      for (int i = 0; i < n; ++i) {
+        for (int64_t k = h.row_ptr[r0 + i]; k < h.row_ptr[r0 + i + 1]; ++k) Gh[(size_t)i * 2 * n + h.col[k]] += h.val[k];
+        Gh[(size_t)i * 2 * n + n + i] = 1.0;
       }
+      double *G = nullptr, *fcol = nullptr, *prow = nullptr;
+      CK(c, cudaMalloc((void**)&G, sizeof(double) * Gh.size()));
+      CK(c, cudaMalloc((void**)&fcol, sizeof(double) * n));
+      CK(c, cudaMalloc((void**)&prow, sizeof(double) * 2 * n));
+      CK(c, cudaMemcpyAsync(G, Gh.data(), sizeof(double) * Gh.size(), cudaMemcpyHostToDevice, st));
+      CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
+      for (int k = 0; k < n; ++k) {
+        gj_prep_kernel<<<nblk(2 * n - k > n ? 2 * n - k : n, 256), 256, 0, st>>>(G, n, k, fcol, prow, c->d_err);
+        gj_update_kernel<<<dim3(nblk(2 * n - k, 256), n), 256, 0, st>>>(G, n, k, fcol, prow);
+      }
+      bump(2 * (long long)n);
+      if (!M.dense_inv || c->dense_n != n) {
+        if ((rc = dalloc(c, &M.dense_inv, (size_t)n * n))) return rc;
+        c->dense_n = n;
+      }
+      gj_extract_kernel<<<nblk((int64_t)n * n, 256), 256, 0, st>>>(G, n, M.dense_inv);
+      bump();
+      int herr = 0;
+      CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+      CK(c, cudaStreamSynchronize(st));
+      cudaFree(G);
+      cudaFree(fcol);
+      cudaFree(prow);
+      CKL(c);
+      if (herr == 0) M.dense_l = lc;
     }
   }
   CKL(c);

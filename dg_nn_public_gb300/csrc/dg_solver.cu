@@ -949,11 +949,15 @@ int dg_build_operator(dg_ctx* c, void* stream) {
       }
     }
     rp[L.n] = (int)nnz;
-    CK(c, cudaMemcpy(L.rowptr, rp.data(), sizeof(int) * rp.size(), cudaMemcpyHostToDevice));
-    CK(c, cudaMemcpy(L.col, cl.data(), sizeof(int) * cl.size(), cudaMemcpyHostToDevice));
-    CK(c, cudaMemcpy(L.val, vl.data(), sizeof(double) * vl.size(), cudaMemcpyHostToDevice));
-    CK(c, cudaMemcpy(L.diag, dg.data(), sizeof(double) * dg.size(), cudaMemcpyHostToDevice));
+    // on the context's stream: no legacy-stream copy that would wait for
+    // other streams (several contexts serve concurrently); copies from
+    // pageable memory return once the source has been staged
+    CK(c, cudaMemcpyAsync(L.rowptr, rp.data(), sizeof(int) * rp.size(), cudaMemcpyHostToDevice, st));
+    CK(c, cudaMemcpyAsync(L.col, cl.data(), sizeof(int) * cl.size(), cudaMemcpyHostToDevice, st));
+    CK(c, cudaMemcpyAsync(L.val, vl.data(), sizeof(double) * vl.size(), cudaMemcpyHostToDevice, st));
+    CK(c, cudaMemcpyAsync(L.diag, dg.data(), sizeof(double) * dg.size(), cudaMemcpyHostToDevice, st));
   }
+  CK(c, cudaStreamSynchronize(st));
   return DG_OK;
 }
 
