@@ -205,11 +205,12 @@ def config_block(args, m, extra=None):
 
 # DRAM bytes (read + write) per launch of the roofline kernels on the
 # 20^3 Kuhn-cube workload (48,000 tets), from one ncu capture of
-# dram__bytes_read.sum + dram__bytes_write.sum (per-launch table in
-# profiles/residual_kernel_bf16_smooth_c2.md); other workloads report null.
+# dram__bytes_read.sum + dram__bytes_write.sum (tables in
+# profiles/residual_tma_kernel_c2.md and profiles/residual_kernel_bf16_smooth_c2.md);
+# other workloads report null.
 TRAFFIC_C2 = {
-    "smooth_pc": {"bytes_per_launch": 237.8e6},
-    "apply_f32": {"bytes_per_launch": 384.2e6},
+    "smooth_pc": {"bytes_per_launch": 242.4e6},
+    "apply_f32": {"bytes_per_launch": 392.7e6},
     "apply_f64": {"bytes_per_launch": 768.0e6},
 }
 
@@ -435,13 +436,13 @@ def run_ours(args):
         mb = 2 if s.mixed_options.get("precond_bf16", True) else 4
         nb = (m.nele + s_int) * N * N * mb + m.nele * N * N * mb + 3 * dofs * 4 + m.nele * F * 4
         t = time_launch(lambda: s.smooth_pc(xs, bs, xo))
-        rooflines.append(("smooth_pc", "residual_kernel<20,4,8,__nv_bfloat16,float,float> (preconditioner "
+        rooflines.append(("smooth_pc", "residual_tma_kernel<bf16> (bulk-copy streamed preconditioner "
                           "smoothing step, BF16 blocks + smoother matrices, FP32 vectors)", nb, t,
                           2.0 * N * N * (2 * m.nele + s_int)))
         ya = torch.empty_like(xs)
         nb = (m.nele + s_int) * N * N * 4 + 2 * dofs * 4 + m.nele * F * 4
         t = time_launch(lambda: s.apply_f32(xs, ya))
-        rooflines.append(("apply_f32", "residual_kernel<20,4,8,float,float,float> (stored-block FP32 apply)",
+        rooflines.append(("apply_f32", "residual_tma_kernel<float> (bulk-copy streamed FP32 apply)",
                           nb, t, 2.0 * N * N * (m.nele + s_int)))
         # per inner iteration: preconditioner + apply; the rest is Gram-Schmidt,
         # Hessenberg updates and the refinement steps

@@ -263,8 +263,9 @@ __device__ __forceinline__ void store_split4(unsigned char* hi, unsigned char* l
 // one block (20x20 BF16, chunked) times the slab of k slots kb .. kb+23 of
 // Xs (hi or lo): accumulates into acc[mt][nt], m tiles mt = 0, 1 (rows 0-15,
 // 16-31), n tiles nt = 0, 1 (RHS rbase + 8 nt ..)
-__device__ __forceinline__ void mma_block(float (&acc)[2][2][4], const unsigned char* blk, const unsigned char* Xs,
-                                          int kb, int rbase, int lane) {
+template <int NT>
+__device__ __forceinline__ void mma_block_t(float (&acc)[2][NT][4], const unsigned char* blk, const unsigned char* Xs,
+                                            int kb, int rbase, int lane) {
   const int g = lane >> 2, t = lane & 3;
   uint32_t a[2][4], a8[2][2];
 #pragma unroll
@@ -279,7 +280,7 @@ __device__ __forceinline__ void mma_block(float (&acc)[2][2][4], const unsigned 
     a8[mt][1] = (v1 && t < 2) ? *reinterpret_cast<const uint32_t*>(blk + 2 * kC20Off2 + r1 * 8 + 4 * t) : 0u;
   }
 #pragma unroll
-  for (int nt = 0; nt < 2; ++nt) {
+  for (int nt = 0; nt < NT; ++nt) {
     const int q0 = rbase + nt * 8;
     uint32_t b0, b1, b8;
     // lanes 0-15: rows kb .. kb+15 (two 8x8 matrices); lanes 0-7: rows kb+16 .. kb+23
@@ -291,6 +292,11 @@ __device__ __forceinline__ void mma_block(float (&acc)[2][2][4], const unsigned 
       mma_bf16_1688(acc[mt][nt], a8[mt][0], a8[mt][1], b8);
     }
   }
+}
+
+__device__ __forceinline__ void mma_block(float (&acc)[2][2][4], const unsigned char* blk, const unsigned char* Xs,
+                                          int kb, int rbase, int lane) {
+  mma_block_t<2>(acc, blk, Xs, kb, rbase, lane);
 }
 
 __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __restrict__ blk,
@@ -441,6 +447,213 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
           *reinterpret_cast<float2*>(x_out + o) = make_float2(c2[mt][nt][2 * hh] + xv.x, c2[mt][nt][2 * hh + 1] + xv.y);
         }
       }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent, pipelined form of bres_mma_kernel: kBS CTAs per SM walk the
+// elements e = blockIdx.x, + gridDim.x, ...; an element's operands arrive by
+// bulk copies (cp.async.bulk, mbarrier completion) into a ring of kBStages
+// shared-memory stages -- its BF16 blocks (4,000 B), its smoother matrix
+// (800 B), the x slabs of the element and its face neighbours (5 x 5,120 B)
+// and its b slab (5,120 B) -- so that the copies of the next element are in
+// flight while this one is converted to BF16 hi / lo rows and multiplied on
+// the tensor cores.  Same arithmetic as bres_mma_kernel (same results).
+// Every mbarrier wait is bounded: on time-out *err = 3, the CTA waits
+// (bounded) for its own copies in flight and returns.
+constexpr int kBStages = 2;
+constexpr int kBS = 2;                                   // CTAs per SM
+constexpr int kSlab = 20 * kNR * 4;                      // 5,120 bytes: one element's x (or b) slab
+constexpr int kStOffW = 4000, kStOffX = 4800, kStOffB = 4800 + 5 * kSlab;
+constexpr int kStageB = kStOffB + kSlab;                 // 35,520 bytes
+constexpr int kBDyn = kBStages * kStageB + 2 * kXK * kXRow + 20 * kNR * 4;   // stages + Xhi/Xlo + rs
+
+constexpr int kBT = 256;                                 // threads: 8 warps, warp w owns RHS 8w .. 8w+7
+__global__ void __launch_bounds__(kBT, kBS) bres_mma_tma_kernel(
+    const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
+    const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
+    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err) {
+  constexpr int N = 20, F = 4;
+  extern __shared__ __align__(128) unsigned char bsm[];
+  unsigned char* stages = bsm;
+  unsigned char* Xhi = bsm + kBStages * kStageB;
+  unsigned char* Xlo = Xhi + kXK * kXRow;
+  float(*rs)[kNR] = reinterpret_cast<float(*)[kNR]>(Xlo + kXK * kXRow);
+  __shared__ __align__(8) uint64_t bar[kBStages];
+  __shared__ int nbs[kBStages][F];
+  __shared__ float Ps[N][F];
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, t = lane & 3;
+  const bool zerox = flags & RF_ZEROX;
+  const bool smooth = flags & RF_SMOOTH;
+  const int64_t stride = gridDim.x;
+  for (int i = tid; i < N * F; i += kBT) Ps[i / F][i % F] = (float)P[i];
+  // zero pad slots (nodes 20..23 of every block), never overwritten
+  for (int i = tid; i < (F + 1) * 4 * (kNR / 4); i += kBT) {
+    const int bb = i / (4 * (kNR / 4)), rem = i % (4 * (kNR / 4));
+    const int row = bb * 24 + 20 + rem / (kNR / 4), q4 = rem % (kNR / 4);
+    *reinterpret_cast<uint2*>(Xhi + row * kXRow + q4 * 8) = make_uint2(0u, 0u);
+    *reinterpret_cast<uint2*>(Xlo + row * kXRow + q4 * 8) = make_uint2(0u, 0u);
+  }
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int s2 = 0; s2 < kBStages; ++s2) mbar_init(&bar[s2], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // thread 0 issues the copies of the CTA's k-th element into stage k % kBStages
+  auto issue = [&](int64_t k, int4 nb) {
+    const int64_t e = blockIdx.x + k * stride;
+    if (e >= B) return;
+    const int s2 = (int)(k % kBStages);
+    unsigned char* st = stages + (size_t)s2 * kStageB;
+    nbs[s2][0] = nb.x;
+    nbs[s2][1] = nb.y;
+    nbs[s2][2] = nb.z;
+    nbs[s2][3] = nb.w;
+    const int nbv[F] = {nb.x, nb.y, nb.z, nb.w};
+    uint32_t bytes = 0;
+    if (!zerox) {
+      bytes += 4000 + kSlab;
+      for (int f = 0; f < F; ++f)
+        if (nbv[f] >= 0) bytes += kSlab;
+    }
+    if (smooth) bytes += 800;
+    if (b) bytes += kSlab;
+    mbar_expect_tx(&bar[s2], bytes);
+    if (!zerox) {
+      bulk_copy_g2s(st, blk + e * 2000, 4000, &bar[s2]);
+      bulk_copy_g2s(st + kStOffX, x + e * (int64_t)N * kNR, kSlab, &bar[s2]);
+      for (int f = 0; f < F; ++f)
+        if (nbv[f] >= 0) bulk_copy_g2s(st + kStOffX + (1 + f) * kSlab, x + (int64_t)nbv[f] * N * kNR, kSlab, &bar[s2]);
+    }
+    if (smooth) bulk_copy_g2s(st + kStOffW, W + e * 400, 800, &bar[s2]);
+    if (b) bulk_copy_g2s(st + kStOffB, b + e * (int64_t)N * kNR, kSlab, &bar[s2]);
+  };
+  auto load_nb = [&](int64_t k) {
+    const int64_t e = blockIdx.x + k * stride;
+    return e < B ? reinterpret_cast<const int4*>(nbe)[e] : make_int4(-1, -1, -1, -1);
+  };
+  int4 nb_next = make_int4(-1, -1, -1, -1);
+  if (tid == 0) {
+    for (int k = 0; k < kBStages; ++k) issue(k, load_nb(k));
+    nb_next = load_nb(kBStages);
+  }
+  const int rbase = warp * 8;
+  const float sgn = (flags & RF_NEG) ? -1.0f : 1.0f;
+  int64_t k = 0;
+  for (int64_t e = blockIdx.x; e < B; e += stride, ++k) {
+    const int s2 = (int)(k % kBStages);
+    if (!mbar_wait_bounded(&bar[s2], (uint32_t)((k / kBStages) & 1))) {
+      atomicExch(err, 3);
+      abort_flag = 1;
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    const unsigned char* st = stages + (size_t)s2 * kStageB;
+    const float* xst = reinterpret_cast<const float*>(st + kStOffX);   // [5][20][kNR]
+    const float* bst = reinterpret_cast<const float*>(st + kStOffB);   // [20][kNR]
+    float acc[2][1][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int nt = 0; nt < 1; ++nt)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) acc[mt][nt][i] = 0.0f;
+    if (!zerox) {
+      for (int i = tid; i < (F + 1) * N * (kNR / 4); i += kBT) {
+        const int bb = i / (N * (kNR / 4)), rem = i % (N * (kNR / 4));
+        if (bb > 0 && nbs[s2][bb - 1] < 0) continue;
+        const int n = rem / (kNR / 4), q4 = rem % (kNR / 4);
+        const int row = bb * 24 + n;
+        store_split4(Xhi + row * kXRow + q4 * 8, Xlo + row * kXRow + q4 * 8,
+                     reinterpret_cast<const float4*>(xst)[i]);
+      }
+      __syncthreads();
+#pragma unroll 1
+      for (int bb = 0; bb <= F; ++bb) {
+        if (bb > 0 && nbs[s2][bb - 1] < 0) continue;
+        mma_block_t<1>(acc, st + bb * 800, Xhi, bb * 24, rbase, lane);
+        mma_block_t<1>(acc, st + bb * 800, Xlo, bb * 24, rbase, lane);
+      }
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int row = mt * 16 + g + 8 * hh;
+        if (row >= N) continue;
+#pragma unroll
+        for (int nt = 0; nt < 1; ++nt) {
+          const int q = rbase + nt * 8 + 2 * t;
+          const int64_t o = (e * N + row) * kNR + q;
+          const float2 bv = b ? *reinterpret_cast<const float2*>(bst + row * kNR + q) : make_float2(0.f, 0.f);
+          const float2 res = make_float2(bv.x - acc[mt][nt][2 * hh], bv.y - acc[mt][nt][2 * hh + 1]);
+          if (r) *reinterpret_cast<float2*>(r + o) = make_float2(sgn * res.x, sgn * res.y);
+          *reinterpret_cast<float2*>(&rs[row][q]) = res;
+        }
+      }
+    if (flags & (RF_RESTRICT | RF_SMOOTH)) {
+      __syncthreads();   // rs complete; Xhi / Xlo no longer read by the MMAs
+      if (flags & RF_RESTRICT) {
+        for (int o = tid; o < F * kNR; o += kBT) {
+          const int cc = o / kNR, q = o % kNR;
+          float sum = 0.0f;
+#pragma unroll
+          for (int n = 0; n < N; ++n) sum += Ps[n][cc] * rs[n][q];
+          r1[(e * F + cc) * kNR + q] = sum;
+        }
+      }
+      if (smooth) {
+        for (int i = tid; i < N * (kNR / 4); i += kBT) {
+          const int n = i / (kNR / 4), q4 = i % (kNR / 4);
+          store_split4(Xhi + n * kXRow + q4 * 8, Xlo + n * kXRow + q4 * 8,
+                       reinterpret_cast<const float4*>(&rs[n][0])[q4]);
+        }
+        __syncthreads();
+        float c2[2][1][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+          for (int nt = 0; nt < 1; ++nt)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) c2[mt][nt][i] = 0.0f;
+        mma_block_t<1>(c2, st + kStOffW, Xhi, 0, rbase, lane);
+        mma_block_t<1>(c2, st + kStOffW, Xlo, 0, rbase, lane);
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+          for (int hh = 0; hh < 2; ++hh) {
+            const int row = mt * 16 + g + 8 * hh;
+            if (row >= N) continue;
+#pragma unroll
+            for (int nt = 0; nt < 1; ++nt) {
+              const int q = rbase + nt * 8 + 2 * t;
+              const int64_t o = (e * N + row) * kNR + q;
+              float2 xo = make_float2(c2[mt][nt][2 * hh], c2[mt][nt][2 * hh + 1]);
+              if (!zerox) {
+                const float2 xv = *reinterpret_cast<const float2*>(xst + row * kNR + q);
+                xo.x += xv.x;
+                xo.y += xv.y;
+              }
+              *reinterpret_cast<float2*>(x_out + o) = xo;
+            }
+          }
+      }
+    }
+    __syncthreads();   // stage s2, Xhi / Xlo and rs free again
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(k + kBStages, nb_next);
+      nb_next = load_nb(k + kBStages + 1);
+    }
+  }
+  if (abort_flag && tid == 0) {
+    for (int64_t j = k; j < k + kBStages; ++j) {
+      if (blockIdx.x + j * stride >= B) break;
+      (void)mbar_wait_bounded(&bar[j % kBStages], (uint32_t)((j / kBStages) & 1));
+    }
   }
 }
 
@@ -855,6 +1068,15 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   float* other = S.t4;
   const bool bf = c->precond_bf16;
   auto pc = [&](const float* xx, float* xo, int flags, float* rr1) -> int {
+    if (bf && c->batched_mma && c->batched_tma) {
+      const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kBS);
+      if (g)
+        bres_mma_tma_kernel<<<g, kBT, kBDyn, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B, flags, c->T.P,
+                                                   rr1, c->d_err);
+      bump();
+      CKL(c);
+      return (int)DG_OK;
+    }
     if (bf && c->batched_mma) {
       if (c->B > 0)
         bres_mma_kernel<<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B, flags,
@@ -959,6 +1181,8 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
   if (M.dense_l < 0) return fail(c, DG_ERR_STATE, "dg_solve_mixed_batched: needs the dense coarse level");
   if (!c->f32_tma) return fail(c, DG_ERR_STATE, "dg_solve_mixed_batched: needs the chunked FP32 block layout");
   if ((rc = ensure_batch(c, m))) return rc;
+  CK(c, cudaFuncSetAttribute(bres_mma_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBDyn));
+  CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));   // bulk-copy wait time-outs land here
   BatchState& S = batch_of(M);
   const int64_t n = c->nonods;
   const int64_t ld = n * kNR;
@@ -1077,6 +1301,15 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
     bump();
     CKL(c);
     if ((rc = outer_residuals())) return rc;
+  }
+  {
+    int herr = 0;
+    CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    if (herr == 3) {
+      c->err = "batched solve: a bulk-copy wait of the preconditioner timed out";
+      return DG_ERR_CUDA;
+    }
   }
   bool all_conv = true;
   for (int q = 0; q < nrhs; ++q) {

@@ -559,6 +559,8 @@ int set_tma_smem(dg_ctx* c) {
 // (8,3,1) 49.2, (8,2,2) 41.2, (4,2,4) 41.3, (4,2,5) 41.6, (4,1,8) 41.5,
 // (6,2,3) 40.7 -- several CTAs per SM hide the per-group round trip that
 // one CTA per SM cannot.
+constexpr int kTmaVariants = 3;
+
 int launch_bf16_tma(dg_ctx* c, Mixed& M, const float* x, const float* b, float* r, float* x_out, int flags,
                     cudaStream_t st) {
   switch (c->tma_variant) {
@@ -1305,6 +1307,56 @@ double hessenberg_ls(const std::vector<double>& Hcm, int m, int k, double beta, 
   return std::fabs(g[k]);
 }
 
+// Launch-shape autotuner for the single-RHS bulk-copy kernels: times every
+// candidate shape (elements per group, stages, CTAs per SM) of the BF16
+// smoothing step on zeroed scratch vectors with CUDA events (one warm launch,
+// then 5 timed) and keeps the fastest.  Runs once per operator build before
+// any graph capture; cached graphs are dropped when the choice changes.
+int autotune_mixed(dg_ctx* c, cudaStream_t st) {
+  if (!c->autotune || c->D != 3 || !c->precond_bf16 || !c->bf16_tma) return DG_OK;
+  Mixed& M = mixed_of(c);
+  const int64_t n = c->nonods;
+  CK(c, cudaMemsetAsync(M.t2, 0, sizeof(float) * n, st));
+  CK(c, cudaMemsetAsync(M.t3, 0, sizeof(float) * n, st));
+  cudaEvent_t e0, e1;
+  CK(c, cudaEventCreate(&e0));
+  CK(c, cudaEventCreate(&e1));
+  const int before = c->tma_variant;
+  float best = 1e30f;
+  int bestv = 0;
+  for (int v = 0; v < kTmaVariants; ++v) {
+    c->tma_variant = v;
+    int rc = launch_bf16_tma(c, M, M.t3, M.t2, nullptr, M.t4, RF_SMOOTH, st);
+    if (!rc) CK(c, cudaEventRecord(e0, st));
+    for (int it = 0; it < 5 && !rc; ++it) rc = launch_bf16_tma(c, M, M.t3, M.t2, nullptr, M.t4, RF_SMOOTH, st);
+    if (rc) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return rc;
+    }
+    CK(c, cudaEventRecord(e1, st));
+    CK(c, cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    CK(c, cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) {
+      best = ms;
+      bestv = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->tma_variant = bestv;
+  if (bestv != before) {
+    for (auto& g : M.graphs)
+      if (g) cudaGraphExecDestroy(g);
+    M.graphs.clear();
+    M.g_m = 0;
+  }
+  if (c->verbose)
+    std::fprintf(stderr, "[autotune] bulk-copy smoothing shape %d (%.1f us per launch)\n", bestv, best * 1e3f / 5.0f);
+  return DG_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1322,6 +1374,7 @@ extern "C" int dg_solve_mixed(dg_ctx* c, double* x, const double* b, double tol,
   if (!M.built || c->mixed_version != c->build_version) {
     if ((rc = build_mixed(c, st))) return rc;
     c->mixed_version = c->build_version;
+    if ((rc = autotune_mixed(c, st))) return rc;
   }
   if ((rc = ensure_krylov32(c, m))) return rc;
   CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));   // bulk-copy wait time-outs land here

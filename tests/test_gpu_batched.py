@@ -74,3 +74,24 @@ def test_batched_nonzero_guess_and_converged_rhs():
     its, res = s.solve_mixed_batched(X, Bm, tol, raise_noconv=True)
     assert its[1] == 0 and torch.equal(X[1], X1_before)
     assert its[0] > 0 and its[2] > 0 and (res <= tol).all()
+
+
+def test_bulk_copy_smoothing_matches_per_element_kernel(monkeypatch):
+    """The persistent bulk-copy form of the batched tensor-core smoothing
+    kernel does the same arithmetic as the one-CTA-per-element form: the whole
+    batched solve is bitwise identical with either."""
+    out = {}
+    for tma in ("1", "0"):
+        monkeypatch.setenv("DG_BATCHED_TMA", tma)
+        m = mesh.build_mesh("tet", 5, seed=2)
+        s = DGSolver(m, sfc.hilbert_sfc_order(m.cg_coords), SolverConfig(pre_smooth_its=2, post_smooth_its=2),
+                     element.p3_element(3))
+        s.build_operator()
+        F = _modes(m, 6, seed=3)
+        Bm = torch.stack([s.rhs(torch.tensor(F[q], device="cuda:0")) for q in range(6)]).contiguous()
+        tol = 1e-10 * torch.linalg.norm(Bm, dim=1).cpu().numpy()
+        X = torch.zeros_like(Bm)
+        its, res = s.solve_mixed_batched(X, Bm, tol, raise_noconv=True)
+        out[tma] = (X, its)
+    assert torch.equal(out["1"][0], out["0"][0])
+    assert (out["1"][1] == out["0"][1]).all()
