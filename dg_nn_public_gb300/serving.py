@@ -138,6 +138,16 @@ class SolveServer:
             return slot
         return None
 
+    def prewarm(self, slots_per_size: Dict[int, int]):
+        """Create slots ahead of traffic (as a deployment would), within the
+        HBM budget: ``slots_per_size[n]`` slots for mesh size n."""
+        for n, k in slots_per_size.items():
+            while len(self.slots[n]) < min(k, self.max_slots):
+                need = self.footprint.get(n)
+                if need is not None and self.used + need > self.hbm_budget and self.slots[n]:
+                    break
+                self._new_slot(n)
+
     # -- one request ------------------------------------------------------
     def solve_one(self, slot: _Slot, req: Request):
         """Rebuild the slot's operator for the request's kappa and solve."""
