@@ -800,19 +800,31 @@ __global__ void __launch_bounds__(256) bmdot_kernel(const float* __restrict__ V,
   float4 acc[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int64_t row = (int64_t)blockIdx.x * 16 + lane; row < n; row += (int64_t)gridDim.x * 16) {
+  const int64_t step = (int64_t)gridDim.x * 16;
+  for (int64_t row = (int64_t)blockIdx.x * 16 + lane; row < n; row += 2 * step) {
+    // two rows per iteration: 18 loads in flight per thread
+    const int64_t row2 = row + step;
+    const bool has2 = row2 < n;
     const float4 zv = reinterpret_cast<const float4*>(z + row * kNR)[q4];
-    float4 v[8];
+    const float4 zv2 = has2 ? reinterpret_cast<const float4*>(z + row2 * kNR)[q4] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 v[8], v2[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
+    for (int j = 0; j < 8; ++j) {
       v[j] = j < cnt ? reinterpret_cast<const float4*>(V + (size_t)(j0 + j) * ld + row * kNR)[q4]
                      : make_float4(0.f, 0.f, 0.f, 0.f);
+      v2[j] = (j < cnt && has2) ? reinterpret_cast<const float4*>(V + (size_t)(j0 + j) * ld + row2 * kNR)[q4]
+                                : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       acc[j].x = fmaf(v[j].x, zv.x, acc[j].x);
       acc[j].y = fmaf(v[j].y, zv.y, acc[j].y);
       acc[j].z = fmaf(v[j].z, zv.z, acc[j].z);
       acc[j].w = fmaf(v[j].w, zv.w, acc[j].w);
+      acc[j].x = fmaf(v2[j].x, zv2.x, acc[j].x);
+      acc[j].y = fmaf(v2[j].y, zv2.y, acc[j].y);
+      acc[j].z = fmaf(v2[j].z, zv2.z, acc[j].z);
+      acc[j].w = fmaf(v2[j].w, zv2.w, acc[j].w);
     }
   }
 #pragma unroll
@@ -850,20 +862,19 @@ __global__ void __launch_bounds__(256) baxpy_kernel(const float* __restrict__ V,
   for (int64_t row = (int64_t)blockIdx.x * 16 + lane; row < n; row += (int64_t)gridDim.x * 16) {
     float4* zp = reinterpret_cast<float4*>(z + row * kNR) + q4;
     float4 zv = *zp;
-    for (int j0 = 0; j0 < nv; j0 += 8) {
-      float4 v[8];
+    // all (up to 32) basis loads of the row are issued before the first use
+    float4 v[32];
 #pragma unroll
-      for (int j = 0; j < 8; ++j)
-        v[j] = j0 + j < nv ? reinterpret_cast<const float4*>(V + (size_t)(j0 + j) * ld + row * kNR)[q4]
-                           : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int j = 0; j < 32; ++j)
+      v[j] = j < nv ? reinterpret_cast<const float4*>(V + (size_t)j * ld + row * kNR)[q4]
+                    : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const float4 hv = hs[(j0 + j) & 31][q4];
-        zv.x -= v[j].x * hv.x;
-        zv.y -= v[j].y * hv.y;
-        zv.z -= v[j].z * hv.z;
-        zv.w -= v[j].w * hv.w;
-      }
+    for (int j = 0; j < 32; ++j) {
+      const float4 hv = hs[j][q4];
+      zv.x -= v[j].x * hv.x;
+      zv.y -= v[j].y * hv.y;
+      zv.z -= v[j].z * hv.z;
+      zv.w -= v[j].w * hv.w;
     }
     *zp = zv;
     acc.x = fmaf(zv.x, zv.x, acc.x);
