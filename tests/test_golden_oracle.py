@@ -142,3 +142,30 @@ def test_face_kappa_coercivity_under_a_kappa_jump():
             xAy, yAx = x @ O.apply_Ax(y).reshape(-1), y @ O.apply_Ax(x).reshape(-1)
             assert abs(xAy - yAx) <= 1e-12 * abs(xAy)
     assert lo["mean"] < 0 < 0.05 < lo["harmonic"], lo
+
+
+def test_vtk_node_order_matches_reference_tables():
+    """The VTK permutation derived from the barycentric node tables equals
+    the reference's hand-written tables (fixture extracted from its source)."""
+    import os
+    from dg_nn_public_gb300.output import vtk_node_order
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "vtk_node_order.npz"))
+    assert (vtk_node_order(3) == d["tet"]).all()
+    assert (vtk_node_order(2) == d["tri"]).all()
+
+
+def test_write_vtu_roundtrip(tmp_path):
+    """The VTU lists every DG node once, cells in VTK order, and the field."""
+    import xml.etree.ElementTree as ET
+    from dg_nn_public_gb300 import mesh
+    from dg_nn_public_gb300.output import write_vtu, vtk_node_order
+    m = mesh.build_mesh("tet", 2, seed=0)
+    u = np.arange(m.nele * m.nloc, dtype=np.float64)
+    p = write_vtu(str(tmp_path / "u.vtu"), m.x_ref_in, {"u": u})
+    root = ET.parse(p).getroot()
+    piece = root.find("UnstructuredGrid/Piece")
+    assert int(piece.get("NumberOfPoints")) == m.nele * 20 and int(piece.get("NumberOfCells")) == m.nele
+    conn = np.array(piece.find("Cells/DataArray[@Name='connectivity']").text.split(), dtype=np.int64)
+    assert (conn.reshape(m.nele, 20)[1] == 20 + vtk_node_order(3)).all()
+    vals = np.array(piece.find("PointData/DataArray[@Name='u']").text.split(), dtype=np.float64)
+    assert np.array_equal(vals, u)
