@@ -95,7 +95,7 @@ struct dg_ctx {
   int tail_max64 = 320, tail_max32 = 800;
   // mixed preconditioner: exact (dense inverse) solve on the first SFC level
   // with at most this many rows (0 = keep the V-cycle to the one-node level)
-  int dense_max32 = 1200;
+  int dense_max32 = 2400;
   int dense_n = 0;
   // mixed preconditioner reads BF16 copies of the blocks / smoother matrices
   bool precond_bf16 = true;

@@ -309,7 +309,7 @@ class DGSolver:
         self._chk(rc)
         return its, res
 
-    def set_mixed_options(self, smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=1200):
+    def set_mixed_options(self, smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=2400):
         """Mixed preconditioner: smoother 'jacobi3' (three point-Jacobi sweeps,
         as the reference) or 'blockinv' (smooth_w * A_ee^-1); BF16 block copies
         for the preconditioner; exact dense solve on the first SFC level with
@@ -326,7 +326,7 @@ class DGSolver:
         self._chk(self._lib.dg_set_launch_options(self._ctx, 1 if use_graph else 0, 1 if use_pdl else 0))
 
     # library defaults of the mixed preconditioner (dg_create)
-    mixed_options = dict(smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=1200)
+    mixed_options = dict(smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=2400)
 
     def solve_mixed(self, x, b, tol, m=None, max_its=None, inner_rtol=1e-3, raise_noconv=False):
         """FP64 iterative refinement around an FP32 right-preconditioned
