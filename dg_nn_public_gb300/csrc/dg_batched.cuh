@@ -299,7 +299,8 @@ __device__ __forceinline__ void mma_block(float (&acc)[2][2][4], const unsigned 
   mma_block_t<2>(acc, blk, Xs, kb, rbase, lane);
 }
 
-__global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __restrict__ blk,
+template <int NWARP>
+__global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat16* __restrict__ blk,
                                                        const __nv_bfloat16* __restrict__ W,
                                                        const int* __restrict__ nbe, const float* __restrict__ x,
                                                        const float* __restrict__ b, float* __restrict__ r,
@@ -319,34 +320,35 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
   const bool smooth = flags & RF_SMOOTH;
   if (tid < F) nbs[tid] = nbe[e * F + tid];
   if (!zerox)
-    for (int i = tid; i < (F + 1) * 800 / 16; i += 128)
+    for (int i = tid; i < (F + 1) * 800 / 16; i += NWARP * 32)
       reinterpret_cast<uint4*>(As)[i] = reinterpret_cast<const uint4*>(blk + e * 2000)[i];
   if (smooth)
-    for (int i = tid; i < 800 / 16; i += 128) reinterpret_cast<uint4*>(Ws)[i] = reinterpret_cast<const uint4*>(W + e * 400)[i];
+    for (int i = tid; i < 800 / 16; i += NWARP * 32) reinterpret_cast<uint4*>(Ws)[i] = reinterpret_cast<const uint4*>(W + e * 400)[i];
   // zero pad slots (nodes 20..23 of every block): 5 x 4 rows x 64 RHS, hi and lo
-  for (int i = tid; i < (F + 1) * 4 * (kNR / 4); i += 128) {
+  for (int i = tid; i < (F + 1) * 4 * (kNR / 4); i += NWARP * 32) {
     const int bb = i / (4 * (kNR / 4)), rem = i % (4 * (kNR / 4));
     const int row = bb * 24 + 20 + rem / (kNR / 4), q4 = rem % (kNR / 4);
     *reinterpret_cast<uint2*>(Xhi + row * kXRow + q4 * 8) = make_uint2(0u, 0u);
     *reinterpret_cast<uint2*>(Xlo + row * kXRow + q4 * 8) = make_uint2(0u, 0u);
   }
   __syncthreads();
-  const int rbase = warp * 16;
-  float acc[2][2][4];
+  constexpr int NT = 8 / NWARP;                            // n8 tiles per warp
+  const int rbase = warp * 8 * NT;
+  float acc[2][NT][4];
 #pragma unroll
   for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt)
+    for (int nt = 0; nt < NT; ++nt)
 #pragma unroll
       for (int i = 0; i < 4; ++i) acc[mt][nt][i] = 0.0f;
   // the epilogue's b and x values of this thread, loaded with the gather
-  float2 bpre[2][2][2], xpre[2][2][2];
+  float2 bpre[2][2][NT], xpre[2][2][NT];
 #pragma unroll
   for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
     for (int hh = 0; hh < 2; ++hh)
 #pragma unroll
-      for (int nt = 0; nt < 2; ++nt) {
+      for (int nt = 0; nt < NT; ++nt) {
         const int row = mt * 16 + g + 8 * hh;
         const int64_t o = (e * N + row) * kNR + rbase + nt * 8 + 2 * t;
         const bool ok = row < N;
@@ -358,11 +360,11 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
     // float4 reads; all of a thread's loads are issued before the first
     // conversion, so the gather costs one round trip, not thirteen
     constexpr int kItems = (F + 1) * N * (kNR / 4);          // 1600 float4
-    constexpr int kPer = (kItems + 127) / 128;               // 13 per thread
+    constexpr int kPer = (kItems + NWARP * 32 - 1) / (NWARP * 32);
     float4 v[kPer];
 #pragma unroll
     for (int u = 0; u < kPer; ++u) {
-      const int i = tid + u * 128;
+      const int i = tid + u * NWARP * 32;
       v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (i < kItems) {
         const int bb = i / (N * (kNR / 4)), rem = i % (N * (kNR / 4));
@@ -372,7 +374,7 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
     }
 #pragma unroll
     for (int u = 0; u < kPer; ++u) {
-      const int i = tid + u * 128;
+      const int i = tid + u * NWARP * 32;
       if (i < kItems) {
         const int bb = i / (N * (kNR / 4)), rem = i % (N * (kNR / 4));
         const int n = rem / (kNR / 4), q4 = rem % (kNR / 4);
@@ -384,8 +386,8 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
 #pragma unroll 1
     for (int bb = 0; bb <= F; ++bb) {
       if (bb > 0 && nbs[bb - 1] < 0) continue;
-      mma_block(acc, As + bb * 800, Xhi, bb * 24, rbase, lane);
-      mma_block(acc, As + bb * 800, Xlo, bb * 24, rbase, lane);
+      mma_block_t<NT>(acc, As + bb * 800, Xhi, bb * 24, rbase, lane);
+      mma_block_t<NT>(acc, As + bb * 800, Xlo, bb * 24, rbase, lane);
     }
   }
   // epilogue: rows (mt*16 + g [+8]), RHS rbase + nt*8 + 2t (+1)
@@ -397,7 +399,7 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
       const int row = mt * 16 + g + 8 * hh;
       if (row >= N) continue;
 #pragma unroll
-      for (int nt = 0; nt < 2; ++nt) {
+      for (int nt = 0; nt < NT; ++nt) {
         const int q = rbase + nt * 8 + 2 * t;
         const int64_t o = (e * N + row) * kNR + q;
         const float2 bv = bpre[mt][hh][nt];
@@ -409,7 +411,7 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
   if (!(flags & (RF_RESTRICT | RF_SMOOTH))) return;
   __syncthreads();
   if (flags & RF_RESTRICT) {
-    for (int o = tid; o < F * kNR; o += 128) {
+    for (int o = tid; o < F * kNR; o += NWARP * 32) {
       const int cc = o / kNR, q = o % kNR;
       float s = 0.0f;
 #pragma unroll
@@ -419,20 +421,20 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
   }
   if (smooth) {
     // res rows into slots 0..19 (slots 20..23 are still zero)
-    for (int i = tid; i < N * (kNR / 4); i += 128) {
+    for (int i = tid; i < N * (kNR / 4); i += NWARP * 32) {
       const int n = i / (kNR / 4), q4 = i % (kNR / 4);
       store_split4(Xhi + n * kXRow + q4 * 8, Xlo + n * kXRow + q4 * 8, reinterpret_cast<const float4*>(&rs[n][0])[q4]);
     }
     __syncthreads();
-    float c2[2][2][4];
+    float c2[2][NT][4];
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-      for (int nt = 0; nt < 2; ++nt)
+      for (int nt = 0; nt < NT; ++nt)
 #pragma unroll
         for (int i = 0; i < 4; ++i) c2[mt][nt][i] = 0.0f;
-    mma_block(c2, Ws, Xhi, 0, rbase, lane);
-    mma_block(c2, Ws, Xlo, 0, rbase, lane);
+    mma_block_t<NT>(c2, Ws, Xhi, 0, rbase, lane);
+    mma_block_t<NT>(c2, Ws, Xlo, 0, rbase, lane);
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
@@ -440,7 +442,7 @@ __global__ void __launch_bounds__(128) bres_mma_kernel(const __nv_bfloat16* __re
         const int row = mt * 16 + g + 8 * hh;
         if (row >= N) continue;
 #pragma unroll
-        for (int nt = 0; nt < 2; ++nt) {
+        for (int nt = 0; nt < NT; ++nt) {
           const int q = rbase + nt * 8 + 2 * t;
           const int64_t o = (e * N + row) * kNR + q;
           const float2 xv = xpre[mt][hh][nt];
@@ -1089,9 +1091,14 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
       return (int)DG_OK;
     }
     if (bf && c->batched_mma) {
-      if (c->B > 0)
-        bres_mma_kernel<<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B, flags,
-                                                        c->T.P, rr1);
+      if (c->B > 0) {
+        if (c->batched_warps == 8)
+          bres_mma_kernel<8><<<(unsigned)c->B, 256, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B,
+                                                             flags, c->T.P, rr1);
+        else
+          bres_mma_kernel<4><<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B,
+                                                             flags, c->T.P, rr1);
+      }
       bump();
       CKL(c);
       return (int)DG_OK;

@@ -113,6 +113,7 @@ struct dg_ctx {
   // solves vs 0.57 s for one CTA per element, whose 5 CTAs per SM hide more
   // of the per-element latency; kept as a tuning option)
   bool batched_tma = false;
+  int batched_warps = 4;   // warps per CTA of the per-element batched smoothing kernel (4 or 8)
   int tma_variant = 0;   // elements per group / stages / CTAs per SM of that kernel
   bool autotune = true;  // pick tma_variant by timing at the first mixed solve after a build
   bool verbose = false;
@@ -696,6 +697,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (ft && ft[0]) c->f32_tma = ft[0] != '0';
     const char* bt2 = std::getenv("DG_BATCHED_TMA");
     if (bt2 && bt2[0]) c->batched_tma = bt2[0] != '0';
+    const char* bw = std::getenv("DG_BATCHED_WARPS");
+    if (bw && bw[0]) c->batched_warps = std::atoi(bw) == 8 ? 8 : 4;
     const char* bm = std::getenv("DG_BATCHED_MMA");
     if (bm && bm[0]) c->batched_mma = bm[0] != '0';
     const char* pd = std::getenv("DG_PDL");

@@ -76,13 +76,18 @@ def test_batched_nonzero_guess_and_converged_rhs():
     assert its[0] > 0 and its[2] > 0 and (res <= tol).all()
 
 
-def test_bulk_copy_smoothing_matches_per_element_kernel(monkeypatch):
-    """The persistent bulk-copy form of the batched tensor-core smoothing
-    kernel does the same arithmetic as the one-CTA-per-element form: the whole
-    batched solve is bitwise identical with either."""
+@pytest.mark.parametrize("variant", [("DG_BATCHED_TMA", "1"), ("DG_BATCHED_WARPS", "8")])
+def test_smoothing_kernel_forms_agree(monkeypatch, variant):
+    """The persistent bulk-copy form and the 8-warp form of the batched
+    tensor-core smoothing kernel do the same arithmetic as the default
+    (one CTA of 4 warps per element): the whole batched solve is bitwise
+    identical with any of them."""
     out = {}
     for tma in ("1", "0"):
-        monkeypatch.setenv("DG_BATCHED_TMA", tma)
+        if tma == "1":
+            monkeypatch.setenv(*variant)
+        else:
+            monkeypatch.delenv(variant[0], raising=False)
         m = mesh.build_mesh("tet", 5, seed=2)
         s = DGSolver(m, sfc.hilbert_sfc_order(m.cg_coords), SolverConfig(pre_smooth_its=2, post_smooth_its=2),
                      element.p3_element(3))
