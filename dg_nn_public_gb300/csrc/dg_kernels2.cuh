@@ -208,12 +208,32 @@ __global__ void lev_jacobi_kernel(const int* __restrict__ rowptr, const int* __r
                                   const T* __restrict__ e_in, const T* __restrict__ b,
                                   T* __restrict__ e_out, T* __restrict__ rr_out, int n,
                                   double w) {
-  pdl_wait_then_trigger();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / LPR, lane = t % LPR;
+  // the level matrix is fixed data: the first four entries of this lane are
+  // read before the programmatic-launch wait, overlapping the previous kernel
+  constexpr int PRE = 4;
+  int k0 = 0, k1 = 0;
+  int cpre[PRE];
+  T vpre[PRE];
+  if (i < n) {
+    k0 = rowptr[i] + lane;
+    k1 = rowptr[i + 1];
+  }
+#pragma unroll
+  for (int q = 0; q < PRE; ++q) {
+    const int k = k0 + q * LPR;
+    cpre[q] = k < k1 ? col[k] : 0;
+    vpre[q] = k < k1 ? val[k] : (T)0;
+  }
+  pdl_wait_then_trigger();
   T s = 0;
-  if (i < n && e_in)
-    for (int k = rowptr[i] + lane; k < rowptr[i + 1]; k += LPR) s += val[k] * e_in[col[k]];
+  if (i < n && e_in) {
+#pragma unroll
+    for (int q = 0; q < PRE; ++q)
+      if (k0 + q * LPR < k1) s += vpre[q] * e_in[cpre[q]];
+    for (int k = k0 + PRE * LPR; k < k1; k += LPR) s += val[k] * e_in[col[k]];
+  }
 #pragma unroll
   for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
   if (i >= n || lane != 0) return;

@@ -110,16 +110,63 @@ int launch_k2(dg_ctx* c, void (*kern)(KArgs...), dim3 grid, unsigned block, size
   return DG_OK;
 }
 
-// e = Ainv r for a small dense level matrix: one warp per row
+// e = Ainv r for a small dense level matrix: one warp per row.  The row of
+// the fixed inverse is read into registers (float4, up to 20 per lane, i.e.
+// n <= 2560 without a second pass) before the programmatic-launch wait, so
+// the 21.5 MB read overlaps the previous kernel; r is read after the wait.
 __global__ void dense_matvec_kernel(const float* __restrict__ Ainv, const float* __restrict__ r,
                                     float* __restrict__ e, int n) {
-  pdl_wait_then_trigger();
+  constexpr int PRE = 20;
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
+  const bool vec = (n & 3) == 0;   // rows 16-byte aligned
+  const int n4 = vec ? n / 4 : 0;
+  const float* ar = Ainv + (size_t)(row < n ? row : 0) * n;
+  float4 a[PRE];
+  if (vec) {
+#pragma unroll
+    for (int q = 0; q < PRE; ++q) {
+      const int k4 = lane + 32 * q;
+      a[q] = (row < n && k4 < n4) ? reinterpret_cast<const float4*>(ar)[k4] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  } else {
+    // scalar loads of columns lane + 32 q, packed four to a register quad
+#pragma unroll
+    for (int q = 0; q < PRE; ++q) {
+      const int k = lane + 128 * q;
+      a[q].x = (row < n && k < n) ? ar[k] : 0.0f;
+      a[q].y = (row < n && k + 32 < n) ? ar[k + 32] : 0.0f;
+      a[q].z = (row < n && k + 64 < n) ? ar[k + 64] : 0.0f;
+      a[q].w = (row < n && k + 96 < n) ? ar[k + 96] : 0.0f;
+    }
+  }
+  pdl_wait_then_trigger();
   if (row >= n) return;
-  const float* a = Ainv + (size_t)row * n;
   float s = 0.0f;
-  for (int k = lane; k < n; k += 32) s += a[k] * r[k];
+  if (vec) {
+#pragma unroll
+    for (int q = 0; q < PRE; ++q) {
+      const int k4 = lane + 32 * q;
+      if (k4 < n4) {
+        const float4 rv = reinterpret_cast<const float4*>(r)[k4];
+        s += a[q].x * rv.x + a[q].y * rv.y + a[q].z * rv.z + a[q].w * rv.w;
+      }
+    }
+    for (int k4 = lane + 32 * PRE; k4 < n4; k4 += 32) {
+      const float4 av = reinterpret_cast<const float4*>(ar)[k4], rv = reinterpret_cast<const float4*>(r)[k4];
+      s += av.x * rv.x + av.y * rv.y + av.z * rv.z + av.w * rv.w;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < PRE; ++q) {
+      const int k = lane + 128 * q;
+      if (k < n) s += a[q].x * r[k];
+      if (k + 32 < n) s += a[q].y * r[k + 32];
+      if (k + 64 < n) s += a[q].z * r[k + 64];
+      if (k + 96 < n) s += a[q].w * r[k + 96];
+    }
+    for (int k = lane + 128 * PRE; k < n; k += 32) s += ar[k] * r[k];
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if (lane == 0) e[row] = s;
@@ -691,6 +738,63 @@ int residual_pc(dg_ctx* c, const float* x, const float* b, float* r, float* x_ou
   return residual32(c, x, b, r, x_out, flags, st);
 }
 
+// P1 -> P3 prolongation of the coarse correction (mixed path, 3D):
+// x[e][n] += sum_c P[n][c] (w_ec ecg[pos(p1cg[e][c])]).  8 elements per CTA;
+// the 4 corner values of an element are formed once (threads m < 4) instead
+// of by each of its 20 node threads.  Same products and summation order as
+// prolong_cg_kernel.  The corner indices are fixed data, read before the
+// programmatic-launch wait.
+__global__ void __launch_bounds__(160) prolong_cg32_kernel(float* __restrict__ x, const float* __restrict__ ecg,
+                                                           const int* __restrict__ pos, const int* __restrict__ p1cg,
+                                                           const double* __restrict__ wdg,
+                                                           const double* __restrict__ P, int64_t B) {
+  __shared__ float vc[8][4];
+  const int le = threadIdx.x / 20, n = threadIdx.x % 20;
+  const int64_t e = (int64_t)blockIdx.x * 8 + le;
+  const bool valid = e < B;
+  int vp = 0;
+  float w = 0.0f;
+  if (valid && n < 4) {
+    vp = pos[p1cg[e * 4 + n]];
+    w = (float)wdg[e * 4 + n];
+  }
+  float p[4];
+#pragma unroll
+  for (int c2 = 0; c2 < 4; ++c2) p[c2] = (float)P[n * 4 + c2];
+  pdl_wait_then_trigger();
+  if (valid && n < 4) vc[le][n] = w * ecg[vp];
+  __syncthreads();
+  if (!valid) return;
+  float v = 0.0f;
+#pragma unroll
+  for (int c2 = 0; c2 < 4; ++c2) v += p[c2] * vc[le][c2];
+  x[e * 20 + n] += v;
+}
+
+// vertex gather of the element P1 restrictions (mixed path): one warp per
+// vertex, lanes over the vertex's DG copies, shuffle-reduced
+__global__ void gather_cg32_kernel(const float* __restrict__ r1, const int* __restrict__ gptr,
+                                   const int* __restrict__ gent, const double* __restrict__ wdg,
+                                   const int* __restrict__ pos, float* __restrict__ out, int ncg) {
+  const int i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  int k0 = 0, k1 = 0;
+  if (i < ncg) {
+    k0 = gptr[i];
+    k1 = gptr[i + 1];
+  }
+  pdl_wait_then_trigger();
+  if (i >= ncg) return;
+  float acc = 0.0f;
+  for (int k = k0 + lane; k < k1; k += 32) {
+    const int ent = gent[k];
+    acc += (float)wdg[ent] * r1[ent];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) out[pos[i]] = acc;
+}
+
 template <int D>
 int launch_transfer32(dg_ctx* c, const float* r, float* cg_out, float* x_add, const float* e_sfc,
                       cudaStream_t st) {
@@ -700,9 +804,14 @@ int launch_transfer32(dg_ctx* c, const float* r, float* cg_out, float* x_add, co
         r, c->T.P, c->d_gptr, c->d_gent, c->d_wdg, c->d_pos, cg_out, (int)c->ncg);
     bump();
   } else {
-    int rc = launch_k(c, prolong_cg_kernel<E::N, E::NC, float>, nblk(c->B * E::N, 256), 256, 0, st, x_add, e_sfc,
-                      (const int*)c->d_pos, (const int*)c->d_p1cg, (const double*)c->d_wdg, (const double*)c->T.P,
-                      (const int*)nullptr, 0, (int64_t)c->B, 1);
+    int rc;
+    if (D == 3)
+      rc = launch_k(c, prolong_cg32_kernel, nblk(c->B, 8), 160, 0, st, x_add, e_sfc, (const int*)c->d_pos,
+                    (const int*)c->d_p1cg, (const double*)c->d_wdg, (const double*)c->T.P, (int64_t)c->B);
+    else
+      rc = launch_k(c, prolong_cg_kernel<E::N, E::NC, float>, nblk(c->B * E::N, 256), 256, 0, st, x_add, e_sfc,
+                    (const int*)c->d_pos, (const int*)c->d_p1cg, (const double*)c->d_wdg, (const double*)c->T.P,
+                    (const int*)nullptr, 0, (int64_t)c->B, 1);
     if (rc) return rc;
   }
   CKL(c);
@@ -846,9 +955,8 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   }
   if ((rc = residual_pc(c, cur, r, nullptr, nullptr, RF_RESTRICT, st))) return rc;   // -> M.r1
   float* cg_dst = M.dense_l > 0 ? M.lev[0].r : M.cg1;
-  if ((rc = launch_k(c, gather_cg_kernel<float>, nblk(c->ncg, 128), 128, 0, st, (const float*)M.r1,
-                     (const int*)c->d_gptr, (const int*)c->d_gent, (const double*)c->d_wdg, (const int*)c->d_pos,
-                     cg_dst, (int)c->ncg)))
+  if ((rc = launch_k(c, gather_cg32_kernel, nblk(c->ncg, 8), 256, 0, st, (const float*)M.r1, (const int*)c->d_gptr,
+                     (const int*)c->d_gent, (const double*)c->d_wdg, (const int*)c->d_pos, cg_dst, (int)c->ncg)))
     return rc;
   if ((rc = vcycle32(c, cg_dst, st))) return rc;
   if ((rc = transfer32(c, nullptr, nullptr, cur, M.lev[0].e, st))) return rc;
