@@ -99,42 +99,66 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled during the timed region.
+
+    The sampler is started before the region and waits for its first line, so
+    that nvidia-smi is already polling (every 25 ms) when the region begins;
+    ``mark()`` brackets the region and only samples taken inside it count (the
+    one nearest after its start when the region is shorter than a period)."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, period_ms=25):
         self.gpu = gpu_index
+        self.period_ms = period_ms
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.perf_counter() + 10.0
+            while not self.lines and time.perf_counter() < deadline and self.proc.poll() is None:
+                time.sleep(0.005)
         except Exception:
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark(self, begin):
+        if begin:
+            self.t0 = time.perf_counter()
+        else:
+            self.t1 = time.perf_counter()
 
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        # one more period so that the sample covering the region's end is read
+        time.sleep(2 * self.period_ms / 1e3)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
+        t0 = self.t0 if self.t0 is not None else -np.inf
+        t1 = self.t1 if self.t1 is not None else np.inf
+        inside = [ln for ts, ln in self.lines if t0 <= ts <= t1 + self.period_ms / 1e3]
+        if not inside:
+            after = [ln for ts, ln in self.lines if ts >= t0]
+            inside = after[:1]
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in inside:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -378,6 +402,8 @@ def run_ours(args):
         l0 = _capi.launch_count()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
+        if clocks:
+            clocks.mark(True)
         ev0.record(stream)
         its_l = []
         for _ in range(args.steps):
@@ -385,6 +411,8 @@ def run_ours(args):
             its_l.append(its)
         ev1.record(stream)
         torch.cuda.synchronize()
+        if clocks:
+            clocks.mark(False)
         if ws > 1:
             torch.distributed.barrier()
         nl = _capi.launch_count() - l0
