@@ -234,8 +234,8 @@ def config_block(args, m, extra=None):
 # DRAM bytes (read + write) per launch of the roofline kernels on the
 # 20^3 Kuhn-cube workload (48,000 tets), from one ncu capture of
 # dram__bytes_read.sum + dram__bytes_write.sum (tables in
-# profiles/residual_tma_kernel_c2.md and profiles/residual_kernel_bf16_smooth_c2.md);
-# other workloads report null.
+# profiles/residual_tma_kernel_c2.md and profiles/residual_kernel_bf16_smooth_c2.md;
+# keys ending in _sf: the shared-face copies); other workloads report null.
 TRAFFIC_C2 = {
     "smooth_pc": {"bytes_per_launch": 242.4e6},
     "apply_f32": {"bytes_per_launch": 392.7e6},
@@ -490,21 +490,39 @@ def run_ours(args):
     N = m.nloc
     F = m.ndim + 1                                   # faces per simplex
 
-    def time_launch(fn, reps=20):
+    flush_buf = []
+
+    def time_launch(fn, reps=20, cold=False):
         # back-to-back launches of one kernel would overlap each other's
-        # prologue under programmatic dependent launch; time them plain
+        # prologue under programmatic dependent launch; time them plain.
+        # cold: each launch timed alone with the L2 flushed before it (a
+        # 512 MB write), so blocks left in L2 by the previous launch are not
+        # counted as HBM bandwidth
         s.set_launch_options(use_graph=True, use_pdl=False)
         for _ in range(3):
             fn()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(reps):
-            fn()
-        e1.record(stream)
-        torch.cuda.synchronize()
+        if cold:
+            if not flush_buf:
+                flush_buf.append(torch.empty(128 << 20, dtype=torch.float32, device=dev))
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+            for e0, e1 in ev:
+                flush_buf[0].fill_(1.0)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+            torch.cuda.synchronize()
+            t = sum(e0.elapsed_time(e1) for e0, e1 in ev) / reps / 1e3
+        else:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) / reps / 1e3
         s.set_launch_options(use_graph=True, use_pdl=True)
-        return e0.elapsed_time(e1) / reps / 1e3
+        return t
 
     peaks, kind = load_peaks()
     peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
@@ -516,16 +534,24 @@ def run_ours(args):
         bs = torch.randn(dofs, dtype=torch.float32, device=dev)
         xo = torch.empty_like(xs)
         mb = 2 if s.mixed_options.get("precond_bf16", True) else 4
-        nb = (m.nele + s_int) * N * N * mb + m.nele * N * N * mb + 3 * dofs * 4 + m.nele * F * 4
-        t = time_launch(lambda: s.smooth_pc(xs, bs, xo))
-        rooflines.append(("smooth_pc", "residual_tma_kernel<bf16> (bulk-copy streamed preconditioner "
-                          "smoothing step, BF16 blocks + smoother matrices, FP32 vectors)", nb, t,
-                          2.0 * N * N * (2 * m.nele + s_int)))
+        # stored blocks: own + one per interior face when faces are shared
+        # (s_int counts interior face sides), else own + one per face side;
+        # plus the face table read per element
+        nsh = int(s.info().get("shared_faces", 0))
+        nblk_a = m.nele + (nsh if nsh else s_int)
+        ftab = m.nele * (F + 1) * 4 if nsh else 0
+        nb = nblk_a * N * N * mb + m.nele * N * N * mb + 3 * dofs * 4 + m.nele * F * 4 + ftab
+        t = time_launch(lambda: s.smooth_pc(xs, bs, xo), cold=True)
+        form = "interior faces stored once" if nsh else "five blocks per element"
+        sfx = "_sf" if nsh else ""
+        rooflines.append(("smooth_pc" + sfx, "residual_tma_kernel<bf16> (bulk-copy streamed preconditioner "
+                          "smoothing step, BF16 blocks (%s) + smoother matrices, FP32 vectors; "
+                          "cold L2)" % form, nb, t, 2.0 * N * N * (2 * m.nele + s_int)))
         ya = torch.empty_like(xs)
-        nb = (m.nele + s_int) * N * N * 4 + 2 * dofs * 4 + m.nele * F * 4
-        t = time_launch(lambda: s.apply_f32(xs, ya))
-        rooflines.append(("apply_f32", "residual_tma_kernel<float> (bulk-copy streamed FP32 apply)",
-                          nb, t, 2.0 * N * N * (m.nele + s_int)))
+        nb = nblk_a * N * N * 4 + 2 * dofs * 4 + m.nele * F * 4 + ftab
+        t = time_launch(lambda: s.apply_f32(xs, ya), cold=True)
+        rooflines.append(("apply_f32" + sfx, "residual_tma_kernel<float> (bulk-copy streamed FP32 apply, "
+                          "%s; cold L2)" % form, nb, t, 2.0 * N * N * (m.nele + s_int)))
         # per inner iteration: preconditioner + apply; the rest is Gram-Schmidt,
         # Hessenberg updates and the refinement steps
         t_pc = time_launch(lambda: s.precond_f32(bs, xo))

@@ -1196,6 +1196,7 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
     if ((rc = build_mixed(c, st))) return rc;
     c->mixed_version = c->build_version;
   }
+  if (!M.has5 && (rc = build_blk5(c, st))) return rc;   // the batched kernels read five blocks per element
   if (M.dense_l < 0) return fail(c, DG_ERR_STATE, "dg_solve_mixed_batched: needs the dense coarse level");
   if (!c->f32_tma) return fail(c, DG_ERR_STATE, "dg_solve_mixed_batched: needs the chunked FP32 block layout");
   if ((rc = ensure_batch(c, m))) return rc;

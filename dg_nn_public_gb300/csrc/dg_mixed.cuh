@@ -40,6 +40,12 @@ struct Mixed {
   // BF16 copies read by the preconditioner's smoothing / residual kernels
   __nv_bfloat16* blk16 = nullptr;
   __nv_bfloat16* W16 = nullptr;
+  // shared-face copies (own blocks, then one block per interior face; 3D
+  // bulk-copy kernels): sf = in use for this build; has5 = the five-blocks
+  // per element copies above are current (plain kernels, batched solve)
+  float* sblk32 = nullptr;
+  __nv_bfloat16* sblk16 = nullptr;
+  bool sf = false, has5 = false;
   std::vector<Lev32> lev;
   float *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr, *t6 = nullptr;
   float *cg1 = nullptr;
@@ -53,6 +59,18 @@ struct Mixed {
   float* dense_inv = nullptr;
   int g_m = 0, g_chunk = 0;
   const float* g_vptr = nullptr;
+  // device-side convergence test of the inner FGMRES (givens_check_kernel,
+  // with dg_ctx::cond_graph):
+  // gv = [cs (m) | sn (m) | g (m+1) | threshold], kdone = first step count
+  // whose least-squares residual is below the threshold (0 = none yet);
+  // g_kern[chunk][step] = kernels of that step in the chunk's graph; cond =
+  // chunk graphs skip the steps after convergence (conditional nodes)
+  double* gv = nullptr;
+  int* kdone = nullptr;
+  std::vector<double> gv_host;
+  std::vector<std::vector<int>> g_kern;
+  std::vector<bool> g_cond;
+  bool cond = true;
   // Gram-Schmidt partial sums: one float4 of the vectors per thread,
   // nblk4 = ceil(nonods / 4 / 256) blocks, KMAXV sums per block
   double* part = nullptr;
@@ -341,6 +359,19 @@ struct Chunk20<__nv_bfloat16> {
   static __device__ __forceinline__ float dot(const Row& q, const float* v, float acc) {
     return dot_row20(q, v, acc);
   }
+  // acc + sum_n blk[n][m] * v[n], n = 0..19 in order: row m of the
+  // transposed block (column m of the stored one), same FMA order as dot
+  static __device__ __forceinline__ float dot_col(const unsigned char* blk, int m, const float* v, float acc) {
+    const int base = m < 8 ? 2 * m : (m < 16 ? 2 * kC20Off1 + 2 * (m - 8) : 2 * kC20Off2 + 2 * (m - 16));
+    const int step = m < 16 ? 16 : 8;
+    const unsigned char* p = blk + base;
+#pragma unroll
+    for (int n = 0; n < 20; ++n) {
+      const uint32_t h = *reinterpret_cast<const unsigned short*>(p + n * step);
+      acc = fmaf(__uint_as_float(h << 16), v[n], acc);
+    }
+    return acc;
+  }
 };
 
 template <>
@@ -363,7 +394,40 @@ struct Chunk20<float> {
     }
     return acc;
   }
+  static __device__ __forceinline__ float dot_col(const unsigned char* blk, int m, const float* v, float acc) {
+    const float* p = reinterpret_cast<const float*>(blk + 320 * (m >> 2) + 4 * (m & 3));
+#pragma unroll
+    for (int n = 0; n < 20; ++n) acc = fmaf(p[4 * n], v[n], acc);
+    return acc;
+  }
 };
+
+// ---------------------------------------------------------------------------
+// Shared face blocks.  The SIP operator is symmetric (A_{e,nb} = A_{nb,e}^T
+// to rounding; the face penalty uses the face's own area from either side),
+// so the reduced-precision copies store each interior face once: an array of
+// B own blocks followed by one block per interior face, that face's block of
+// its lower-numbered element (rows of that element, columns of the
+// neighbour).  fref5[e][0] = 2 e (own block), fref5[e][1 + f] = 2 (B + id) for
+// a face e owns, 2 (B + id) + 1 for a face its neighbour owns (read
+// transposed), -1 on the boundary.  The FP32 apply and the BF16 steps then
+// stream (B + #interior faces) blocks instead of 5 B.
+//
+// dst block i <- src block (idx[i]), converted into the chunked layout
+template <typename MT>
+__global__ void convert_gather_chunk20_kernel(const double* __restrict__ a, const int* __restrict__ idx,
+                                              MT* __restrict__ b, int64_t nblock) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nblock * 400) return;
+  const int64_t blk = k / 400;
+  const int rem = (int)(k - blk * 400);
+  const int n = rem / 20, m = rem % 20;
+  const float v = (float)a[(int64_t)idx[blk] * 400 + rem];
+  if constexpr (std::is_same<MT, float>::value)
+    b[blk * 400 + chunk20f_index(m, n)] = v;
+  else
+    b[blk * 400 + chunk20_index(m, n)] = __float2bfloat16_rn(v);
+}
 
 // ---------------------------------------------------------------------------
 // The residual / smoothing step of residual_kernel<20, 4, ., MT, float,
@@ -449,11 +513,11 @@ __device__ __forceinline__ void bulk_copy_g2s_hint(void* dst, const void* src, u
       : "memory");
 }
 
-template <typename MT, int EPB, int S, int MINB, bool WITH_W>
+template <typename MT, int EPB, int S, int MINB, bool WITH_W, bool SF>
 __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     const MT* __restrict__ blk, const MT* __restrict__ W, const int* __restrict__ nbe, const float* __restrict__ x,
     const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out, int64_t B, int flags,
-    const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err) {
+    const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const int* __restrict__ fref5) {
   constexpr int N = 20, F = 4;
   using G = TmaGroup<MT, EPB, WITH_W>;
   using C = Chunk20<MT>;
@@ -479,26 +543,93 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
   __syncthreads();
   const uint64_t pol = l2_evict_first_policy();
   const bool hint = flags & RF_STREAM_HINT;
-  // copies of the CTA's k-th group go to stage k % S, phase parity (k / S) & 1
+  const int lane = tid & 31;
+  // Shared-face mode, stage layout: the group's own blocks in slots
+  // 0 .. ne-1 (one copy), the face blocks the group's elements own from slot
+  // EPB on (their ids are consecutive: one copy), then one slot per face
+  // block owned by a neighbour (one copy each, read transposed).  For face
+  // (le, f) = lane 4 le + f: fslot[stage][lane] = its slot, bit lane of
+  // tmask[stage] = read transposed.
+  __shared__ uint32_t tmask[S];
+  __shared__ unsigned char fslot[S][32];
+  static_assert(!SF || 4 * EPB <= 32, "one lane per face of a group");
+  // warp 0, shared-face mode: fref5 entry of face (lane / 4, lane % 4) of
+  // the next group to be issued (loaded one group ahead)
+  int fr_a = -1;
+  auto load_fr = [&](int64_t k) {
+    fr_a = -1;
+    const int64_t g = blockIdx.x + k * stride;
+    if (!SF || zerox || g >= ngroups) return;
+    const int64_t e0 = g * EPB;
+    const int nf4 = 4 * (int)((B - e0) < EPB ? (B - e0) : EPB);
+    if (lane < nf4) fr_a = fref5[(e0 + lane / 4) * 5 + 1 + (lane & 3)];
+  };
+  // copies of the CTA's k-th group go to stage k % S, phase parity (k / S) & 1;
+  // called by all of warp 0 (the group test is uniform across the warp)
   auto issue = [&](int64_t k) {
     const int64_t g = blockIdx.x + k * stride;
     if (g >= ngroups) return;
     const int64_t e0 = g * EPB;
     const uint32_t ne = (uint32_t)((B - e0) < EPB ? (B - e0) : EPB);
-    const uint32_t ba = zerox ? 0u : ne * 5u * G::BlockBytes;
     const uint32_t bw = smooth ? ne * (uint32_t)G::BlockBytes : 0u;
     unsigned char* sp = tma_smem + (size_t)(k % S) * G::StageBytes;
-    mbar_expect_tx(&bar[k % S], ba + bw);
-    if (hint) {
-      if (ba) bulk_copy_g2s_hint(sp, blk + e0 * 2000, ba, &bar[k % S], pol);
-      if (bw) bulk_copy_g2s_hint(sp + G::ABytes, W + e0 * 400, bw, &bar[k % S], pol);
-    } else {
-      if (ba) bulk_copy_g2s(sp, blk + e0 * 2000, ba, &bar[k % S]);
-      if (bw) bulk_copy_g2s(sp + G::ABytes, W + e0 * 400, bw, &bar[k % S]);
+    uint64_t* br = &bar[k % S];
+    if constexpr (SF) {
+      constexpr uint32_t BB = G::BlockBytes;
+      const bool owned = fr_a >= 0 && !(fr_a & 1), trans = fr_a >= 0 && (fr_a & 1);
+      const uint32_t bi = (uint32_t)fr_a >> 1;   // block index in the shared array
+      const uint32_t mo = __ballot_sync(0xffffffffu, owned);
+      const uint32_t mt = __ballot_sync(0xffffffffu, trans);
+      const uint32_t bi0 = __reduce_min_sync(0xffffffffu, owned ? bi : 0xffffffffu);
+      const uint32_t no = __popc(mo), nt = __popc(mt);
+      uint32_t slot = owned ? EPB + (bi - bi0) : EPB + no + __popc(mt & ((1u << lane) - 1u));
+      if (fr_a >= 0 && slot >= 5u * EPB) {   // face table not in owner order: report, stay in the stage
+        atomicExch(err, 5);
+        slot = 0;
+      }
+      fslot[k % S][lane] = (unsigned char)(fr_a >= 0 ? slot : 0u);
+      if (lane == 0) {
+        tmask[k % S] = mt;
+        const uint32_t bo = zerox ? 0u : ne * BB;
+        mbar_expect_tx(br, bo + (no + nt) * BB + bw);
+        // own blocks, transposed reads and smoother matrices are their last
+        // use in this pass (evict first); a face block read as stored is read
+        // again, transposed, by the neighbour shortly after, so it stays in L2
+        if (hint) {
+          if (bo) bulk_copy_g2s_hint(sp, blk + e0 * 400, bo, br, pol);
+          if (bw) bulk_copy_g2s_hint(sp + G::ABytes, W + e0 * 400, bw, br, pol);
+        } else {
+          if (bo) bulk_copy_g2s(sp, blk + e0 * 400, bo, br);
+          if (bw) bulk_copy_g2s(sp + G::ABytes, W + e0 * 400, bw, br);
+        }
+        if (no) bulk_copy_g2s(sp + (size_t)EPB * BB, blk + (int64_t)bi0 * 400, no * BB, br);
+      }
+      __syncwarp();
+      if (trans) {
+        const MT* src = blk + (int64_t)bi * 400;
+        unsigned char* dst = sp + (size_t)slot * BB;
+        if (hint) bulk_copy_g2s_hint(dst, src, BB, br, pol);
+        else bulk_copy_g2s(dst, src, BB, br);
+      }
+    } else if (lane == 0) {
+      const uint32_t ba = zerox ? 0u : ne * 5u * G::BlockBytes;
+      mbar_expect_tx(br, ba + bw);
+      if (hint) {
+        if (ba) bulk_copy_g2s_hint(sp, blk + e0 * 2000, ba, br, pol);
+        if (bw) bulk_copy_g2s_hint(sp + G::ABytes, W + e0 * 400, bw, br, pol);
+      } else {
+        if (ba) bulk_copy_g2s(sp, blk + e0 * 2000, ba, br);
+        if (bw) bulk_copy_g2s(sp + G::ABytes, W + e0 * 400, bw, br);
+      }
     }
   };
-  if (tid == 0)
-    for (int k = 0; k < S; ++k) issue(k);
+  if (tid < 32) {
+    for (int k = 0; k < S; ++k) {
+      load_fr(k);
+      issue(k);
+    }
+    load_fr(S);
+  }
   // register prefetch of the gathers of the next group
   auto load_nb = [&](int64_t g) {
     const int64_t e = g * EPB + le;
@@ -543,11 +674,19 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     const unsigned char* sp = tma_smem + (size_t)s * G::StageBytes;
     float acc = 0.0f;
     if (valid && !zerox) {
-      const unsigned char* Ae = sp + (size_t)le * 5 * G::BlockBytes;
+      const unsigned char* Ae = sp + (size_t)le * (SF ? 1 : 5) * G::BlockBytes;
+      const uint32_t tm = SF ? tmask[s] >> (4 * le) : 0u;
       acc = C::dot(C::lds(Ae, m), xs[le][0], acc);
 #pragma unroll
       for (int f = 0; f < F; ++f)
-        if (nbv[f] >= 0) acc = C::dot(C::lds(Ae + (1 + f) * G::BlockBytes, m), xs[le][1 + f], acc);
+        if (nbv[f] >= 0) {
+          const unsigned char* Af =
+              SF ? sp + (size_t)fslot[s][4 * le + f] * G::BlockBytes : Ae + (1 + f) * G::BlockBytes;
+          if (SF && ((tm >> f) & 1u))
+            acc = C::dot_col(Af, m, xs[le][1 + f], acc);
+          else
+            acc = C::dot(C::lds(Af, m), xs[le][1 + f], acc);
+        }
     }
     float res = 0.0f;
     if (valid) {
@@ -568,9 +707,10 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
                            C::dot(C::lds(sp + G::ABytes + (size_t)le * G::BlockBytes, m), rs[le], 0.0f);
     }
     __syncthreads();   // stage s and xs / rs free again
-    if (tid == 0) {
+    if (tid < 32) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       issue(k + S);
+      if (SF) load_fr(k + S + 1);
     }
   }
   if (abort_flag && tid == 0) {
@@ -582,22 +722,31 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
   }
 }
 
+// sf: shared-face block array (blk = own blocks + one block per interior
+// face, addressed through c->d_fref5); otherwise five blocks per element
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
 int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out,
-               int flags, float* r1, cudaStream_t st) {
+               int flags, float* r1, cudaStream_t st, bool sf) {
   if (c->l2_hint) flags |= RF_STREAM_HINT;
   const int64_t ngroups = (c->B + EPB - 1) / EPB;
   const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
-  return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W>, g, EPB * 20,
-                  (size_t)S * TmaGroup<MT, EPB, WITH_W>::StageBytes, st, blk, W, (const int*)c->d_nbe, x, b, r,
-                  x_out, (int64_t)c->B, flags, (const double*)c->T.P, r1, (int*)c->d_err);
+  const size_t smem = (size_t)S * TmaGroup<MT, EPB, WITH_W>::StageBytes;
+  if (sf)
+    return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W, true>, g, EPB * 20, smem, st, blk, W,
+                    (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const double*)c->T.P, r1,
+                    (int*)c->d_err, (const int*)c->d_fref5);
+  return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W, false>, g, EPB * 20, smem, st, blk, W,
+                  (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const double*)c->T.P, r1,
+                  (int*)c->d_err, (const int*)nullptr);
 }
 
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
 int set_tma_smem(dg_ctx* c) {
-  CK(c, cudaFuncSetAttribute(residual_tma_kernel<MT, EPB, S, MINB, WITH_W>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             S * TmaGroup<MT, EPB, WITH_W>::StageBytes));
+  const int bytes = S * TmaGroup<MT, EPB, WITH_W>::StageBytes;
+  CK(c, cudaFuncSetAttribute(residual_tma_kernel<MT, EPB, S, MINB, WITH_W, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  CK(c, cudaFuncSetAttribute(residual_tma_kernel<MT, EPB, S, MINB, WITH_W, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   return DG_OK;
 }
 
@@ -610,10 +759,11 @@ constexpr int kTmaVariants = 3;
 
 int launch_bf16_tma(dg_ctx* c, Mixed& M, const float* x, const float* b, float* r, float* x_out, int flags,
                     cudaStream_t st) {
+  const __nv_bfloat16* A = M.sf ? M.sblk16 : M.blk16;
   switch (c->tma_variant) {
-    case 1: return launch_tma<__nv_bfloat16, 8, 2, 2, true>(c, M.blk16, M.W16, x, b, r, x_out, flags, M.r1, st);
-    case 2: return launch_tma<__nv_bfloat16, 4, 2, 4, true>(c, M.blk16, M.W16, x, b, r, x_out, flags, M.r1, st);
-    default: return launch_tma<__nv_bfloat16, 6, 2, 3, true>(c, M.blk16, M.W16, x, b, r, x_out, flags, M.r1, st);
+    case 1: return launch_tma<__nv_bfloat16, 8, 2, 2, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf);
+    case 2: return launch_tma<__nv_bfloat16, 4, 2, 4, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf);
+    default: return launch_tma<__nv_bfloat16, 6, 2, 3, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf);
   }
 }
 
@@ -684,8 +834,9 @@ int launch_residual32(dg_ctx* c, const float* x, const float* b, float* r, float
   using E = Elem<D>;
   Mixed& M = mixed_of(c);
   if (D == 3 && c->f32_tma) {   // chunked FP32 copy, bulk-copy kernel
-    if (flags & RF_SMOOTH) return launch_tma<float, 4, 2, 2, true>(c, M.blk, M.W, x, b, r, x_out, flags, M.r1, st);
-    return launch_tma<float, 4, 2, 3, false>(c, M.blk, M.W, x, b, r, x_out, flags, M.r1, st);
+    const float* A = M.sf ? M.sblk32 : M.blk;
+    if (flags & RF_SMOOTH) return launch_tma<float, 4, 2, 2, true>(c, A, M.W, x, b, r, x_out, flags, M.r1, st, M.sf);
+    return launch_tma<float, 4, 2, 3, false>(c, A, M.W, x, b, r, x_out, flags, M.r1, st, M.sf);
   }
   unsigned g = nblk(c->B, E::EPB);
   if (g)
@@ -838,13 +989,15 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
     // lev[0].r (gathered there directly when r_sfc is lev[0].r) and level 0
     // starts from a zero guess (e_in = NULL in its first sweep)
     const int lc = M.dense_l;
+    const int npre = c->mixed_lev_sweeps >= 0 ? c->mixed_lev_sweeps : c->cfg.pre_smooth_its;
+    const int npost = c->mixed_lev_sweeps >= 0 ? c->mixed_lev_sweeps : c->cfg.post_smooth_its;
     int rc;
     if (r_sfc != M.lev[0].r)
       CK(c, cudaMemcpyAsync(M.lev[0].r, r_sfc, sizeof(float) * M.lev[0].n, cudaMemcpyDeviceToDevice, st));
     for (int l = 0; l < lc; ++l) {
       Lev32& L = M.lev[l];
       const unsigned gj = nblk((int64_t)L.n * LPR, TB);
-      for (int it = 0; it < c->cfg.pre_smooth_its; ++it) {
+      for (int it = 0; it < npre; ++it) {
         const float* ein = (l == 0 && it == 0) ? nullptr : L.e;
         if ((rc = launch_k(c, lev_jacobi_kernel<float>, gj, TB, 0, st, (const int*)L.rowptr, (const int*)L.col,
                            (const float*)L.val, (const float*)L.diag, ein, (const float*)L.r, L.e2,
@@ -852,7 +1005,7 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
           return rc;
         std::swap(L.e, L.e2);
       }
-      const float* ein = (l == 0 && c->cfg.pre_smooth_its == 0) ? nullptr : L.e;
+      const float* ein = (l == 0 && npre == 0) ? nullptr : L.e;
       if ((rc = launch_k(c, lev_jacobi_kernel<float>, gj, TB, 0, st, (const int*)L.rowptr, (const int*)L.col,
                          (const float*)L.val, (const float*)L.diag, ein, (const float*)L.r, L.e2, L.rr, L.n, w)))
         return rc;
@@ -873,7 +1026,7 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
       if ((rc = launch_k(c, lev_prolong_kernel<float>, nblk(L.n, TB), TB, 0, st, L.e, (const float*)M.lev[l + 1].e,
                          (const int*)L.up, L.n)))
         return rc;
-      for (int it = 0; it < c->cfg.post_smooth_its; ++it) {
+      for (int it = 0; it < npost; ++it) {
         if ((rc = launch_k(c, lev_jacobi_kernel<float>, nblk((int64_t)L.n * LPR, TB), TB, 0, st,
                            (const int*)L.rowptr, (const int*)L.col, (const float*)L.val, (const float*)L.diag,
                            (const float*)L.e, (const float*)L.r, L.e2, (float*)nullptr, L.n, w)))
@@ -941,7 +1094,7 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
 int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   Mixed& M = mixed_of(c);
   int rc;
-  const int nsm = c->cfg.pre_smooth_its;
+  const int nsm = c->mixed_sweeps >= 0 ? c->mixed_sweeps : c->cfg.pre_smooth_its;
   float* cur = M.t3;
   float* other = M.t4;
   if (nsm > 0) {
@@ -980,6 +1133,33 @@ __global__ void convert_f64_bf16_kernel(const double* __restrict__ a, __nv_bfloa
   if (k < n) b[k] = __float2bfloat16_rn((float)a[k]);
 }
 
+// Five blocks per element copies of the operator (FP32; BF16 when the
+// preconditioner reads BF16), read by the plain kernels and the batched solve.
+int build_blk5(dg_ctx* c, cudaStream_t st) {
+  Mixed& M = mixed_of(c);
+  int rc;
+  const size_t nb = (size_t)c->B * (c->F + 1) * c->N * c->N;
+  if (!M.blk && (rc = dalloc(c, &M.blk, nb))) return rc;
+  if (c->D == 3 && c->f32_tma)
+    convert_f64_f32_chunk20_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk,
+                                                                          (int64_t)c->B * (c->F + 1));
+  else
+    convert_f64_f32_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk, (int64_t)nb);
+  bump();
+  if (c->precond_bf16) {
+    if (!M.blk16 && (rc = dalloc(c, &M.blk16, nb))) return rc;
+    if (c->D == 3)   // chunked layout read by residual_bf16c20_kernel
+      convert_f64_bf16_chunk20_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk16,
+                                                                             (int64_t)c->B * (c->F + 1));
+    else
+      convert_f64_bf16_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk16, (int64_t)nb);
+    bump();
+  }
+  CKL(c);
+  M.has5 = true;
+  return DG_OK;
+}
+
 int build_mixed(dg_ctx* c, cudaStream_t st) {
   Mixed& M = mixed_of(c);
   int rc;
@@ -987,22 +1167,31 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
       (rc = set_tma_smem<__nv_bfloat16, 4, 2, 4, true>(c)) || (rc = set_tma_smem<float, 4, 2, 3, false>(c)) ||
       (rc = set_tma_smem<float, 4, 2, 2, true>(c)))
     return rc;
-  const size_t nb = (size_t)c->B * (c->F + 1) * c->N * c->N;
   const size_t nw = (size_t)c->B * c->N * c->N;
-  if (!M.blk) {
-    if ((rc = dalloc(c, &M.blk, nb))) return rc;
-    if ((rc = dalloc(c, &M.W, nw))) return rc;
+  if (!M.t1) {
     for (float** t : {&M.t1, &M.t2, &M.t3, &M.t4, &M.t5, &M.t6})
       if ((rc = dalloc(c, t, (size_t)c->nonods))) return rc;
     if ((rc = dalloc(c, &M.cg1, (size_t)c->ncg))) return rc;
     if ((rc = dalloc(c, &M.r1, (size_t)c->B * c->NC))) return rc;
   }
-  if (c->D == 3 && c->f32_tma)
-    convert_f64_f32_chunk20_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk,
-                                                                          (int64_t)c->B * (c->F + 1));
-  else
-    convert_f64_f32_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk, (int64_t)nb);
-  bump();
+  if (!M.W && (rc = dalloc(c, &M.W, nw))) return rc;
+  // operator copies: shared-face arrays for the 3D bulk-copy kernels, else
+  // five blocks per element
+  M.sf = c->D == 3 && c->shared_faces && c->d_fref5 && c->f32_tma && c->bf16_tma && c->precond_bf16;
+  M.has5 = false;
+  if (M.sf) {
+    const int64_t ns = (int64_t)c->B + c->nface_sh;
+    if (!M.sblk32 && (rc = dalloc(c, &M.sblk32, (size_t)ns * 400))) return rc;
+    if (!M.sblk16 && (rc = dalloc(c, &M.sblk16, (size_t)ns * 400))) return rc;
+    convert_gather_chunk20_kernel<float><<<nblk(ns * 400, 256), 256, 0, st>>>(c->d_blk, c->d_sfsrc, M.sblk32, ns);
+    bump();
+    convert_gather_chunk20_kernel<__nv_bfloat16><<<nblk(ns * 400, 256), 256, 0, st>>>(c->d_blk, c->d_sfsrc,
+                                                                                        M.sblk16, ns);
+    bump();
+    CKL(c);
+  } else if ((rc = build_blk5(c, st))) {
+    return rc;
+  }
   // smoother matrices of the mixed preconditioner
   const double* Wsrc = c->d_W;
   double* Winv = nullptr;
@@ -1022,22 +1211,12 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
     convert_f64_f32_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W, (int64_t)nw);
   bump();
   if (c->precond_bf16) {
-    if (!M.blk16) {
-      if ((rc = dalloc(c, &M.blk16, nb))) return rc;
-      if ((rc = dalloc(c, &M.W16, nw))) return rc;
-    }
-    if (c->D == 3) {   // chunked layout read by residual_bf16c20_kernel
-      convert_f64_bf16_chunk20_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk16,
-                                                                             (int64_t)c->B * (c->F + 1));
-      bump();
+    if (!M.W16 && (rc = dalloc(c, &M.W16, nw))) return rc;
+    if (c->D == 3)
       convert_f64_bf16_chunk20_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W16, (int64_t)c->B);
-      bump();
-    } else {
-      convert_f64_bf16_kernel<<<nblk((int64_t)nb, 256), 256, 0, st>>>(c->d_blk, M.blk16, (int64_t)nb);
-      bump();
+    else
       convert_f64_bf16_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W16, (int64_t)nw);
-      bump();
-    }
+    bump();
   }
   if (Winv) {
     int herr = 0;
@@ -1132,6 +1311,10 @@ int ensure_krylov32(dg_ctx* c, int m) {
   if (!M.part) {
     M.nblk4 = (int)((c->nonods / 4 + RED_TB - 1) / RED_TB);
     if ((rc = dalloc(c, &M.part, (size_t)std::max(M.nblk4, 1) * KMAXV))) return rc;
+  }
+  if (!M.gv) {   // sized for the largest restart length (256)
+    if ((rc = dalloc(c, &M.gv, (size_t)3 * 256 + 2))) return rc;
+    if ((rc = dalloc(c, &M.kdone, 1))) return rc;
   }
   M.vcap = m + 1;
   return DG_OK;
@@ -1337,26 +1520,120 @@ int cgs2_32(dg_ctx* c, int j, float* w, int m, cudaStream_t st) {
   return DG_OK;
 }
 
-// inner Arnoldi steps j0 .. j0+cnt-1: z_j = M v_j (kept), w = A z_j, CGS2
-int arnoldi32_steps(dg_ctx* c, int j0, int cnt, int m, cudaStream_t st) {
+// Incremental Givens QR of the inner Hessenberg matrix, one FP64 thread:
+// rotations 0..j-1 (kept in gv) carried down column j of H, then rotation j
+// and the least-squares residual |g[j+1]| of the j+1 step Krylov space.  At
+// or below the threshold (or NaN) the step count goes to *kdone and, inside a
+// chunk graph, the conditional node of step j+1 is switched off, so the
+// remaining steps of the chunk are skipped on the device.  H is not changed:
+// the host solves the least-squares problem from H itself.
+__global__ void givens_check_kernel(const double* __restrict__ H, int m, int j, double* __restrict__ gv,
+                                    int* __restrict__ kdone, cudaGraphConditionalHandle next, int has_next) {
+  pdl_wait_then_trigger();
+  if (threadIdx.x != 0) return;
+  double* cs = gv;
+  double* sn = gv + m;
+  double* g = gv + 2 * m;
+  const double thresh = gv[3 * m + 1];
+  const double* h = H + (size_t)j * (m + 1);
+  double hi = h[0];
+  for (int i = 0; i < j; ++i) hi = -sn[i] * hi + cs[i] * h[i + 1];
+  const double hj1 = h[j + 1];
+  const double r = sqrt(hi * hi + hj1 * hj1);
+  double cr = 1.0, sr = 0.0;
+  if (r > 0.0) {
+    cr = hi / r;
+    sr = hj1 / r;
+  }
+  cs[j] = cr;
+  sn[j] = sr;
+  const double gj = g[j];
+  g[j] = cr * gj;
+  g[j + 1] = -sr * gj;
+  const bool done = !(fabs(g[j + 1]) > thresh);
+  if (done && *kdone == 0) *kdone = j + 1;
+  if (has_next) cudaGraphSetConditional(next, done ? 0u : 1u);
+}
+
+// inner Arnoldi step j: z_j = M v_j (kept), w = A z_j, Gram-Schmidt, then
+// the device-side convergence test
+int arnoldi32_step(dg_ctx* c, int j, int m, cudaStream_t st, cudaGraphConditionalHandle next, int has_next) {
   Mixed& M = mixed_of(c);
   int rc;
-  for (int j = j0; j < j0 + cnt; ++j) {
-    float* zj = M.Z + (size_t)j * c->nonods;
-    if ((rc = precond32(c, M.V + (size_t)j * c->nonods, zj, st))) return rc;
-    if ((rc = residual32(c, zj, nullptr, M.t1, nullptr, RF_NEG, st))) return rc;   // t1 = A z_j
-    if ((rc = cgs2_32(c, j, M.t1, m, st))) return rc;
-  }
+  float* zj = M.Z + (size_t)j * c->nonods;
+  if ((rc = precond32(c, M.V + (size_t)j * c->nonods, zj, st))) return rc;
+  if ((rc = residual32(c, zj, nullptr, M.t1, nullptr, RF_NEG, st))) return rc;   // t1 = A z_j
+  if ((rc = cgs2_32(c, j, M.t1, m, st))) return rc;
+  if (!c->cond_graph) return DG_OK;
+  return launch_k(c, givens_check_kernel, 1, 32, 0, st, (const double*)M.H, m, j, M.gv, M.kdone, next, has_next);
+}
+
+int arnoldi32_steps(dg_ctx* c, int j0, int cnt, int m, cudaStream_t st) {
+  int rc;
+  for (int j = j0; j < j0 + cnt; ++j)
+    if ((rc = arnoldi32_step(c, j, m, st, 0, 0))) return rc;
   return DG_OK;
 }
 
-int run_arnoldi32(dg_ctx* c, int j0, int cnt, int m, int chunk, cudaStream_t st) {
+// Graph of steps j0 .. j0+cnt-1, each step the body of an IF conditional
+// node; the node of step j0 runs at every launch (default 1), the others run
+// when the preceding step's convergence test leaves them on.  kern[i] =
+// kernels of step i.  Returns cudaSuccess or the first CUDA error (the caller
+// then falls back to plain captured chunks).
+cudaError_t build_cond_chunk(dg_ctx* c, int j0, int cnt, int m, cudaGraphExec_t* exec, std::vector<int>& kern,
+                             int* rc_out) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  std::vector<cudaGraphConditionalHandle> h(cnt);
+  for (int i = 0; i < cnt && e == cudaSuccess; ++i)
+    e = cudaGraphConditionalHandleCreate(&h[i], g, i == 0 ? 1u : 0u, cudaGraphCondAssignDefault);
+  cudaGraphNode_t prev = nullptr;
+  kern.assign(cnt, 0);
+  for (int i = 0; i < cnt && e == cudaSuccess; ++i) {
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h[i];
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    e = cudaGraphAddNode(&node, g, prev ? &prev : nullptr, nullptr, prev ? 1 : 0, &p);
+    if (e != cudaSuccess) break;
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(c->cap_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) break;
+    const long long k0 = g_launches.load();
+    const int rc = arnoldi32_step(c, j0 + i, m, c->cap_stream, i + 1 < cnt ? h[i + 1] : 0, i + 1 < cnt ? 1 : 0);
+    kern[i] = (int)(g_launches.load() - k0);
+    g_launches.fetch_sub(kern[i]);   // captured, not launched
+    cudaGraph_t got = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(c->cap_stream, &got);
+    if (rc) {
+      *rc_out = rc;
+      cudaGraphDestroy(g);
+      return cudaSuccess;
+    }
+    e = ee;
+    prev = node;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  return e;
+}
+
+// Runs steps j0 .. j0+cnt-1 (one chunk).  *mode: 0 = direct launches (all
+// steps ran, kernels already counted), 1 = plain chunk graph (all steps ran),
+// 2 = conditional chunk graph (steps up to the convergence test's step ran).
+int run_arnoldi32(dg_ctx* c, int j0, int cnt, int m, int chunk, cudaStream_t st, int* mode) {
   Mixed& M = mixed_of(c);
+  *mode = 0;
   if (!c->use_graph) return arnoldi32_steps(c, j0, cnt, m, st);
   if (M.g_m != m || M.g_chunk != chunk || M.g_vptr != M.V) {
     for (auto& g : M.graphs)
       if (g) cudaGraphExecDestroy(g);
     M.graphs.assign((m + chunk - 1) / chunk, nullptr);
+    M.g_kern.assign(M.graphs.size(), std::vector<int>());
+    M.g_cond.assign(M.graphs.size(), false);
     M.g_m = m;
     M.g_chunk = chunk;
     M.g_vptr = M.V;
@@ -1365,21 +1642,53 @@ int run_arnoldi32(dg_ctx* c, int j0, int cnt, int m, int chunk, cudaStream_t st)
   if (cnt != std::min(chunk, m - j0) || j0 % chunk) return arnoldi32_steps(c, j0, cnt, m, st);
   if (!M.graphs[gi]) {
     if (!c->cap_stream) CK(c, cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
-    CK(c, cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
-    int rc = arnoldi32_steps(c, j0, cnt, m, c->cap_stream);
-    cudaGraph_t g = nullptr;
-    cudaError_t ee = cudaStreamEndCapture(c->cap_stream, &g);
-    if (rc) {
-      if (g) cudaGraphDestroy(g);
-      return rc;
+    M.g_cond.resize(M.graphs.size());
+    M.g_cond[gi] = false;
+    if (M.cond && c->cond_graph) {
+      int rc = DG_OK;
+      const cudaError_t e = build_cond_chunk(c, j0, cnt, m, &M.graphs[gi], M.g_kern[gi], &rc);
+      if (rc) return rc;
+      if (e != cudaSuccess) {   // no conditional nodes here: plain chunks from now on
+        cudaGetLastError();
+        if (c->verbose) std::fprintf(stderr, "[dg_solve_mixed] conditional chunk graph: %s\n", cudaGetErrorString(e));
+        M.cond = false;
+        M.graphs[gi] = nullptr;
+      } else {
+        M.g_cond[gi] = true;
+      }
     }
-    if (ee != cudaSuccess) return fail(c, DG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
-    cudaError_t ie = cudaGraphInstantiate(&M.graphs[gi], g, 0);
-    cudaGraphDestroy(g);
-    if (ie != cudaSuccess) return fail(c, DG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    if (!M.graphs[gi]) {
+      CK(c, cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
+      const long long k0 = g_launches.load();
+      int rc = arnoldi32_steps(c, j0, cnt, m, c->cap_stream);
+      const int nk = (int)(g_launches.load() - k0);
+      g_launches.fetch_sub(nk);
+      M.g_kern[gi].assign(cnt, nk / std::max(cnt, 1));
+      cudaGraph_t g = nullptr;
+      cudaError_t ee = cudaStreamEndCapture(c->cap_stream, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (ee != cudaSuccess) return fail(c, DG_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ee));
+      cudaError_t ie = cudaGraphInstantiate(&M.graphs[gi], g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) return fail(c, DG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    }
   }
   CK(c, cudaGraphLaunch(M.graphs[gi], st));
+  *mode = M.g_cond[gi] ? 2 : 1;
   return DG_OK;
+}
+
+// Kernel count of the first `ran` steps of the chunk graph starting at j0
+long long chunk_kernels(dg_ctx* c, int j0, int ran) {
+  Mixed& M = mixed_of(c);
+  const int gi = j0 / std::max(M.g_chunk, 1);
+  long long k = 0;
+  if (gi < (int)M.g_kern.size())
+    for (int i = 0; i < ran && i < (int)M.g_kern[gi].size(); ++i) k += M.g_kern[gi][i];
+  return k;
 }
 
 // Givens least squares on the leading (k+1) x k block of the column-major
@@ -1528,18 +1837,31 @@ extern "C" int dg_solve_mixed(dg_ctx* c, double* x, const double* b, double tol,
       scale_kernel<float><<<nblk(n, 256), 256, 0, st>>>(V0, c->d_scal, V0, n);
       bump();
       CK(c, cudaMemsetAsync(M.H, 0, sizeof(double) * (m + 1) * m, st));
+      // device-side convergence test: g = beta e1, threshold target * beta0
+      M.gv_host.assign((size_t)3 * m + 2, 0.0);
+      M.gv_host[2 * m] = beta;
+      M.gv_host[3 * m + 1] = target * beta0;
+      CK(c, cudaMemcpyAsync(M.gv, M.gv_host.data(), sizeof(double) * M.gv_host.size(), cudaMemcpyHostToDevice, st));
+      CK(c, cudaMemsetAsync(M.kdone, 0, sizeof(int), st));
       int k = 0;
       bool conv = false, ok = true;
       for (int j0 = 0; j0 < m; j0 += chunk) {
         const int cnt = std::min(chunk, m - j0);
-        if ((rc = run_arnoldi32(c, j0, cnt, m, chunk, st))) return rc;
-        its += cnt;
-        k = j0 + cnt;
+        int mode = 0, kd = 0;
+        if ((rc = run_arnoldi32(c, j0, cnt, m, chunk, st, &mode))) return rc;
         CK(c, cudaMemcpyAsync(Hh.data(), M.H, sizeof(double) * Hh.size(), cudaMemcpyDeviceToHost, st));
+        CK(c, cudaMemcpyAsync(&kd, M.kdone, sizeof(int), cudaMemcpyDeviceToHost, st));
         CK(c, cudaStreamSynchronize(st));
+        // steps that ran: all of the chunk, or (conditional chunk graph) up to
+        // the step that met the threshold; the solution uses the Krylov space
+        // of that step either way
+        const int ran = (kd > 0 && mode == 2) ? kd - j0 : cnt;
+        if (mode != 0) bump(chunk_kernels(c, j0, ran));
+        its += ran;
+        k = kd > 0 ? kd : j0 + cnt;
         double est = hessenberg_ls(Hh, m, k, beta, y, ok);
         if (!ok) break;
-        if (est <= target * beta0) {
+        if (kd > 0 || est <= target * beta0) {
           conv = true;
           break;
         }
@@ -1579,6 +1901,10 @@ extern "C" int dg_solve_mixed(dg_ctx* c, double* x, const double* b, double tol,
     if (herr == 3) {
       c->err = "mixed solve: a bulk-copy wait of the preconditioner timed out";
       return DG_ERR_CUDA;
+    }
+    if (herr == 5) {
+      c->err = "mixed solve: shared-face table not in owner order";
+      return DG_ERR_STATE;
     }
   }
   if (status == DG_OK && rn > tol) {

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "dg_internal.h"
@@ -55,6 +56,12 @@ struct dg_ctx {
   std::vector<void*> allocs;
   double* d_x = nullptr;
   int *d_nbe = nullptr, *d_nbface = nullptr, *d_aln = nullptr, *d_bct = nullptr;
+  // shared-face tables of the reduced-precision copies (3D): d_fref5[e][j]
+  // addresses slot j of element e in the shared block array (2 * block + 1
+  // when read transposed, -1 on the boundary); d_sfsrc[i] = FP64 source
+  // block of shared block i; nface_sh = interior faces
+  int *d_fref5 = nullptr, *d_sfsrc = nullptr;
+  int64_t nface_sh = 0;
   double* d_kappa = nullptr;
   Tables T{};
   double* d_blk = nullptr;
@@ -105,6 +112,20 @@ struct dg_ctx {
   bool f32_tma = true;
   // bulk-copy block streams read with an L2 evict-first policy
   bool l2_hint = true;
+  // store each interior face block once in the reduced-precision copies
+  // (c2: DRAM bytes of the BF16 step 238 -> 161 MB and of the FP32 apply
+  // 385 -> 235 MB, but 37.5 -> 49 us and 59 -> 70 us: the transposed reads
+  // are column reads from shared memory; kept as an option)
+  bool shared_faces = false;
+  // mixed preconditioner: DG-level smoothing steps before / after the coarse
+  // correction and Jacobi sweeps on the SFC levels (-1 = the configured
+  // pre_smooth_its, as in the FP64 preconditioner)
+  int mixed_sweeps = -1, mixed_lev_sweeps = -1;
+  // mixed inner FGMRES: per-step convergence test on the device, chunk
+  // graphs with one conditional node per step (c2: 100 -> 98 inner steps,
+  // but 30.5 -> 31.4 ms: the stops land where the chunk checks already did
+  // and the per-step nodes cost ~15 us; kept as an option)
+  bool cond_graph = false;
   // link the kernels of an inner Arnoldi step by programmatic dependent launch
   bool use_pdl = true;
   // batched solve: BF16 preconditioner steps on the tensor cores (mma.sync)
@@ -135,6 +156,7 @@ struct dg_ctx {
   void* mixed_state = nullptr;
   int build_version = 0;
   int mixed_version = -1;
+  long long arnoldi_kernels = 0;   // kernels in the captured Arnoldi cycle graph
 };
 
 namespace {
@@ -558,7 +580,10 @@ int run_arnoldi(dg_ctx* c, int m, cudaStream_t st) {
     }
     if (!c->cap_stream) CK(c, cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
     CK(c, cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const long long k0 = g_launches.load();
     int rc = arnoldi_steps(c, m, c->cap_stream);
+    c->arnoldi_kernels = g_launches.load() - k0;
+    g_launches.fetch_sub(c->arnoldi_kernels);   // captured, counted per replay below
     cudaGraph_t g = nullptr;
     cudaError_t ee = cudaStreamEndCapture(c->cap_stream, &g);
     if (rc) {
@@ -573,6 +598,7 @@ int run_arnoldi(dg_ctx* c, int m, cudaStream_t st) {
     c->arnoldi_vptr = c->d_V;
   }
   CK(c, cudaGraphLaunch(c->arnoldi_exec, st));
+  bump(c->arnoldi_kernels);
   return DG_OK;
 }
 
@@ -644,10 +670,12 @@ void dg_destroy(dg_ctx* ctx) {
 
 int dg_info(const dg_ctx* ctx, int64_t* out, int32_t nout) {
   if (!ctx || !out) return set_thread_error(DG_ERR_ARG, "dg_info: null argument");
-  int64_t v[14] = {ctx->D, ctx->N, ctx->B, ctx->nonods, ctx->ncg, (int64_t)ctx->cola.size(), ctx->ncolor,
+  const bool sf = ctx->D == 3 && ctx->shared_faces && ctx->d_fref5 && ctx->f32_tma && ctx->bf16_tma &&
+                  ctx->precond_bf16;
+  int64_t v[15] = {ctx->D, ctx->N, ctx->B, ctx->nonods, ctx->ncg, (int64_t)ctx->cola.size(), ctx->ncolor,
                    (int64_t)ctx->lev.size(), ctx->nbf, ctx->built ? 1 : 0, ctx->VG, ctx->SG, ctx->tma_variant,
-                   ctx->batched_tma ? 1 : 0};
-  for (int i = 0; i < nout && i < 14; ++i) out[i] = v[i];
+                   ctx->batched_tma ? 1 : 0, sf ? ctx->nface_sh : 0};
+  for (int i = 0; i < nout && i < 15; ++i) out[i] = v[i];
   return DG_OK;
 }
 
@@ -705,6 +733,14 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (pd && pd[0]) c->use_pdl = pd[0] != '0';
     const char* lh = std::getenv("DG_L2_HINT");
     if (lh && lh[0]) c->l2_hint = lh[0] != '0';
+    const char* sf = std::getenv("DG_SHARED_FACES");
+    if (sf && sf[0]) c->shared_faces = sf[0] != '0';
+    const char* cg = std::getenv("DG_COND_GRAPH");
+    if (cg && cg[0]) c->cond_graph = cg[0] != '0';
+    const char* msw = std::getenv("DG_MIXED_SWEEPS");
+    if (msw && msw[0]) c->mixed_sweeps = std::atoi(msw);
+    const char* mlw = std::getenv("DG_MIXED_LEV_SWEEPS");
+    if (mlw && mlw[0]) c->mixed_lev_sweeps = std::atoi(mlw);
     const char* tv = std::getenv("DG_TMA_VARIANT");
     if (tv && tv[0]) {
       c->tma_variant = std::atoi(tv);
@@ -754,6 +790,38 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
   if ((rc = upload(c.get(), &c->d_x, m->x_ref_in, (size_t)c->B * D * N))) return rc;
   if ((rc = upload_vec(c.get(), &c->d_nbe, nbe))) return rc;
   if ((rc = upload_vec(c.get(), &c->d_nbface, nbface))) return rc;
+  if (D == 3) {
+    // shared-face tables: an interior face belongs to its lower-numbered
+    // element; the tables are left out (five-block copies only) unless every
+    // face pair is reciprocal
+    std::vector<int> fref5((size_t)c->B * (F + 1), -1), sfsrc((size_t)c->B), fid(nf, -1);
+    bool ok = (int64_t)c->B * (F + 1) * 4 < (int64_t)INT32_MAX;
+    for (int64_t e = 0; e < c->B; ++e) {
+      sfsrc[e] = (int)(e * (F + 1));
+      fref5[e * (F + 1)] = (int)(2 * e);
+    }
+    for (int64_t k = 0; ok && k < nf; ++k) {
+      const int64_t e = k / F, nb = nbe[k];
+      if (nb < 0) continue;
+      const int64_t kb = nb * F + nbface[k];
+      if (nb == e || nbe[kb] != e || nbface[kb] != (int)(k % F)) ok = false;
+      else if (e < nb) {
+        fid[k] = (int)(sfsrc.size() - c->B);
+        sfsrc.push_back((int)(e * (F + 1) + 1 + k % F));
+      }
+    }
+    for (int64_t k = 0; ok && k < nf; ++k) {
+      const int64_t e = k / F, nb = nbe[k];
+      if (nb < 0) continue;
+      const int64_t own = e < nb ? k : nb * F + nbface[k];
+      fref5[e * (F + 1) + 1 + k % F] = (int)(2 * (c->B + fid[own]) + (e < nb ? 0 : 1));
+    }
+    if (ok) {
+      c->nface_sh = (int64_t)sfsrc.size() - c->B;
+      if ((rc = upload_vec(c.get(), &c->d_fref5, fref5))) return rc;
+      if ((rc = upload_vec(c.get(), &c->d_sfsrc, sfsrc))) return rc;
+    }
+  }
   if ((rc = upload_vec(c.get(), &c->d_aln, aln))) return rc;
   if ((rc = upload_vec(c.get(), &c->d_bct, bct))) return rc;
   c->kappa.assign(c->B, 1.0);

@@ -114,10 +114,10 @@ class DGSolver:
         return t.data_ptr()
 
     def info(self):
-        out = np.zeros(14, dtype=np.int64)
-        self._chk(self._lib.dg_info(self._ctx, out.ctypes.data, 14))
+        out = np.zeros(15, dtype=np.int64)
+        self._chk(self._lib.dg_info(self._ctx, out.ctypes.data, 15))
         keys = ["ndim", "nloc", "nele", "nonods", "cg_nonods", "ncola", "ncolor", "nlevel", "nbface",
-                "built", "ngi", "sngi", "tma_variant", "batched_tma"]
+                "built", "ngi", "sngi", "tma_variant", "batched_tma", "shared_faces"]
         return dict(zip(keys, out.tolist()))
 
     def close(self):

@@ -110,6 +110,7 @@ def test_bulk_copy_kernels_match_plain_loads(n, monkeypatch):
     FP32 apply agree bit for bit (7^3 * 6 = 2058 tets leaves partial last
     groups of elements)."""
     outs = {}
+    monkeypatch.setenv("DG_SHARED_FACES", "0")
     for tma in ("1", "0"):
         monkeypatch.setenv("DG_BF16_TMA", tma)
         monkeypatch.setenv("DG_F32_TMA", tma)
@@ -125,3 +126,56 @@ def test_bulk_copy_kernels_match_plain_loads(n, monkeypatch):
         outs[tma] = res
     for a, c in zip(outs["1"], outs["0"]):
         assert torch.equal(a, c)
+
+
+@pytest.mark.parametrize("n", [6, 7])
+def test_shared_face_copies_match_five_block_copies(n, monkeypatch):
+    """Each interior face block stored once (read transposed by the
+    neighbour) against five stored blocks per element, both through the
+    bulk-copy kernels.  The operator is symmetric to FP64 rounding, so the
+    reduced-precision copies differ at most by one rounding step in a few
+    entries: FP32 apply within 1e-6, BF16 smoothing step and FP32
+    preconditioner within 1e-4 (relative to the max entry); the mixed solve
+    reaches the same FP64 tolerance with the same solution to 1e-9."""
+    outs = {}
+    for sf in ("1", "0"):
+        monkeypatch.setenv("DG_SHARED_FACES", sf)
+        m, s, f, u = _setup("tet", n, 2, kappa_sigma=0.5, seed=2)
+        g = torch.Generator(device="cuda:0").manual_seed(8)
+        x = torch.randn(s.nonods, dtype=torch.float32, device="cuda:0", generator=g)
+        b = torch.randn(s.nonods, dtype=torch.float32, device="cuda:0", generator=g)
+        res = [s.apply_f32(x), s.smooth_pc(x, b), s.precond_f32(b)]
+        bb = s.rhs(torch.tensor(f, device="cuda:0"))
+        tol = 1e-10 * float(torch.linalg.norm(bb))
+        xm = torch.zeros_like(bb)
+        its, r, outer = s.solve_mixed(xm, bb, tol)
+        assert r <= tol
+        torch.cuda.synchronize()
+        outs[sf] = res + [xm]
+    for (a, c), t in zip(zip(outs["1"], outs["0"]), (1e-6, 1e-4, 1e-4, 1e-9)):
+        err = float(torch.abs(a.double() - c.double()).max() / torch.abs(c.double()).max())
+        assert err < t, (t, err)
+
+
+@pytest.mark.parametrize("cond", ["0", "1"])
+def test_chunk_graphs_match_direct_launches(cond, monkeypatch):
+    """Chunk graphs against direct launches of the inner Arnoldi steps: the
+    solution is bitwise the same.  With the device-side convergence test
+    (cond = 1: Givens update per step, one conditional graph node per step)
+    the graphs skip the steps after the test is met, direct launches run the
+    whole chunk and stop at the same Krylov step, so the graph form runs no
+    more steps."""
+    outs = {}
+    monkeypatch.setenv("DG_COND_GRAPH", cond)
+    for ng in ("1", "0"):
+        monkeypatch.setenv("DG_NO_GRAPH", ng)
+        m, s, f, u = _setup("tet", 8, 2, kappa_sigma=0.5, seed=3)
+        b = s.rhs(torch.tensor(f, device="cuda:0"))
+        tol = 1e-10 * float(torch.linalg.norm(b))
+        x = torch.zeros_like(b)
+        its, res, outer = s.solve_mixed(x, b, tol)
+        assert res <= tol
+        torch.cuda.synchronize()
+        outs[ng] = (x.cpu(), its)
+    assert torch.equal(outs["0"][0], outs["1"][0])
+    assert outs["0"][1] <= outs["1"][1]
