@@ -58,6 +58,8 @@ def parse():
                          "mean (weighted-average SIP); c3 uses harmonic")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--smooth", type=int, default=2, help="V(s,s) smoothing steps")
+    ap.add_argument("--serve-dense-max", type=int, default=1200,
+                    help="c5: rows of the exact coarse solve rebuilt per request")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-roofline", action="store_true", help="skip the isolated apply timing")
@@ -662,7 +664,7 @@ def run_serving(args):
     free, total = torch.cuda.mem_get_info(local)
     t0 = time.perf_counter()
     srv = serving.SolveServer(sizes, hbm_budget=0.5 * free, rtol=1e-10, smooth=args.smooth, device=local,
-                              seed=args.seed)
+                              seed=args.seed, dense_max=args.serve_dense_max)
     reqs = serving.make_requests(sizes, args.requests, args.rate, sigma=0.5, seed=args.seed + 5, meshes=srv.meshes)
     # slots created ahead of traffic (3 per mesh, within the budget), then a
     # warm-up request per mesh
@@ -684,7 +686,10 @@ def run_serving(args):
                                   "to 1e-10, HBM admission budget %.1f GB" % (
                                       len(res), args.rate, args.seed + 5, sizes, srv.hbm_budget / 1e9),
                       "sizes": sizes, "requests": len(res), "rate_per_s": args.rate},
-           "latency": {"p50_s": st["p50_s"], "p99_s": st["p99_s"], "mean_s": st["mean_s"]},
+           "latency": {"p50_s": st["p50_s"], "p99_s": st["p99_s"], "mean_s": st["mean_s"],
+                       "mean_wait_s": st["mean_wait_s"], "mean_build_s": st["mean_build_s"],
+                       "mean_solve_s": st["mean_solve_s"]},
+           "dense_max": srv.dense_max,
            "span_s": st["span_s"], "worst_residual_over_tol": worst,
            "slots": {str(n): len(srv.slots[n]) for n in sizes},
            "slot_footprint_gb": {str(n): srv.footprint.get(n, 0.0) / 1e9 for n in sizes},

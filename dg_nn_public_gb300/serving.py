@@ -65,6 +65,8 @@ class Result:
     arrival: float
     start: float                 # admission time
     end: float                   # completion time (solution on the host)
+    build_s: float = 0.0         # operator rebuild for the request's kappa
+    solve_s: float = 0.0         # mixed solve (incl. its reduced-precision copies and coarse inverse)
 
     @property
     def latency(self) -> float:
@@ -83,13 +85,18 @@ class SolveServer:
     """Continuous-batching server for SIP-DG solves on resident meshes."""
 
     def __init__(self, sizes, hbm_budget: float, rtol: float = 1e-10, face_kappa: str = "harmonic",
-                 smooth: int = 2, device: int = 0, max_slots_per_size: int = 8, seed: int = 0):
+                 smooth: int = 2, device: int = 0, max_slots_per_size: int = 8, seed: int = 0,
+                 dense_max: int = 1200):
         self.sizes = list(sizes)
         self.hbm_budget = float(hbm_budget)
         self.rtol = rtol
         self.face_kappa = face_kappa
         self.device = device
         self.max_slots = max_slots_per_size
+        # exact coarse solve size of the mixed preconditioner: its inverse is
+        # rebuilt per request (Gauss-Jordan, cost ~ rows^3), so a serving slot
+        # keeps it smaller than the library default
+        self.dense_max = dense_max
         self.cfg = SolverConfig(pre_smooth_its=smooth, post_smooth_its=smooth, device=device)
         self.meshes = {}
         self.orders = {}
@@ -109,6 +116,7 @@ class SolveServer:
         torch.cuda.synchronize(self.device)
         free0, _ = torch.cuda.mem_get_info(self.device)
         s = DGSolver(self.meshes[n], self.orders[n], self.cfg, self.el)
+        s.set_mixed_options(dense_max=self.dense_max)
         slot = _Slot(s)
         if n not in self.footprint:
             # warm set-up on a unit-kappa problem measures the slot's footprint
@@ -153,6 +161,7 @@ class SolveServer:
         """Rebuild the slot's operator for the request's kappa and solve."""
         torch = _torch()
         s = slot.solver
+        t0 = time.perf_counter()
         with torch.cuda.stream(slot.stream):
             s.set_kappa(req.kappa)
             s.set_face_kappa(self.face_kappa)
@@ -161,10 +170,12 @@ class SolveServer:
             b = s.rhs(f)
             x = torch.zeros_like(b)
             tol = self.rtol * float(torch.linalg.norm(b))
+            t1 = time.perf_counter()
             its, res, _ = s.solve_mixed(x, b, tol)
             xh = x.cpu()
         slot.stream.synchronize()
-        return xh.numpy(), its, res, tol
+        t2 = time.perf_counter()
+        return xh.numpy(), its, res, tol, t1 - t0, t2 - t1
 
     # -- the serving loop ---------------------------------------------------
     def run(self, requests: List[Request]) -> List[Result]:
@@ -179,10 +190,10 @@ class SolveServer:
 
         def worker(slot: _Slot, req: Request, start: float):
             try:
-                x, its, res, tol = self.solve_one(slot, req)
+                x, its, res, tol, tb, ts = self.solve_one(slot, req)
                 end = time.perf_counter() - t0
                 with self._lock:
-                    results.append(Result(req.rid, req.n, x, its, res, tol, req.arrival, start, end))
+                    results.append(Result(req.rid, req.n, x, its, res, tol, req.arrival, start, end, tb, ts))
             except Exception as exc:  # reported after the run
                 with self._lock:
                     errors.append((req.rid, exc))
@@ -260,4 +271,7 @@ def latency_stats(results: List[Result]) -> dict:
     dofs = sum(r.x.size for r in results)
     return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "mean_s": float(lat.mean()), "requests": len(results), "span_s": float(span),
-            "dofs_per_s": float(dofs / span)}
+            "dofs_per_s": float(dofs / span),
+            "mean_build_s": float(np.mean([r.build_s for r in results])),
+            "mean_solve_s": float(np.mean([r.solve_s for r in results])),
+            "mean_wait_s": float(np.mean([r.start - r.arrival for r in results]))}
