@@ -284,6 +284,188 @@ __global__ void __launch_bounds__(N* N) build_blocks_kernel(BuildParams p) {
 }
 
 // ---------------------------------------------------------------------------
+// Stored-block assembly for straight-sided (affine) elements.  With a
+// constant Jacobian J (inverse M, determinant det), a constant unit normal
+// n_f and area element sdet_f per face, every quadrature sum of the general
+// kernel factors into a geometric coefficient times a reference matrix that
+// is the same for all elements (ftab, formed once per context on the host):
+//   volume   det * sum_{jj,kk} (M^T M)[jj][kk] K[jj][kk]
+//   cs, sc   sdet_f * sum_jj c_f[jj] R[f][jj] (and its transpose),
+//            c_f = M^T n_f
+//   ss       sdet_f * Mf[f]
+//   cnb      sdet_f * sum_jj cn_f[jj] Q[f][fn][al][jj], cn_f = M_nb^T n_f
+//   snbv     sdet_f * sum_jj c_f[jj] P[f][fn][al][jj]
+//   ssnb     sdet_f * S[f][fn][al]
+// with al the face's alignment code and fn the neighbour's local face, so the
+// blocks equal the general kernel's to rounding (tested).  Table layout:
+// K (D*D), R (F*D), Mf (F), Q (F*F*D*D), P (F*F*D*D), S (F*F*D) matrices of
+// N*N doubles, entry (m, n) at [m * N + n].
+template <int D, int N, int F>
+struct FastTab {
+  static constexpr int NN = N * N;
+  static constexpr int K = 0;
+  static constexpr int R = K + D * D * NN;
+  static constexpr int Mf = R + F * D * NN;
+  static constexpr int Q = Mf + F * NN;
+  static constexpr int P = Q + F * F * D * D * NN;
+  static constexpr int S = P + F * F * D * D * NN;
+  static constexpr int Size = S + F * F * D * NN;
+};
+
+template <int D, int N, int F, int VG, int SG>
+__global__ void __launch_bounds__(N* N) build_blocks_affine_kernel(BuildParams p, const double* __restrict__ ftab) {
+  using TB = FastTab<D, N, F>;
+  constexpr int NN = N * N;
+  __shared__ double xe[D * N];
+  __shared__ double xnb[F][D * N];
+  __shared__ double Mi[D * D], C[D * D], det_s;
+  __shared__ double cf[F][D], cn[F][D], sdet[F], gam[F], kf[F];
+  __shared__ int nbi[F], nbfc[F], aln[F], bct[F];
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x;
+  const Tables& T = p.T;
+  for (int k = tid; k < D * N; k += NN) xe[k] = p.x[e * D * N + k];
+  if (tid < F) {
+    const int64_t fi = e * F + tid;
+    nbi[tid] = p.nbe[fi];
+    nbfc[tid] = p.nbface[fi];
+    aln[tid] = p.aln[fi];
+    bct[tid] = p.bct[fi];
+  }
+  __syncthreads();
+  for (int k = tid; k < F * D * N; k += NN) {
+    const int f = k / (D * N), r = k % (D * N);
+    const int nb = nbi[f];
+    xnb[f][r] = nb >= 0 ? p.x[(int64_t)nb * D * N + r] : 0.0;
+  }
+  if (tid == 0) {
+    double j[D * D];
+    jacobian<D, N>(T.nlx, VG, 0, xe, j);
+    const double det = inv_det<D>(j, Mi);
+    det_s = det;
+    if (!(det > 0.0)) atomicExch(p.err, 1);
+#pragma unroll
+    for (int a = 0; a < D; ++a)
+#pragma unroll
+      for (int b = 0; b < D; ++b) {
+        double t = 0.0;
+#pragma unroll
+        for (int i = 0; i < D; ++i) t += Mi[i * D + a] * Mi[i * D + b];
+        C[a * D + b] = t;
+      }
+  }
+  __syncthreads();
+  for (int g = tid; g < VG; g += NN) p.detw[e * VG + g] = det_s * T.weight[g];
+  if (tid < F) {
+    const int f = tid;
+    double j[D * D], nrm[D];
+    jacobian<D, N>(T.nlx, VG, 0, xe, j);
+    const double sd = face_normal<D>(j, T.drst + f * D * (D - 1), nrm);
+    sdet[f] = sd;
+#pragma unroll
+    for (int jj = 0; jj < D; ++jj) {
+      double t = 0.0;
+#pragma unroll
+      for (int i = 0; i < D; ++i) t += Mi[i * D + jj] * nrm[i];
+      cf[f][jj] = t;
+    }
+    double h = 0.0;
+    for (int g = 0; g < SG; ++g) h += sd * T.sweight[g];
+    if (D == 3) h = sqrt(h);
+    gam[f] = p.eta / h;
+    const double ke = p.kappa[e];
+    if (bct[f] < 0) {
+      const int nb = nbi[f];
+      const double kn = nb >= 0 ? p.kappa[nb] : ke;
+      kf[f] = p.mu * (p.face_kappa ? 2.0 * ke * kn / (ke + kn) : 0.5 * (ke + kn));
+    } else if (bct[f] == 0) {
+      kf[f] = p.mu * ke;
+    } else {
+      kf[f] = 0.0;
+    }
+    if (nbi[f] >= 0) {
+      double jn[D * D], mn[D * D];
+      jacobian<D, N>(T.nlx, VG, 0, xnb[f], jn);
+      inv_det<D>(jn, mn);
+#pragma unroll
+      for (int jj = 0; jj < D; ++jj) {
+        double t = 0.0;
+#pragma unroll
+        for (int i = 0; i < D; ++i) t += mn[i * D + jj] * nrm[i];
+        cn[f][jj] = t;
+      }
+    } else {
+#pragma unroll
+      for (int jj = 0; jj < D; ++jj) cn[f][jj] = 0.0;
+    }
+  }
+  __syncthreads();
+  const int m = tid % N, n = tid / N;
+  const int mn_ = m * N + n, nm_ = n * N + m;
+  double vol = 0.0;
+#pragma unroll
+  for (int a = 0; a < D * D; ++a) vol += C[a] * __ldg(ftab + TB::K + a * NN + mn_);
+  double diag = p.mu * p.kappa[e] * det_s * vol;
+  double* out = p.blk + (size_t)e * (F + 1) * N * N;
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    double off = 0.0;
+    if (kf[f] != 0.0) {
+      const bool interior = bct[f] < 0;
+      const double a = interior ? 0.5 : 1.0;
+      double cs = 0.0, sc = 0.0;
+#pragma unroll
+      for (int jj = 0; jj < D; ++jj) {
+        const double* R = ftab + TB::R + (f * D + jj) * NN;
+        cs += cf[f][jj] * __ldg(R + mn_);
+        sc += cf[f][jj] * __ldg(R + nm_);
+      }
+      const double ss = __ldg(ftab + TB::Mf + f * NN + mn_);
+      diag += kf[f] * sdet[f] * (-a * cs - a * sc + gam[f] * ss);
+      if (interior) {
+        const int cmb = (f * F + nbfc[f]) * D + aln[f];
+        double cnb = 0.0, snbv = 0.0;
+#pragma unroll
+        for (int jj = 0; jj < D; ++jj) {
+          cnb += cn[f][jj] * __ldg(ftab + TB::Q + (cmb * D + jj) * NN + mn_);
+          snbv += cf[f][jj] * __ldg(ftab + TB::P + (cmb * D + jj) * NN + mn_);
+        }
+        const double ssnb = __ldg(ftab + TB::S + cmb * NN + mn_);
+        off = kf[f] * sdet[f] * (-0.5 * cnb + 0.5 * snbv - gam[f] * ssnb);
+      }
+    }
+    out[(size_t)(1 + f) * N * N + n * N + m] = off;
+  }
+  out[n * N + m] = diag;
+}
+
+// Largest deviation of the volume-point Jacobians of an element from its
+// first one, relative to the largest entry (0 for straight-sided elements);
+// the maximum over elements goes to *dev (bit pattern of a non-negative
+// double, so an integer maximum orders it).
+template <int D, int N, int VG>
+__global__ void affine_check_kernel(const double* __restrict__ x, const double* __restrict__ nlx, int64_t B,
+                                    unsigned long long* dev) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= B) return;
+  double xe[D * N];
+#pragma unroll
+  for (int k = 0; k < D * N; ++k) xe[k] = x[e * D * N + k];
+  double j0[D * D], j[D * D];
+  jacobian<D, N>(nlx, VG, 0, xe, j0);
+  double big = 0.0, d = 0.0;
+#pragma unroll
+  for (int k = 0; k < D * D; ++k) big = fmax(big, fabs(j0[k]));
+  for (int g = 1; g < VG; ++g) {
+    jacobian<D, N>(nlx, VG, g, xe, j);
+#pragma unroll
+    for (int k = 0; k < D * D; ++k) d = fmax(d, fabs(j[k] - j0[k]));
+  }
+  const double rel = big > 0.0 ? d / big : 1.0;
+  atomicMax(dev, (unsigned long long)__double_as_longlong(rel));
+}
+
+// ---------------------------------------------------------------------------
 // Smoother matrix.  The reference smooths with three point-Jacobi sweeps on
 // each element block, c <- c + w D^-1 (r - A_ee c) from c = 0, then
 // x += w c (z06/volume_mf_diff.py:474-480).  That is the fixed linear map
@@ -319,46 +501,59 @@ __global__ void __launch_bounds__(N* N) smoother_matrix_kernel(const double* __r
 // FP64 without pivoting: A_ee is symmetric positive definite for a
 // sufficient penalty, so every pivot is positive (a non-positive pivot sets
 // the error word and leaves W_e as the Jacobi inverse of the diagonal).
+// One warp per element, lane m holding row m of [A_ee | I] in registers: per
+// pivot one reciprocal, the pivot row broadcast by shuffles, and the row
+// update in FP64 FMAs (FP64 throughput is what bounds this kernel, so the
+// division is taken once per row and pivot, not per entry).
 template <int N, int F>
-__global__ void __launch_bounds__(N* N) block_inverse_kernel(const double* __restrict__ blk,
-                                                             double* __restrict__ W, int64_t B, double w,
-                                                             int* err) {
-  __shared__ double a[N][N + 1];
-  __shared__ double inv[N][N + 1];
-  __shared__ int bad;
-  const int64_t e = blockIdx.x;
-  const int tid = threadIdx.x;
-  const int m = tid % N, n = tid / N;
-  const double* A = blk + (size_t)e * (F + 1) * N * N;
-  a[m][n] = A[n * N + m];
-  inv[m][n] = (m == n) ? 1.0 : 0.0;
-  if (tid == 0) bad = 0;
-  __syncthreads();
-  for (int k = 0; k < N; ++k) {
-    const double piv = a[k][k];
-    if (!(piv > 0.0)) {
-      if (tid == 0) bad = 1;
-      break;   // uniform: every thread reads the same pivot
-    }
-    const double fm = a[m][k] / piv;   // factor of row m
-    const double akn = a[k][n], ikn = inv[k][n];
-    __syncthreads();
-    if (m == k) {
-      a[m][n] = akn / piv;
-      inv[m][n] = ikn / piv;
-    } else {
-      a[m][n] -= fm * akn;
-      inv[m][n] -= fm * ikn;
-    }
-    __syncthreads();
+__global__ void __launch_bounds__(256) block_inverse_kernel(const double* __restrict__ blk, double* __restrict__ W,
+                                                            int64_t B, double w, int* err) {
+  static_assert(N <= 32, "one lane per row");
+  constexpr int WPB = 8;
+  const int lane = threadIdx.x & 31;
+  const int64_t e = (int64_t)blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (e >= B) return;   // whole warp
+  const int m = lane < N ? lane : N - 1;   // lanes >= N repeat the last row, write nothing
+  const double* A = blk + (size_t)e * (F + 1) * N * N;   // A(m, n) at [n * N + m]
+  double a[N], inv[N];
+#pragma unroll
+  for (int n = 0; n < N; ++n) {
+    a[n] = A[n * N + m];
+    inv[n] = (n == m) ? 1.0 : 0.0;
   }
-  __syncthreads();
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    const double piv = __shfl_sync(0xffffffffu, a[k], k);
+    if (!(piv > 0.0)) {   // uniform: every lane holds the same pivot
+      bad = true;
+      break;
+    }
+    const double rp = 1.0 / piv;
+    const double fm = a[k];   // this row's entry in the pivot column
+#pragma unroll
+    for (int n = 0; n < N; ++n) {
+      const double pa = __shfl_sync(0xffffffffu, a[n], k) * rp;
+      const double pi = __shfl_sync(0xffffffffu, inv[n], k) * rp;
+      if (m == k) {
+        a[n] = pa;
+        inv[n] = pi;
+      } else {
+        a[n] = fma(-fm, pa, a[n]);
+        inv[n] = fma(-fm, pi, inv[n]);
+      }
+    }
+  }
+  if (lane >= N) return;
+  double* Wo = W + (size_t)e * N * N;
   if (bad) {
-    if (tid == 0) atomicExch(err, 2);
-    W[(size_t)e * N * N + n * N + m] = (m == n) ? w / A[m * N + m] : 0.0;
+    if (lane == 0) atomicExch(err, 2);
+#pragma unroll
+    for (int n = 0; n < N; ++n) Wo[n * N + m] = (m == n) ? w / A[m * N + m] : 0.0;
     return;
   }
-  W[(size_t)e * N * N + n * N + m] = w * inv[m][n];
+#pragma unroll
+  for (int n = 0; n < N; ++n) Wo[n * N + m] = w * inv[n];
 }
 
 // ---------------------------------------------------------------------------

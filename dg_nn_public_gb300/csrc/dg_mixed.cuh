@@ -67,6 +67,11 @@ struct Mixed {
   // chunk graphs skip the steps after convergence (conditional nodes)
   double* gv = nullptr;
   int* kdone = nullptr;
+  // operator-build scratch kept with the context: FP64 smoother blocks and
+  // the Gauss-Jordan augmented matrix of the dense coarse level
+  double* winv = nullptr;
+  double* gj = nullptr;
+  size_t gj_cap = 0;
   std::vector<double> gv_host;
   std::vector<std::vector<int>> g_kern;
   std::vector<bool> g_cond;
@@ -1163,6 +1168,7 @@ int build_blk5(dg_ctx* c, cudaStream_t st) {
 int build_mixed(dg_ctx* c, cudaStream_t st) {
   Mixed& M = mixed_of(c);
   int rc;
+  const auto t0 = std::chrono::steady_clock::now();
   if ((rc = set_tma_smem<__nv_bfloat16, 6, 2, 3, true>(c)) || (rc = set_tma_smem<__nv_bfloat16, 8, 2, 2, true>(c)) ||
       (rc = set_tma_smem<__nv_bfloat16, 4, 2, 4, true>(c)) || (rc = set_tma_smem<float, 4, 2, 3, false>(c)) ||
       (rc = set_tma_smem<float, 4, 2, 2, true>(c)))
@@ -1192,18 +1198,29 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
   } else if ((rc = build_blk5(c, st))) {
     return rc;
   }
+  auto vt = [&](const char* what) {   // verbose phase timings
+    if (!c->verbose) return;
+    cudaStreamSynchronize(st);
+    std::fprintf(stderr, "[build_mixed] %s done at %.2f ms\n", what,
+                 std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
+  };
+  vt("operator copies");
   // smoother matrices of the mixed preconditioner
   const double* Wsrc = c->d_W;
   double* Winv = nullptr;
   if (c->mixed_smoother == 1) {
-    CK(c, cudaMalloc((void**)&Winv, sizeof(double) * nw));
+    // scratch kept with the context: a cudaFree here would wait for every
+    // stream of the device (other contexts' solves on a serving GPU)
+    if (!M.winv && (rc = dalloc(c, &M.winv, nw))) return rc;
+    Winv = M.winv;
     CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
     if (c->D == 3)
-      block_inverse_kernel<20, 4><<<(unsigned)c->B, 400, 0, st>>>(c->d_blk, Winv, c->B, c->mixed_smooth_w, c->d_err);
+      block_inverse_kernel<20, 4><<<nblk(c->B, 8), 256, 0, st>>>(c->d_blk, Winv, c->B, c->mixed_smooth_w, c->d_err);
     else
-      block_inverse_kernel<10, 3><<<(unsigned)c->B, 100, 0, st>>>(c->d_blk, Winv, c->B, c->mixed_smooth_w, c->d_err);
+      block_inverse_kernel<10, 3><<<nblk(c->B, 8), 256, 0, st>>>(c->d_blk, Winv, c->B, c->mixed_smooth_w, c->d_err);
     bump();
     Wsrc = Winv;
+    vt("block inverses");
   }
   if (c->D == 3 && c->f32_tma)
     convert_f64_f32_chunk20_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W, (int64_t)c->B);
@@ -1222,9 +1239,9 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
     int herr = 0;
     CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(c, cudaStreamSynchronize(st));
-    cudaFree(Winv);
     if (herr) return fail(c, DG_ERR_NUMERIC, "element block with a non-positive pivot (not positive definite)");
   }
+  vt("smoother copies");
   if (M.lev.size() != c->lev.size()) {
     M.lev.assign(c->lev.size(), Lev32());
     for (size_t l = 0; l < c->lev.size(); ++l) {
@@ -1253,6 +1270,8 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
     convert_f64_f32_kernel<<<nblk(D.n, 256), 256, 0, st>>>(D.diag, L.diag, D.n);
     bump();
   }
+  if (c->verbose) CK(c, cudaStreamSynchronize(st));
+  const auto t1 = std::chrono::steady_clock::now();
   // exact coarse solve on the first level with at most dense_max rows
   M.dense_l = -1;
   if (c->dense_max32 > 0) {
@@ -1269,10 +1288,15 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
         for (int64_t k = h.row_ptr[r0 + i]; k < h.row_ptr[r0 + i + 1]; ++k) Gh[(size_t)i * 2 * n + h.col[k]] += h.val[k];
         Gh[(size_t)i * 2 * n + n + i] = 1.0;
       }
-      double *G = nullptr, *fcol = nullptr, *prow = nullptr;
-      CK(c, cudaMalloc((void**)&G, sizeof(double) * Gh.size()));
-      CK(c, cudaMalloc((void**)&fcol, sizeof(double) * n));
-      CK(c, cudaMalloc((void**)&prow, sizeof(double) * 2 * n));
+      // augmented matrix and pivot row / column, kept with the context
+      const size_t gneed = Gh.size() + 3 * (size_t)n;
+      if (M.gj_cap < gneed) {
+        if ((rc = dalloc(c, &M.gj, gneed))) return rc;
+        M.gj_cap = gneed;
+      }
+      double* G = M.gj;
+      double* fcol = G + Gh.size();
+      double* prow = fcol + n;
       CK(c, cudaMemcpyAsync(G, Gh.data(), sizeof(double) * Gh.size(), cudaMemcpyHostToDevice, st));
       CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
       for (int k = 0; k < n; ++k) {
@@ -1289,15 +1313,16 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
       int herr = 0;
       CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
       CK(c, cudaStreamSynchronize(st));
-      cudaFree(G);
-      cudaFree(fcol);
-      cudaFree(prow);
       CKL(c);
       if (herr == 0) M.dense_l = lc;
     }
   }
   CKL(c);
   M.built = true;
+  if (c->verbose)
+    std::fprintf(stderr, "[build_mixed] ms: copies + smoother blocks + levels %.2f, dense coarse inverse (%d rows) %.2f\n",
+                 std::chrono::duration<double, std::milli>(t1 - t0).count(), c->dense_n,
+                 std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count());
   return DG_OK;
 }
 

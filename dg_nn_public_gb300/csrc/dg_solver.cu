@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -61,6 +62,11 @@ struct dg_ctx {
   // when read transposed, -1 on the boundary); d_sfsrc[i] = FP64 source
   // block of shared block i; nface_sh = interior faces
   int *d_fref5 = nullptr, *d_sfsrc = nullptr;
+  // reference matrices of the affine block build; fast_build: -1 not yet
+  // checked, 1 all elements straight-sided, 0 otherwise (quadrature build)
+  double* d_ftab = nullptr;
+  int fast_build = -1;
+  bool general_build = false;
   int64_t nface_sh = 0;
   double* d_kappa = nullptr;
   Tables T{};
@@ -234,9 +240,32 @@ int launch_build(dg_ctx* c, cudaStream_t st) {
   p.B = c->B;
   p.err = c->d_err;
   p.face_kappa = c->face_kappa;
-  auto k = build_blocks_kernel<D, E::N, E::F, E::VG, E::SG>;
-  CK(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm)));
-  if (c->B > 0) k<<<(unsigned)c->B, E::N * E::N, sizeof(Sm), st>>>(p);
+  if (c->fast_build < 0 && c->B > 0) {
+    // straight-sided elements (constant Jacobian) take the table build;
+    // decided once, the coordinates are fixed for the context
+    unsigned long long* dv = nullptr;
+    int rc;
+    if ((rc = dalloc(c, &dv, 1))) return rc;
+    CK(c, cudaMemsetAsync(dv, 0, sizeof(unsigned long long), st));
+    affine_check_kernel<D, E::N, E::VG><<<nblk(c->B, 128), 128, 0, st>>>(c->d_x, c->T.nlx, c->B, dv);
+    bump();
+    unsigned long long hv = 0;
+    CK(c, cudaMemcpyAsync(&hv, dv, sizeof(hv), cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    double rel;
+    std::memcpy(&rel, &hv, sizeof(rel));
+    c->fast_build = rel < 1e-10 ? 1 : 0;
+    if (c->verbose) std::fprintf(stderr, "[dg_build_operator] Jacobian variation %.3e: %s build\n", rel,
+                                 c->fast_build ? "affine" : "quadrature");
+  }
+  if (c->fast_build == 1 && !c->general_build && c->d_ftab) {
+    if (c->B > 0)
+      build_blocks_affine_kernel<D, E::N, E::F, E::VG, E::SG><<<(unsigned)c->B, E::N * E::N, 0, st>>>(p, c->d_ftab);
+  } else {
+    auto k = build_blocks_kernel<D, E::N, E::F, E::VG, E::SG>;
+    CK(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm)));
+    if (c->B > 0) k<<<(unsigned)c->B, E::N * E::N, sizeof(Sm), st>>>(p);
+  }
   bump();
   if (c->B > 0) smoother_matrix_kernel<E::N, E::F><<<(unsigned)c->B, E::N * E::N, 0, st>>>(
       c->d_blk, c->d_W, c->B, c->cfg.jac_wei);
@@ -735,6 +764,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (lh && lh[0]) c->l2_hint = lh[0] != '0';
     const char* sf = std::getenv("DG_SHARED_FACES");
     if (sf && sf[0]) c->shared_faces = sf[0] != '0';
+    const char* gb = std::getenv("DG_BUILD_GENERAL");
+    if (gb && gb[0]) c->general_build = gb[0] != '0';
     const char* cg = std::getenv("DG_COND_GRAPH");
     if (cg && cg[0]) c->cond_graph = cg[0] != '0';
     const char* msw = std::getenv("DG_MIXED_SWEEPS");
@@ -853,6 +884,66 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     int* q;
     if ((rc = upload_vec(c.get(), &q, al))) return rc;
     c->T.align = q;
+    // reference matrices of the straight-sided (affine) block build, entry
+    // (m, n) of each N x N matrix at [m * N + n]: K[jj][kk], R[f][jj], Mf[f],
+    // Q[f][fn][al][jj], P[f][fn][al][jj], S[f][fn][al] (see
+    // build_blocks_affine_kernel)
+    const int NN = N * N;
+    const int nK = D * D, nR = F * D, nM = F, nQ = F * F * D * D, nS = F * F * D;
+    std::vector<double> ft((size_t)(nK + nR + nM + 2 * nQ + nS) * NN, 0.0);
+    double* tK = ft.data();
+    double* tR = tK + (size_t)nK * NN;
+    double* tM = tR + (size_t)nR * NN;
+    double* tQ = tM + (size_t)nM * NN;
+    double* tP = tQ + (size_t)nQ * NN;
+    double* tS = tP + (size_t)nQ * NN;
+    auto nlx = [&](int jj, int n, int g) { return m->nlx[(jj * N + n) * VG + g]; };
+    auto sn = [&](int f, int n, int g) { return m->sn[(f * N + n) * SG + g]; };
+    auto snlx = [&](int f, int jj, int n, int g) { return m->snlx[(size_t)f * D * N * SG + (jj * N + n) * SG + g]; };
+    for (int jj = 0; jj < D; ++jj)
+      for (int kk = 0; kk < D; ++kk)
+        for (int a = 0; a < N; ++a)
+          for (int b = 0; b < N; ++b) {
+            double t = 0.0;
+            for (int g = 0; g < VG; ++g) t += m->weight[g] * nlx(jj, a, g) * nlx(kk, b, g);
+            tK[(size_t)(jj * D + kk) * NN + a * N + b] = t;
+          }
+    for (int f = 0; f < F; ++f)
+      for (int a = 0; a < N; ++a)
+        for (int b = 0; b < N; ++b) {
+          double t = 0.0;
+          for (int g = 0; g < SG; ++g) t += m->sweight[g] * sn(f, a, g) * sn(f, b, g);
+          tM[(size_t)f * NN + a * N + b] = t;
+          for (int jj = 0; jj < D; ++jj) {
+            double r = 0.0;
+            for (int g = 0; g < SG; ++g) r += m->sweight[g] * sn(f, a, g) * snlx(f, jj, b, g);
+            tR[(size_t)(f * D + jj) * NN + a * N + b] = r;
+          }
+        }
+    for (int f = 0; f < F; ++f)
+      for (int fn = 0; fn < F; ++fn)
+        for (int lg = 0; lg < D; ++lg) {
+          const int cmb = (f * F + fn) * D + lg;
+          for (int a = 0; a < N; ++a)
+            for (int b = 0; b < N; ++b) {
+              double ts = 0.0;
+              for (int g = 0; g < SG; ++g) ts += m->sweight[g] * sn(f, a, g) * sn(fn, b, al[lg * SG + g]);
+              tS[(size_t)cmb * NN + a * N + b] = ts;
+              for (int jj = 0; jj < D; ++jj) {
+                double tq = 0.0, tp = 0.0;
+                for (int g = 0; g < SG; ++g) {
+                  const int ag = al[lg * SG + g];
+                  tq += m->sweight[g] * sn(f, a, g) * snlx(fn, jj, b, ag);
+                  tp += m->sweight[g] * snlx(f, jj, a, g) * sn(fn, b, ag);
+                }
+                tQ[(size_t)(cmb * D + jj) * NN + a * N + b] = tq;
+                tP[(size_t)(cmb * D + jj) * NN + a * N + b] = tp;
+              }
+            }
+        }
+    double* dft;
+    if ((rc = upload_vec(c.get(), &dft, ft))) return rc;
+    c->d_ftab = dft;
   }
   if ((rc = dalloc(c.get(), &c->d_blk, (size_t)c->B * (F + 1) * N * N))) return rc;
   if ((rc = dalloc(c.get(), &c->d_W, (size_t)c->B * N * N))) return rc;
@@ -949,11 +1040,16 @@ int dg_build_operator(dg_ctx* c, void* stream) {
   cudaStream_t st = S(stream);
   CK(c, cudaSetDevice(c->dev));
   int rc;
+  const auto t0 = std::chrono::steady_clock::now();
+  auto ms_since = [](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+  };
   CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
   if ((rc = (c->D == 3 ? launch_build<3>(c, st) : launch_build<2>(c, st)))) return rc;
   int herr = 0;
   CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
   CK(c, cudaStreamSynchronize(st));
+  const double t_blocks = ms_since(t0);
   if (herr) return fail(c, DG_ERR_MESH, "non-positive element Jacobian (element not positively oriented)");
   c->built = true;   // blocks are usable from here on (the probes below apply them)
   ++c->build_version;
@@ -972,11 +1068,13 @@ int dg_build_operator(dg_ctx* c, void* stream) {
   c->rar_host.assign(c->cola.size(), 0.0);
   CK(c, cudaMemcpyAsync(c->rar_host.data(), c->d_rar, sizeof(double) * c->cola.size(), cudaMemcpyDeviceToHost, st));
   CK(c, cudaStreamSynchronize(st));
+  const double t_probes = ms_since(t0);
   // SFC levels (compact_fcode.f90 + get_a_diaga)
   SfcHierarchy& h = c->sfc_h;
   h = SfcHierarchy();
   if ((rc = sfc_levels(c->ncg, c->fina.data(), c->cola.data(), c->rar_host.data(), c->sfc.data(), h)))
     return fail(c, rc, g_thread_error);
+  const double t_sfc = ms_since(t0);
   // (re)allocate the device levels
   if (c->lev.size() != (size_t)h.nlevel) {
     c->lev.assign(h.nlevel, DevLevel());
@@ -1042,6 +1140,9 @@ int dg_build_operator(dg_ctx* c, void* stream) {
     CK(c, cudaMemcpyAsync(L.diag, dg.data(), sizeof(double) * dg.size(), cudaMemcpyHostToDevice, st));
   }
   CK(c, cudaStreamSynchronize(st));
+  if (c->verbose)
+    std::fprintf(stderr, "[dg_build_operator] ms: blocks %.2f, colour probes %.2f, SFC levels (host) %.2f, "
+                 "level upload %.2f\n", t_blocks, t_probes - t_blocks, t_sfc - t_probes, ms_since(t0) - t_sfc);
   return DG_OK;
 }
 

@@ -113,7 +113,8 @@ class SolveServer:
     # -- slots ------------------------------------------------------------
     def _new_slot(self, n: int) -> _Slot:
         torch = _torch()
-        torch.cuda.synchronize(self.device)
+        # no device-wide synchronize: other slots may be capturing CUDA graphs
+        # on their streams, and a device synchronize during a capture fails
         free0, _ = torch.cuda.mem_get_info(self.device)
         s = DGSolver(self.meshes[n], self.orders[n], self.cfg, self.el)
         s.set_mixed_options(dense_max=self.dense_max)
