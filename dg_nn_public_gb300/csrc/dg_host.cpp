@@ -10,6 +10,9 @@
 
 #include "dg_internal.h"
 
+#include <atomic>
+#include <thread>
+
 namespace dg {
 
 thread_local std::string g_thread_error;
@@ -133,44 +136,55 @@ int sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double
     sz = (sz - 1) / 2 + 1;
   }
   int64_t total = h.start.back();
-  h.row_ptr.assign(total + 1, 0);
-  h.col.clear();
-  h.val.clear();
-  std::vector<int64_t> slot(total, -1);   // coarse column -> entry of the current row
-  for (int l = 0; l < h.nlevel; ++l) {
-    int64_t nc = h.sizes[l];
-    int64_t disp = h.start[l];
-    int64_t row_begin = (int64_t)h.col.size();
-    int64_t cur_row = -1;
+  // the levels are independent (each is summed from the fine matrix in curve
+  // order), so they are formed on parallel host threads
+  struct Lv {
+    std::vector<int64_t> rp, col;
+    std::vector<double> val;
+  };
+  std::vector<Lv> lv(h.nlevel);
+  auto build_level = [&](int l) {
+    Lv& L = lv[l];
+    const int64_t nc = h.sizes[l];
+    L.rp.assign(nc + 1, 0);
+    std::vector<int64_t> slot(nc, -1);   // coarse column -> entry of the current row
     std::vector<int64_t> touched;
+    int64_t cur_row = -1;
     for (int64_t s = 0; s < n; ++s) {
-      int64_t ic = s >> l;
+      const int64_t ic = s >> l;
       if (ic != cur_row) {
         for (int64_t t : touched) slot[t] = -1;
         touched.clear();
-        if (cur_row >= 0) h.row_ptr[disp + cur_row + 1] = (int64_t)h.col.size();
-        for (int64_t r = cur_row + 1; r < ic; ++r) h.row_ptr[disp + r + 1] = (int64_t)h.col.size();
+        if (cur_row >= 0) L.rp[cur_row + 1] = (int64_t)L.col.size();
+        for (int64_t r = cur_row + 1; r < ic; ++r) L.rp[r + 1] = (int64_t)L.col.size();
         cur_row = ic;
-        h.row_ptr[disp + ic] = (int64_t)h.col.size();
+        L.rp[ic] = (int64_t)L.col.size();
       }
-      int64_t node = inv[s];
+      const int64_t node = inv[s];
       for (int64_t k = fina[node]; k < fina[node + 1]; ++k) {
-        int64_t jc = pos[cola[k]] >> l;
+        const int64_t jc = pos[cola[k]] >> l;
         int64_t& sl = slot[jc];
         if (sl >= 0) {
-          h.val[sl] += a[k];
+          L.val[sl] += a[k];
         } else {
-          sl = (int64_t)h.col.size();
+          sl = (int64_t)L.col.size();
           touched.push_back(jc);
-          h.col.push_back(jc);
-          h.val.push_back(a[k]);
+          L.col.push_back(jc);
+          L.val.push_back(a[k]);
         }
       }
     }
-    for (int64_t t : touched) slot[t] = -1;
-    if (cur_row >= 0) h.row_ptr[disp + cur_row + 1] = (int64_t)h.col.size();
-    (void)nc;
-    (void)row_begin;
+    if (cur_row >= 0) L.rp[cur_row + 1] = (int64_t)L.col.size();
+  };
+  parallel_for(h.nlevel, build_level);
+  h.row_ptr.assign(total + 1, 0);
+  h.col.clear();
+  h.val.clear();
+  for (int l = 0; l < h.nlevel; ++l) {
+    const int64_t off = (int64_t)h.col.size();
+    for (int64_t i = 0; i <= h.sizes[l]; ++i) h.row_ptr[h.start[l] + i] = off + lv[l].rp[i];
+    h.col.insert(h.col.end(), lv[l].col.begin(), lv[l].col.end());
+    h.val.insert(h.val.end(), lv[l].val.begin(), lv[l].val.end());
   }
   return DG_OK;
 }

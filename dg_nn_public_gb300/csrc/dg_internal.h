@@ -3,6 +3,9 @@
 #include <array>
 #include <cstdint>
 #include <string>
+#include <algorithm>
+#include <atomic>
+#include <thread>
 #include <vector>
 
 #include "../../include/dgsip.h"
@@ -20,6 +23,25 @@ struct SfcHierarchy {
   std::vector<int64_t> col;       // level-local column index
   std::vector<double> val;
 };
+
+// Runs fn(0) .. fn(count - 1) on up to hardware_concurrency() host threads
+// (independent items, taken in order from a shared counter).
+template <typename Fn>
+void parallel_for(int count, Fn fn) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = (int)std::min<unsigned>(hw, (unsigned)std::max(count, 0));
+  if (nt <= 1) {
+    for (int i = 0; i < count; ++i) fn(i);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back([&] {
+      for (int i = next.fetch_add(1); i < count; i = next.fetch_add(1)) fn(i);
+    });
+  for (auto& x : th) x.join();
+}
 
 int p1cg_sparsity(int64_t nele, int ncorner, const int64_t* p1cg, int64_t n,
                   std::vector<int64_t>& fina, std::vector<int64_t>& cola);

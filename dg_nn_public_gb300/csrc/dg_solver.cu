@@ -1110,34 +1110,48 @@ int dg_build_operator(dg_ctx* c, void* stream) {
     }
   }
   choose_vcycle_cluster(c);
-  for (int l = 0; l < h.nlevel; ++l) {
-    DevLevel& L = c->lev[l];
-    int64_t r0 = h.start[l];
-    int64_t base = h.row_ptr[r0];
-    int64_t nnz = h.row_ptr[h.start[l + 1]] - base;
-    std::vector<int> rp(L.n + 1), cl(nnz);
-    std::vector<double> vl(nnz), dg(L.n, 0.0);
-    // sort each row by column (torch CSR from COO), take the diagonal
-    for (int i = 0; i < L.n; ++i) {
-      int64_t a = h.row_ptr[r0 + i], b = h.row_ptr[r0 + i + 1];
-      std::vector<std::pair<int64_t, double>> row;
+  // rows sorted by column (torch CSR from COO) and the diagonal taken, level
+  // by level on parallel host threads; then the uploads in level order
+  struct Up {
+    std::vector<int> rp, cl;
+    std::vector<double> vl, dg;
+  };
+  std::vector<Up> ups(h.nlevel);
+  parallel_for(h.nlevel, [&](int l) {
+    Up& U = ups[l];
+    const int n = (int)h.sizes[l];
+    const int64_t r0 = h.start[l];
+    const int64_t base = h.row_ptr[r0];
+    const int64_t nnz = h.row_ptr[h.start[l + 1]] - base;
+    U.rp.resize(n + 1);
+    U.cl.resize(nnz);
+    U.vl.resize(nnz);
+    U.dg.assign(n, 0.0);
+    std::vector<std::pair<int64_t, double>> row;
+    for (int i = 0; i < n; ++i) {
+      const int64_t a = h.row_ptr[r0 + i], b = h.row_ptr[r0 + i + 1];
+      row.clear();
       for (int64_t k = a; k < b; ++k) row.emplace_back(h.col[k], h.val[k]);
-      std::sort(row.begin(), row.end(), [](auto& x, auto& y) { return x.first < y.first; });
-      rp[i] = (int)(a - base);
+      std::sort(row.begin(), row.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+      U.rp[i] = (int)(a - base);
       for (size_t k = 0; k < row.size(); ++k) {
-        cl[a - base + k] = (int)row[k].first;
-        vl[a - base + k] = row[k].second;
-        if (row[k].first == i) dg[i] = row[k].second;
+        U.cl[a - base + k] = (int)row[k].first;
+        U.vl[a - base + k] = row[k].second;
+        if (row[k].first == i) U.dg[i] = row[k].second;
       }
     }
-    rp[L.n] = (int)nnz;
+    U.rp[n] = (int)nnz;
+  });
+  for (int l = 0; l < h.nlevel; ++l) {
+    DevLevel& L = c->lev[l];
+    const Up& U = ups[l];
     // on the context's stream: no legacy-stream copy that would wait for
     // other streams (several contexts serve concurrently); copies from
     // pageable memory return once the source has been staged
-    CK(c, cudaMemcpyAsync(L.rowptr, rp.data(), sizeof(int) * rp.size(), cudaMemcpyHostToDevice, st));
-    CK(c, cudaMemcpyAsync(L.col, cl.data(), sizeof(int) * cl.size(), cudaMemcpyHostToDevice, st));
-    CK(c, cudaMemcpyAsync(L.val, vl.data(), sizeof(double) * vl.size(), cudaMemcpyHostToDevice, st));
-    CK(c, cudaMemcpyAsync(L.diag, dg.data(), sizeof(double) * dg.size(), cudaMemcpyHostToDevice, st));
+    CK(c, cudaMemcpyAsync(L.rowptr, U.rp.data(), sizeof(int) * U.rp.size(), cudaMemcpyHostToDevice, st));
+    CK(c, cudaMemcpyAsync(L.col, U.cl.data(), sizeof(int) * U.cl.size(), cudaMemcpyHostToDevice, st));
+    CK(c, cudaMemcpyAsync(L.val, U.vl.data(), sizeof(double) * U.vl.size(), cudaMemcpyHostToDevice, st));
+    CK(c, cudaMemcpyAsync(L.diag, U.dg.data(), sizeof(double) * U.dg.size(), cudaMemcpyHostToDevice, st));
   }
   CK(c, cudaStreamSynchronize(st));
   if (c->verbose)
