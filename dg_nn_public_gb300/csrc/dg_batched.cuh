@@ -56,7 +56,8 @@ __global__ void __launch_bounds__(128) bres_kernel(const MT* __restrict__ blk, c
                                                    const int* __restrict__ nbe, const float* __restrict__ x,
                                                    const float* __restrict__ b, float* __restrict__ r,
                                                    float* __restrict__ x_out, int64_t B, int flags,
-                                                   const double* __restrict__ P, float* __restrict__ r1) {
+                                                   const double* __restrict__ P, float* __restrict__ r1,
+                                                   float ws) {
   constexpr int N = 20, F = 4;
   constexpr int BLK = N * N;                     // entries per block
   constexpr int EL_BYTES = (F + 1) * BLK * (int)sizeof(MT);
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(128) bres_kernel(const MT* __restrict__ blk, c
 #pragma unroll
       for (int i = 0; i < 5; ++i) {
         const int64_t o = (e * N + m0 + i) * kNR + r0;
-        float2 xo = make_float2(c[i][0], c[i][1]);
+        float2 xo = make_float2(ws * c[i][0], ws * c[i][1]);
         if (!zerox) {
           xo.x += xs[0][m0 + i][r0];
           xo.y += xs[0][m0 + i][r0 + 1];
@@ -305,7 +306,8 @@ __global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat1
                                                        const int* __restrict__ nbe, const float* __restrict__ x,
                                                        const float* __restrict__ b, float* __restrict__ r,
                                                        float* __restrict__ x_out, int64_t B, int flags,
-                                                       const double* __restrict__ P, float* __restrict__ r1) {
+                                                       const double* __restrict__ P, float* __restrict__ r1,
+                                                       float ws) {
   constexpr int N = 20, F = 4;
   __shared__ __align__(16) unsigned char As[(F + 1) * 800];
   __shared__ __align__(16) unsigned char Ws[800];
@@ -446,7 +448,8 @@ __global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat1
           const int q = rbase + nt * 8 + 2 * t;
           const int64_t o = (e * N + row) * kNR + q;
           const float2 xv = xpre[mt][hh][nt];
-          *reinterpret_cast<float2*>(x_out + o) = make_float2(c2[mt][nt][2 * hh] + xv.x, c2[mt][nt][2 * hh + 1] + xv.y);
+          *reinterpret_cast<float2*>(x_out + o) =
+              make_float2(ws * c2[mt][nt][2 * hh] + xv.x, ws * c2[mt][nt][2 * hh + 1] + xv.y);
         }
       }
   }
@@ -474,7 +477,7 @@ constexpr int kBT = 256;                                 // threads: 8 warps, wa
 __global__ void __launch_bounds__(kBT, kBS) bres_mma_tma_kernel(
     const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
     const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
-    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err) {
+    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, float ws) {
   constexpr int N = 20, F = 4;
   extern __shared__ __align__(128) unsigned char bsm[];
   unsigned char* stages = bsm;
@@ -633,7 +636,7 @@ __global__ void __launch_bounds__(kBT, kBS) bres_mma_tma_kernel(
             for (int nt = 0; nt < 1; ++nt) {
               const int q = rbase + nt * 8 + 2 * t;
               const int64_t o = (e * N + row) * kNR + q;
-              float2 xo = make_float2(c2[mt][nt][2 * hh], c2[mt][nt][2 * hh + 1]);
+              float2 xo = make_float2(ws * c2[mt][nt][2 * hh], ws * c2[mt][nt][2 * hh + 1]);
               if (!zerox) {
                 const float2 xv = *reinterpret_cast<const float2*>(xst + row * kNR + q);
                 xo.x += xv.x;
@@ -1062,9 +1065,9 @@ int ensure_batch(dg_ctx* c, int m) {
 
 template <typename MT>
 int bres(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out, int flags,
-         float* r1, cudaStream_t st) {
+         float* r1, cudaStream_t st, float ws = 1.0f) {
   if (c->B > 0)
-    bres_kernel<MT><<<(unsigned)c->B, 128, 0, st>>>(blk, W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, r1);
+    bres_kernel<MT><<<(unsigned)c->B, 128, 0, st>>>(blk, W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, r1, ws);
   bump();
   CKL(c);
   return DG_OK;
@@ -1080,12 +1083,14 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   float* cur = S.t3;
   float* other = S.t4;
   const bool bf = c->precond_bf16;
-  auto pc = [&](const float* xx, float* xo, int flags, float* rr1) -> int {
+  // DG-level smoothing step k damped like the single-RHS preconditioner
+  auto wsk = [&](int k) { return (nsm == 2 || c->omegas_set) && k < 4 ? c->mixed_wscale[k] : 1.0f; };
+  auto pc = [&](const float* xx, float* xo, int flags, float* rr1, float ws) -> int {
     if (bf && c->batched_mma && c->batched_tma) {
       const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kBS);
       if (g)
         bres_mma_tma_kernel<<<g, kBT, kBDyn, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B, flags, c->T.P,
-                                                   rr1, c->d_err);
+                                                   rr1, c->d_err, ws);
       bump();
       CKL(c);
       return (int)DG_OK;
@@ -1094,24 +1099,24 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
       if (c->B > 0) {
         if (c->batched_warps == 8)
           bres_mma_kernel<8><<<(unsigned)c->B, 256, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B,
-                                                             flags, c->T.P, rr1);
+                                                             flags, c->T.P, rr1, ws);
         else
           bres_mma_kernel<4><<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B,
-                                                             flags, c->T.P, rr1);
+                                                             flags, c->T.P, rr1, ws);
       }
       bump();
       CKL(c);
       return (int)DG_OK;
     }
-    return bf ? bres<__nv_bfloat16>(c, M.blk16, M.W16, xx, r, nullptr, xo, flags, rr1, st)
-              : bres<float>(c, M.blk, M.W, xx, r, nullptr, xo, flags, rr1, st);
+    return bf ? bres<__nv_bfloat16>(c, M.blk16, M.W16, xx, r, nullptr, xo, flags, rr1, st, ws)
+              : bres<float>(c, M.blk, M.W, xx, r, nullptr, xo, flags, rr1, st, ws);
   };
-  if ((rc = pc(nullptr, cur, RF_ZEROX | RF_SMOOTH, nullptr))) return rc;
+  if ((rc = pc(nullptr, cur, RF_ZEROX | RF_SMOOTH, nullptr, wsk(0)))) return rc;
   for (int it = 1; it < nsm; ++it) {
-    if ((rc = pc(cur, other, RF_SMOOTH, nullptr))) return rc;
+    if ((rc = pc(cur, other, RF_SMOOTH, nullptr, wsk(it)))) return rc;
     std::swap(cur, other);
   }
-  if ((rc = pc(cur, nullptr, RF_RESTRICT, S.r1))) return rc;
+  if ((rc = pc(cur, nullptr, RF_RESTRICT, S.r1, 1.0f))) return rc;
   bgather_kernel<<<(unsigned)c->ncg, kNR, 0, st>>>(S.r1, c->d_gptr, c->d_gent, c->d_wdg, c->d_pos, S.lr[0],
                                                    (int)c->ncg);
   bump();
@@ -1149,7 +1154,7 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   bump();
   for (int it = 0; it < nsm; ++it) {
     float* out = (it == nsm - 1) ? z : other;
-    if ((rc = pc(cur, out, RF_SMOOTH, nullptr))) return rc;
+    if ((rc = pc(cur, out, RF_SMOOTH, nullptr, wsk(nsm - 1 - it)))) return rc;
     other = cur;
     cur = out;
   }

@@ -583,7 +583,7 @@ __global__ void __launch_bounds__(EPB* N) residual_kernel(const MT* __restrict__
                                                           VT* __restrict__ r,
                                                           VT* __restrict__ x_out, int64_t B,
                                                           int flags, const double* __restrict__ P = nullptr,
-                                                          VT* __restrict__ r1 = nullptr) {
+                                                          VT* __restrict__ r1 = nullptr, AT wscale = (AT)1) {
   __shared__ AT xs[EPB][F + 1][N];
   __shared__ AT rs[EPB][N];
   __shared__ int nbs[EPB][F];
@@ -642,7 +642,7 @@ __global__ void __launch_bounds__(EPB* N) residual_kernel(const MT* __restrict__
       AT c = 0;
 #pragma unroll
       for (int n = 0; n < N; ++n) c += (AT)We[n * N + m] * rs[le][n];
-      x_out[e * N + m] = (VT)((zerox ? (AT)0 : xs[le][0][m]) + c);
+      x_out[e * N + m] = (VT)((zerox ? (AT)0 : xs[le][0][m]) + wscale * c);
     }
   }
 }

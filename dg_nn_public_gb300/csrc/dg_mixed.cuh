@@ -266,7 +266,7 @@ template <int EPB>
 __global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
     const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
     const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
-    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1) {
+    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, float wscale) {
   constexpr int N = 20, F = 4;
   __shared__ float xs[EPB][F + 1][N];
   __shared__ float rs[EPB][N];
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
   if (smooth) {
     rs[le][m] = res;
     __syncthreads();
-    if (valid) x_out[e * N + m] = (zerox ? 0.0f : xs[le][0][m]) + dot_row20(wq, rs[le], 0.0f);
+    if (valid) x_out[e * N + m] = (zerox ? 0.0f : xs[le][0][m]) + wscale * dot_row20(wq, rs[le], 0.0f);
   }
 }
 
@@ -522,7 +522,8 @@ template <typename MT, int EPB, int S, int MINB, bool WITH_W, bool SF>
 __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     const MT* __restrict__ blk, const MT* __restrict__ W, const int* __restrict__ nbe, const float* __restrict__ x,
     const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out, int64_t B, int flags,
-    const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const int* __restrict__ fref5) {
+    const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const int* __restrict__ fref5,
+    float wscale) {
   constexpr int N = 20, F = 4;
   using G = TmaGroup<MT, EPB, WITH_W>;
   using C = Chunk20<MT>;
@@ -709,7 +710,7 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
       }
       if (smooth && valid)
         x_out[e * N + m] = (zerox ? 0.0f : xs[le][0][m]) +
-                           C::dot(C::lds(sp + G::ABytes + (size_t)le * G::BlockBytes, m), rs[le], 0.0f);
+                           wscale * C::dot(C::lds(sp + G::ABytes + (size_t)le * G::BlockBytes, m), rs[le], 0.0f);
     }
     __syncthreads();   // stage s and xs / rs free again
     if (tid < 32) {
@@ -731,7 +732,7 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
 // face, addressed through c->d_fref5); otherwise five blocks per element
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
 int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out,
-               int flags, float* r1, cudaStream_t st, bool sf) {
+               int flags, float* r1, cudaStream_t st, bool sf, float wscale = 1.0f) {
   if (c->l2_hint) flags |= RF_STREAM_HINT;
   const int64_t ngroups = (c->B + EPB - 1) / EPB;
   const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
@@ -739,10 +740,10 @@ int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const floa
   if (sf)
     return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W, true>, g, EPB * 20, smem, st, blk, W,
                     (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const double*)c->T.P, r1,
-                    (int*)c->d_err, (const int*)c->d_fref5);
+                    (int*)c->d_err, (const int*)c->d_fref5, wscale);
   return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W, false>, g, EPB * 20, smem, st, blk, W,
                   (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const double*)c->T.P, r1,
-                  (int*)c->d_err, (const int*)nullptr);
+                  (int*)c->d_err, (const int*)nullptr, wscale);
 }
 
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
@@ -763,12 +764,12 @@ int set_tma_smem(dg_ctx* c) {
 constexpr int kTmaVariants = 3;
 
 int launch_bf16_tma(dg_ctx* c, Mixed& M, const float* x, const float* b, float* r, float* x_out, int flags,
-                    cudaStream_t st) {
+                    cudaStream_t st, float ws = 1.0f) {
   const __nv_bfloat16* A = M.sf ? M.sblk16 : M.blk16;
   switch (c->tma_variant) {
-    case 1: return launch_tma<__nv_bfloat16, 8, 2, 2, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf);
-    case 2: return launch_tma<__nv_bfloat16, 4, 2, 4, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf);
-    default: return launch_tma<__nv_bfloat16, 6, 2, 3, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf);
+    case 1: return launch_tma<__nv_bfloat16, 8, 2, 2, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws);
+    case 2: return launch_tma<__nv_bfloat16, 4, 2, 4, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws);
+    default: return launch_tma<__nv_bfloat16, 6, 2, 3, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws);
   }
 }
 
@@ -835,63 +836,68 @@ void destroy_mixed(dg_ctx* c) {
 
 template <int D>
 int launch_residual32(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags,
-                      cudaStream_t st) {
+                      cudaStream_t st, float ws = 1.0f) {
   using E = Elem<D>;
   Mixed& M = mixed_of(c);
   if (D == 3 && c->f32_tma) {   // chunked FP32 copy, bulk-copy kernel
     const float* A = M.sf ? M.sblk32 : M.blk;
-    if (flags & RF_SMOOTH) return launch_tma<float, 4, 2, 2, true>(c, A, M.W, x, b, r, x_out, flags, M.r1, st, M.sf);
+    if (flags & RF_SMOOTH)
+      return launch_tma<float, 4, 2, 2, true>(c, A, M.W, x, b, r, x_out, flags, M.r1, st, M.sf, ws);
     return launch_tma<float, 4, 2, 3, false>(c, A, M.W, x, b, r, x_out, flags, M.r1, st, M.sf);
   }
   unsigned g = nblk(c->B, E::EPB);
   if (g)
     residual_kernel<E::N, E::F, E::EPB, float, float, float><<<g, E::EPB * E::N, 0, st>>>(
-        M.blk, M.W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, M.r1);
+        M.blk, M.W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, M.r1, ws);
   bump();
   CKL(c);
   return DG_OK;
 }
 
-int residual32(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags, cudaStream_t st) {
-  return c->D == 3 ? launch_residual32<3>(c, x, b, r, x_out, flags, st)
-                   : launch_residual32<2>(c, x, b, r, x_out, flags, st);
+int residual32(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags, cudaStream_t st,
+               float ws = 1.0f) {
+  return c->D == 3 ? launch_residual32<3>(c, x, b, r, x_out, flags, st, ws)
+                   : launch_residual32<2>(c, x, b, r, x_out, flags, st, ws);
 }
 
 // residual / smoothing with the BF16 block copies (FP32 vectors and sums)
 template <int D>
 int launch_residual16(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags,
-                      cudaStream_t st) {
+                      cudaStream_t st, float ws = 1.0f) {
   using E = Elem<D>;
   Mixed& M = mixed_of(c);
   unsigned g = nblk(c->B, E::EPB);
   if (g)
     residual_kernel<E::N, E::F, E::EPB, __nv_bfloat16, float, float><<<g, E::EPB * E::N, 0, st>>>(
-        M.blk16, M.W16, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, M.r1);
+        M.blk16, M.W16, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, M.r1, ws);
   bump();
   CKL(c);
   return DG_OK;
 }
 
 // residual in the preconditioner: BF16 blocks when enabled, FP32 otherwise
-int residual_pc(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags, cudaStream_t st) {
+// ws scales the smoother's correction of this step (x_out = x + ws W_e res):
+// with W_e = w A_ee^-1 the step is damped by ws * w
+int residual_pc(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags, cudaStream_t st,
+                float ws = 1.0f) {
   if (c->precond_bf16) {
     if (c->D == 3 && c->bf16_tma) {
       Mixed& M = mixed_of(c);
-      return launch_bf16_tma(c, M, x, b, r, x_out, flags, st);
+      return launch_bf16_tma(c, M, x, b, r, x_out, flags, st, ws);
     }
     if (c->D == 3) {
       Mixed& M = mixed_of(c);
       unsigned g = nblk(c->B, 8);
       if (g)
         residual_bf16c20_kernel<8><<<g, 8 * 20, 0, st>>>(M.blk16, M.W16, c->d_nbe, x, b, r, x_out, c->B, flags,
-                                                          c->T.P, M.r1);
+                                                          c->T.P, M.r1, ws);
       bump();
       CKL(c);
       return DG_OK;
     }
-    return launch_residual16<2>(c, x, b, r, x_out, flags, st);
+    return launch_residual16<2>(c, x, b, r, x_out, flags, st, ws);
   }
-  return residual32(c, x, b, r, x_out, flags, st);
+  return residual32(c, x, b, r, x_out, flags, st, ws);
 }
 
 // P1 -> P3 prolongation of the coarse correction (mixed path, 3D):
@@ -1102,10 +1108,13 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   const int nsm = c->mixed_sweeps >= 0 ? c->mixed_sweeps : c->cfg.pre_smooth_its;
   float* cur = M.t3;
   float* other = M.t4;
+  // per-step damping: pre-smoothing steps k = 0, 1, ... use ws[k], the
+  // post-smoothing steps the same factors in reverse order
+  auto ws = [&](int k) { return (nsm == 2 || c->omegas_set) && k < 4 ? c->mixed_wscale[k] : 1.0f; };
   if (nsm > 0) {
-    if ((rc = residual_pc(c, nullptr, r, nullptr, cur, RF_ZEROX | RF_SMOOTH, st))) return rc;
+    if ((rc = residual_pc(c, nullptr, r, nullptr, cur, RF_ZEROX | RF_SMOOTH, st, ws(0)))) return rc;
     for (int it = 1; it < nsm; ++it) {
-      if ((rc = residual_pc(c, cur, r, nullptr, other, RF_SMOOTH, st))) return rc;
+      if ((rc = residual_pc(c, cur, r, nullptr, other, RF_SMOOTH, st, ws(it)))) return rc;
       std::swap(cur, other);
     }
   } else {
@@ -1120,7 +1129,7 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   if ((rc = transfer32(c, nullptr, nullptr, cur, M.lev[0].e, st))) return rc;
   for (int it = 0; it < nsm; ++it) {
     float* out = (it == nsm - 1) ? z : other;
-    if ((rc = residual_pc(c, cur, r, nullptr, out, RF_SMOOTH, st))) return rc;
+    if ((rc = residual_pc(c, cur, r, nullptr, out, RF_SMOOTH, st, ws(nsm - 1 - it)))) return rc;
     other = cur;
     cur = out;
   }

@@ -127,6 +127,15 @@ struct dg_ctx {
   // correction and Jacobi sweeps on the SFC levels (-1 = the configured
   // pre_smooth_its, as in the FP64 preconditioner)
   int mixed_sweeps = -1, mixed_lev_sweeps = -1;
+  // mixed preconditioner with two DG-level smoothing steps: step k damped by
+  // mixed_smooth_w * mixed_wscale[k] (pre-smoothing k = 0, 1; post-smoothing
+  // in reverse), a degree-2 polynomial smoother with roots 1/0.7 and 1/1.4
+  // at the default w = 0.8.  c2: 100 -> 90 inner iterations (30.4 -> 27.4
+  // ms), c3: 120 -> 110; damping pairs (0.5-0.85, 1.2-1.7) all gave 90 on
+  // c2, uniform 0.8 / 0.9 and (1.0, 0.7) gave 100.  Other step counts take
+  // the uniform damping w.
+  float mixed_wscale[4] = {0.875f, 1.75f, 1.0f, 1.0f};
+  bool omegas_set = false;   // DG_MIXED_OMEGAS given: its factors for any step count
   // mixed inner FGMRES: per-step convergence test on the device, chunk
   // graphs with one conditional node per step (c2: 100 -> 98 inner steps,
   // but 30.5 -> 31.4 ms: the stops land where the chunk checks already did
@@ -768,6 +777,19 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (gb && gb[0]) c->general_build = gb[0] != '0';
     const char* cg = std::getenv("DG_COND_GRAPH");
     if (cg && cg[0]) c->cond_graph = cg[0] != '0';
+    const char* om = std::getenv("DG_MIXED_OMEGAS");   // absolute damping per step, "w0,w1,..."
+    if (om && om[0]) {
+      c->omegas_set = true;
+      for (float& v : c->mixed_wscale) v = 1.0f;
+      const char* q = om;
+      for (int k = 0; k < 4 && *q; ++k) {
+        char* end = nullptr;
+        const double v = std::strtod(q, &end);
+        if (end == q) break;
+        c->mixed_wscale[k] = (float)(v / c->mixed_smooth_w);
+        q = (*end == ',') ? end + 1 : end;
+      }
+    }
     const char* msw = std::getenv("DG_MIXED_SWEEPS");
     if (msw && msw[0]) c->mixed_sweeps = std::atoi(msw);
     const char* mlw = std::getenv("DG_MIXED_LEV_SWEEPS");
