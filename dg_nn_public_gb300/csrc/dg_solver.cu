@@ -129,18 +129,23 @@ struct dg_ctx {
   int mixed_sweeps = -1, mixed_lev_sweeps = -1;
   // mixed preconditioner with two DG-level smoothing steps: step k damped by
   // mixed_smooth_w * mixed_wscale[k] (pre-smoothing k = 0, 1; post-smoothing
-  // in reverse), a degree-2 polynomial smoother with roots 1/0.7 and 1/1.4
-  // at the default w = 0.8.  c2: 100 -> 90 inner iterations (30.4 -> 27.4
-  // ms), c3: 120 -> 110; damping pairs (0.5-0.85, 1.2-1.7) all gave 90 on
-  // c2, uniform 0.8 / 0.9 and (1.0, 0.7) gave 100.  Other step counts take
-  // the uniform damping w.
-  float mixed_wscale[4] = {0.875f, 1.75f, 1.0f, 1.0f};
-  bool omegas_set = false;   // DG_MIXED_OMEGAS given: its factors for any step count
+  // in reverse), a degree-2 Chebyshev polynomial smoother whose factors are
+  // set at each mixed build from an estimate of lambda_max(A_ee^-1 A)
+  // (set_smoother_schedule); other step counts take the uniform damping w
+  float mixed_wscale[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  double smoother_lmax = 0.0;
+  bool omegas_set = false;   // DG_MIXED_OMEGAS given: its factors, for any step count
   // mixed inner FGMRES: per-step convergence test on the device, chunk
   // graphs with one conditional node per step (c2: 100 -> 98 inner steps,
   // but 30.5 -> 31.4 ms: the stops land where the chunk checks already did
   // and the per-step nodes cost ~15 us; kept as an option)
   bool cond_graph = false;
+  // inner Arnoldi steps per captured graph; the host checks the
+  // least-squares residual after each, so a refinement step runs at most
+  // chunk - 1 steps past its target (c2 with the Chebyshev smoothing:
+  // chunk 10 / 5 / 4 / 3 -> 90 / 85 / 80 / 81 steps, 27.4 / 25.9 / 24.6 /
+  // 25.0 ms; c3: chunk 10 / 5 -> 212 / 202 ms)
+  int mixed_chunk = 4;
   // link the kernels of an inner Arnoldi step by programmatic dependent launch
   bool use_pdl = true;
   // batched solve: BF16 preconditioner steps on the tensor cores (mma.sync)
@@ -775,6 +780,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (sf && sf[0]) c->shared_faces = sf[0] != '0';
     const char* gb = std::getenv("DG_BUILD_GENERAL");
     if (gb && gb[0]) c->general_build = gb[0] != '0';
+    const char* mch = std::getenv("DG_MIXED_CHUNK");
+    if (mch && mch[0]) c->mixed_chunk = std::max(1, std::atoi(mch));
     const char* cg = std::getenv("DG_COND_GRAPH");
     if (cg && cg[0]) c->cond_graph = cg[0] != '0';
     const char* om = std::getenv("DG_MIXED_OMEGAS");   // absolute damping per step, "w0,w1,..."
