@@ -57,8 +57,9 @@ __global__ void __launch_bounds__(128) bres_kernel(const MT* __restrict__ blk, c
                                                    const float* __restrict__ b, float* __restrict__ r,
                                                    float* __restrict__ x_out, int64_t B, int flags,
                                                    const double* __restrict__ P, float* __restrict__ r1,
-                                                   float ws) {
+                                                   const float* __restrict__ wsp) {
   constexpr int N = 20, F = 4;
+  const float ws = wsp ? *wsp : 1.0f;
   constexpr int BLK = N * N;                     // entries per block
   constexpr int EL_BYTES = (F + 1) * BLK * (int)sizeof(MT);
   constexpr int W_BYTES = BLK * (int)sizeof(MT);
@@ -307,8 +308,9 @@ __global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat1
                                                        const float* __restrict__ b, float* __restrict__ r,
                                                        float* __restrict__ x_out, int64_t B, int flags,
                                                        const double* __restrict__ P, float* __restrict__ r1,
-                                                       float ws) {
+                                                       const float* __restrict__ wsp) {
   constexpr int N = 20, F = 4;
+  const float ws = wsp ? *wsp : 1.0f;
   __shared__ __align__(16) unsigned char As[(F + 1) * 800];
   __shared__ __align__(16) unsigned char Ws[800];
   __shared__ __align__(16) unsigned char Xhi[kXK * kXRow];
@@ -477,8 +479,10 @@ constexpr int kBT = 256;                                 // threads: 8 warps, wa
 __global__ void __launch_bounds__(kBT, kBS) bres_mma_tma_kernel(
     const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
     const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
-    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, float ws) {
+    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err,
+    const float* __restrict__ wsp) {
   constexpr int N = 20, F = 4;
+  const float ws = wsp ? *wsp : 1.0f;
   extern __shared__ __align__(128) unsigned char bsm[];
   unsigned char* stages = bsm;
   unsigned char* Xhi = bsm + kBStages * kStageB;
@@ -1065,7 +1069,7 @@ int ensure_batch(dg_ctx* c, int m) {
 
 template <typename MT>
 int bres(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out, int flags,
-         float* r1, cudaStream_t st, float ws = 1.0f) {
+         float* r1, cudaStream_t st, const float* ws = nullptr) {
   if (c->B > 0)
     bres_kernel<MT><<<(unsigned)c->B, 128, 0, st>>>(blk, W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, r1, ws);
   bump();
@@ -1084,8 +1088,8 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   float* other = S.t4;
   const bool bf = c->precond_bf16;
   // DG-level smoothing step k damped like the single-RHS preconditioner
-  auto wsk = [&](int k) { return (nsm == 2 || c->omegas_set) && k < 4 ? c->mixed_wscale[k] : 1.0f; };
-  auto pc = [&](const float* xx, float* xo, int flags, float* rr1, float ws) -> int {
+  auto wsk = [&](int k) -> const float* { return (nsm == 2 || c->omegas_set) && k < 4 ? M.d_ws + k : nullptr; };
+  auto pc = [&](const float* xx, float* xo, int flags, float* rr1, const float* ws) -> int {
     if (bf && c->batched_mma && c->batched_tma) {
       const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kBS);
       if (g)
@@ -1116,7 +1120,7 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
     if ((rc = pc(cur, other, RF_SMOOTH, nullptr, wsk(it)))) return rc;
     std::swap(cur, other);
   }
-  if ((rc = pc(cur, nullptr, RF_RESTRICT, S.r1, 1.0f))) return rc;
+  if ((rc = pc(cur, nullptr, RF_RESTRICT, S.r1, nullptr))) return rc;
   bgather_kernel<<<(unsigned)c->ncg, kNR, 0, st>>>(S.r1, c->d_gptr, c->d_gent, c->d_wdg, c->d_pos, S.lr[0],
                                                    (int)c->ncg);
   bump();

@@ -583,7 +583,9 @@ __global__ void __launch_bounds__(EPB* N) residual_kernel(const MT* __restrict__
                                                           VT* __restrict__ r,
                                                           VT* __restrict__ x_out, int64_t B,
                                                           int flags, const double* __restrict__ P = nullptr,
-                                                          VT* __restrict__ r1 = nullptr, AT wscale = (AT)1) {
+                                                          VT* __restrict__ r1 = nullptr,
+                                                          const float* __restrict__ wsp = nullptr) {
+  const AT wscale = wsp ? (AT)*wsp : (AT)1;
   __shared__ AT xs[EPB][F + 1][N];
   __shared__ AT rs[EPB][N];
   __shared__ int nbs[EPB][F];

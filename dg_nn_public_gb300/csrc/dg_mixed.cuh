@@ -71,6 +71,9 @@ struct Mixed {
   // the Gauss-Jordan augmented matrix of the dense coarse level
   double* winv = nullptr;
   double* gj = nullptr;
+  // damping factors of the smoothing steps (device copy of
+  // dg_ctx::mixed_wscale, read by the smoothing kernels)
+  float* d_ws = nullptr;
   size_t gj_cap = 0;
   std::vector<double> gv_host;
   std::vector<std::vector<int>> g_kern;
@@ -266,7 +269,8 @@ template <int EPB>
 __global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
     const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
     const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
-    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, float wscale) {
+    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, const float* __restrict__ wsp) {
+  const float wscale = wsp ? *wsp : 1.0f;
   constexpr int N = 20, F = 4;
   __shared__ float xs[EPB][F + 1][N];
   __shared__ float rs[EPB][N];
@@ -523,7 +527,8 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     const MT* __restrict__ blk, const MT* __restrict__ W, const int* __restrict__ nbe, const float* __restrict__ x,
     const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out, int64_t B, int flags,
     const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const int* __restrict__ fref5,
-    float wscale) {
+    const float* __restrict__ wsp) {
+  const float wscale = wsp ? *wsp : 1.0f;
   constexpr int N = 20, F = 4;
   using G = TmaGroup<MT, EPB, WITH_W>;
   using C = Chunk20<MT>;
@@ -732,7 +737,7 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
 // face, addressed through c->d_fref5); otherwise five blocks per element
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
 int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out,
-               int flags, float* r1, cudaStream_t st, bool sf, float wscale = 1.0f) {
+               int flags, float* r1, cudaStream_t st, bool sf, const float* wscale = nullptr) {
   if (c->l2_hint) flags |= RF_STREAM_HINT;
   const int64_t ngroups = (c->B + EPB - 1) / EPB;
   const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
@@ -764,7 +769,7 @@ int set_tma_smem(dg_ctx* c) {
 constexpr int kTmaVariants = 3;
 
 int launch_bf16_tma(dg_ctx* c, Mixed& M, const float* x, const float* b, float* r, float* x_out, int flags,
-                    cudaStream_t st, float ws = 1.0f) {
+                    cudaStream_t st, const float* ws = nullptr) {
   const __nv_bfloat16* A = M.sf ? M.sblk16 : M.blk16;
   switch (c->tma_variant) {
     case 1: return launch_tma<__nv_bfloat16, 8, 2, 2, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws);
@@ -836,7 +841,7 @@ void destroy_mixed(dg_ctx* c) {
 
 template <int D>
 int launch_residual32(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags,
-                      cudaStream_t st, float ws = 1.0f) {
+                      cudaStream_t st, const float* ws = nullptr) {
   using E = Elem<D>;
   Mixed& M = mixed_of(c);
   if (D == 3 && c->f32_tma) {   // chunked FP32 copy, bulk-copy kernel
@@ -855,7 +860,7 @@ int launch_residual32(dg_ctx* c, const float* x, const float* b, float* r, float
 }
 
 int residual32(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags, cudaStream_t st,
-               float ws = 1.0f) {
+               const float* ws = nullptr) {
   return c->D == 3 ? launch_residual32<3>(c, x, b, r, x_out, flags, st, ws)
                    : launch_residual32<2>(c, x, b, r, x_out, flags, st, ws);
 }
@@ -863,7 +868,7 @@ int residual32(dg_ctx* c, const float* x, const float* b, float* r, float* x_out
 // residual / smoothing with the BF16 block copies (FP32 vectors and sums)
 template <int D>
 int launch_residual16(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags,
-                      cudaStream_t st, float ws = 1.0f) {
+                      cudaStream_t st, const float* ws = nullptr) {
   using E = Elem<D>;
   Mixed& M = mixed_of(c);
   unsigned g = nblk(c->B, E::EPB);
@@ -876,10 +881,11 @@ int launch_residual16(dg_ctx* c, const float* x, const float* b, float* r, float
 }
 
 // residual in the preconditioner: BF16 blocks when enabled, FP32 otherwise
-// ws scales the smoother's correction of this step (x_out = x + ws W_e res):
-// with W_e = w A_ee^-1 the step is damped by ws * w
+// *ws (device memory, so that captured graphs follow a rebuilt schedule;
+// nullptr = 1) scales the smoother's correction of this step,
+// x_out = x + ws W_e res: with W_e = w A_ee^-1 the step is damped by ws * w
 int residual_pc(dg_ctx* c, const float* x, const float* b, float* r, float* x_out, int flags, cudaStream_t st,
-                float ws = 1.0f) {
+                const float* ws = nullptr) {
   if (c->precond_bf16) {
     if (c->D == 3 && c->bf16_tma) {
       Mixed& M = mixed_of(c);
@@ -1110,7 +1116,7 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   float* other = M.t4;
   // per-step damping: pre-smoothing steps k = 0, 1, ... use ws[k], the
   // post-smoothing steps the same factors in reverse order
-  auto ws = [&](int k) { return (nsm == 2 || c->omegas_set) && k < 4 ? c->mixed_wscale[k] : 1.0f; };
+  auto ws = [&](int k) -> const float* { return (nsm == 2 || c->omegas_set) && k < 4 ? M.d_ws + k : nullptr; };
   if (nsm > 0) {
     if ((rc = residual_pc(c, nullptr, r, nullptr, cur, RF_ZEROX | RF_SMOOTH, st, ws(0)))) return rc;
     for (int it = 1; it < nsm; ++it) {
@@ -1399,7 +1405,14 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
   }
   CKL(c);
   M.built = true;
-  if (!c->omegas_set && c->mixed_smoother == 1 && (rc = set_smoother_schedule(c, st))) return rc;
+  if (!M.d_ws && (rc = dalloc(c, &M.d_ws, 4))) return rc;
+  if (!c->omegas_set && c->mixed_smoother == 1) {
+    if ((rc = set_smoother_schedule(c, st))) return rc;
+  } else if (!c->omegas_set) {
+    for (float& f : c->mixed_wscale) f = 1.0f;
+  }
+  CK(c, cudaMemcpyAsync(M.d_ws, c->mixed_wscale, sizeof(float) * 4, cudaMemcpyHostToDevice, st));
+  CK(c, cudaStreamSynchronize(st));
   if (c->verbose)
     std::fprintf(stderr, "[build_mixed] ms: copies + smoother blocks + levels %.2f, dense coarse inverse (%d rows) %.2f\n",
                  std::chrono::duration<double, std::milli>(t1 - t0).count(), c->dense_n,
