@@ -1212,7 +1212,7 @@ int set_smoother_schedule(dg_ctx* c, cudaStream_t st) {
   }
   CKL(c);
   const double lmax = lam / c->mixed_smooth_w;   // of A_ee^-1 A
-  const double beta = 1.05 * lmax, alpha = beta / 8.0;
+  const double beta = c->cheb_margin * lmax, alpha = beta / 8.0;
   const double mid = 0.5 * (beta + alpha), half = 0.5 * (beta - alpha) * std::sqrt(0.5);
   const double om0 = 1.0 / (mid + half), om1 = 1.0 / (mid - half);
   c->mixed_wscale[0] = (float)(om0 / c->mixed_smooth_w);

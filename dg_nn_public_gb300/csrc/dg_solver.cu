@@ -134,6 +134,10 @@ struct dg_ctx {
   // (set_smoother_schedule); other step counts take the uniform damping w
   float mixed_wscale[4] = {1.0f, 1.0f, 1.0f, 1.0f};
   double smoother_lmax = 0.0;
+  // beta = margin x the estimated lambda_max (c2: margin 1.05 / 1.1 / 1.2
+  // -> 80 / 84 / 88 inner steps; c3: 94 / 94 / 106); a larger margin keeps
+  // the polynomial below 1 further past an underestimated lambda_max
+  double cheb_margin = 1.05;
   bool omegas_set = false;   // DG_MIXED_OMEGAS given: its factors, for any step count
   // mixed inner FGMRES: per-step convergence test on the device, chunk
   // graphs with one conditional node per step (c2: 100 -> 98 inner steps,
@@ -780,6 +784,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (sf && sf[0]) c->shared_faces = sf[0] != '0';
     const char* gb = std::getenv("DG_BUILD_GENERAL");
     if (gb && gb[0]) c->general_build = gb[0] != '0';
+    const char* cmg = std::getenv("DG_CHEB_MARGIN");
+    if (cmg && cmg[0]) c->cheb_margin = std::max(1.0, std::atof(cmg));
     const char* mch = std::getenv("DG_MIXED_CHUNK");
     if (mch && mch[0]) c->mixed_chunk = std::max(1, std::atoi(mch));
     const char* cg = std::getenv("DG_COND_GRAPH");
