@@ -91,6 +91,22 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(value, ws, device="cpu"):
+    """The largest value over the ranks (the slowest replica's time); the
+    value itself on one rank."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank, ws, seconds):
+    """Whole-job rate of ws independent replicas that each processed
+    units_per_rank in (at most) the given wall time."""
+    return ws * units_per_rank / seconds
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -330,7 +346,9 @@ def batched_leg(args, s, m, dofs, dev, stream, ws, R64=None, RMX=None):
         its_b.append(int(itb.max()))
     e1.record(stream)
     torch.cuda.synchronize()
-    tb = e0.elapsed_time(e1) / 1e3
+    if ws > 1:
+        torch.distributed.barrier()
+    tb = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws, dev)
     rel_b = max(float(torch.linalg.norm(s.residual(Xb[q].contiguous(), Bm[q].contiguous())) / tolb[q] * 1e-10)
                 for q in range(args.nrhs))
     err_b = float(np.abs(Xb.cpu().numpy() - Ub).max() / np.abs(Ub).max())
@@ -419,12 +437,9 @@ def run_ours(args):
             torch.distributed.barrier()
         nl = _capi.launch_count() - l0
         clk = clocks.stop() if clocks else None
-        t = torch.tensor([ev0.elapsed_time(ev1)], device=dev)
-        if ws > 1:
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(t.item())
+        t_ms = max_over_ranks(ev0.elapsed_time(ev1), ws, dev)
         return dict(x=x, its=its_l, res=res, tol=tol, t_ms=t_ms, launches=nl, clocks=clk,
-                    value=ws * dofs * args.steps / (t_ms / 1e3))
+                    value=replica_throughput(dofs * args.steps, ws, t_ms / 1e3))
 
     if args.mode == "batched":
         res_b = batched_leg(args, s, m, dofs, dev, stream, ws)
@@ -479,10 +494,7 @@ def run_ours(args):
         s.solve(f_host, out=x_host, mode=mode)
     torch.cuda.synchronize()
     t_e2e = time.perf_counter() - t0
-    te = torch.tensor([t_e2e], device=dev)
-    if ws > 1:
-        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = ws * dofs * args.steps / float(te.item())
+    e2e_value = replica_throughput(dofs * args.steps, ws, max_over_ranks(t_e2e, ws, dev))
 
     # roofline of the dominant kernel of the headline mode, timed alone with
     # CUDA events on the launching stream.  Mixed mode: the preconditioner's
