@@ -626,7 +626,13 @@ def run_ours(args):
                                           "(its set-up at this size takes minutes)"}
     elif rank == 0 and not args.no_cpu_baseline:
         try:
-            out["cpu_baseline"] = cpu_baseline_sample(m, order, el, int(np.median(its_list)),
+            # the restatement runs the reference's FP64 algorithm, so its solve
+            # takes that algorithm's iteration count: the FP64 GPU solve's
+            # (identical to the reference's on the pinned cases) when it ran,
+            # else the reference's count for this size
+            its_cpu = (int(np.median(R64["its"])) if R64 is not None
+                       else REFERENCE_ITS.get(args.n, int(np.median(its_list))))
+            out["cpu_baseline"] = cpu_baseline_sample(m, order, el, its_cpu,
                                                       rar=s.rar_values().cpu().numpy(), smooth=args.smooth)
         except Exception as exc:  # reported, not fatal
             out["cpu_baseline"] = {"value": None, "error": repr(exc)}
