@@ -91,6 +91,22 @@ def dist_env():
     return ws, rank, local
 
 
+L2_BYTES = 126e6   # GB300 L2 cache
+
+
+def l2_policy(m):
+    """Whether the timed steps stream the operator from HBM: the FP64 blocks
+    and the BF16 preconditioner copies against the L2 size."""
+    nloc = m.nloc
+    b64 = m.nele * (m.ndim + 2) * nloc * nloc * 8
+    b16 = m.nele * (m.ndim + 2) * nloc * nloc * 2
+    if b16 > L2_BYTES:
+        return ("inputs larger than L2: the FP64 operator blocks (%.0f MB) and the BF16 preconditioner "
+                "copies (%.0f MB) stream from HBM every pass" % (b64 / 1e6, b16 / 1e6))
+    return ("inputs not larger than L2 (FP64 blocks %.0f MB, BF16 copies %.0f MB, L2 126 MB): a small case, "
+            "not an HBM measurement" % (b64 / 1e6, b16 / 1e6))
+
+
 def max_over_ranks(value, ws, device="cpu"):
     """The largest value over the ranks (the slowest replica's time); the
     value itself on one rank."""
@@ -242,8 +258,7 @@ def config_block(args, m, extra=None):
                    ((20, 0.0, "mean"), (40, 1.0, "harmonic")) else "custom",
          "nele": int(m.nele), "dofs": int(m.nele * m.nloc), "eta_e": 90.0, "gmres_m": 30,
          "smoothing": "V(%d,%d)" % (args.smooth, args.smooth),
-         "l2_policy": "inputs larger than L2: the FP64 operator blocks (%.0f MB) stream from HBM every apply"
-                      % (m.nele * 5 * 400 * 8 / 1e6)}
+         "l2_policy": l2_policy(m)}
     if extra:
         d.update(extra)
     return d
