@@ -169,3 +169,32 @@ def test_write_vtu_roundtrip(tmp_path):
     assert (conn.reshape(m.nele, 20)[1] == 20 + vtk_node_order(3)).all()
     vals = np.array(piece.find("PointData/DataArray[@Name='u']").text.split(), dtype=np.float64)
     assert np.array_equal(vals, u)
+
+
+@pytest.mark.parametrize("kind,n", [("tet", 2), ("tri", 4)])
+def test_colour_probe_rar_equals_galerkin_product(kind, n):
+    """The colour-probe P1CG operator (one apply per colour of a distance-2
+    colouring) is the Galerkin product I_cf A I_fc entry for entry: a
+    direct assembly from the element blocks has to reproduce exactly these
+    values (up to summation order).  Dense products on a small jittered mesh
+    with log-normal kappa."""
+    from dg_nn_public_gb300 import mesh
+    m = mesh.build_mesh(kind, n, seed=3)
+    el = element.p3_element(m.ndim)
+    kap = np.exp(0.6 * np.random.default_rng(2).standard_normal(m.nele))
+    O = OracleDG(m, el, element.drst_duv(m.ndim), eta_e=90.0, kappa=kap)
+    pc = O.p1cg()
+    probe = O.rar(pc)
+    ndg, ncg = m.nele * m.nloc, m.cg_nonods
+    eye_dg, eye_cg = np.eye(ndg), np.eye(ncg)
+    A = np.stack([O.apply_Ax(eye_dg[i]).ravel() for i in range(ndg)], axis=1)
+    P = np.stack([O.prolong_from_cg(eye_cg[j], pc).ravel() for j in range(ncg)], axis=1)
+    R = np.stack([O.restrict_to_cg(eye_dg[i], pc) for i in range(ndg)], axis=1)
+    G = R @ A @ P
+    rows = np.repeat(np.arange(ncg), np.diff(pc["fina"]))
+    direct = G[rows, pc["cola"]]
+    assert np.abs(direct - probe).max() <= 1e-12 * np.abs(probe).max()
+    # and nothing of the product lies outside the P1CG sparsity
+    mask = np.zeros((ncg, ncg), dtype=bool)
+    mask[rows, pc["cola"]] = True
+    assert np.abs(G[~mask]).max(initial=0.0) <= 1e-12 * np.abs(probe).max()
