@@ -76,6 +76,7 @@ _SIGNATURES = {
     "dg_nlevel_sfc": (C.c_int32, [C.c_int64]),
     "dg_sfc_levels": (_I, [C.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_int64, _P]),
     "dg_face_connectivity": (_I, [C.c_int32, C.c_int64, _P, _P, _P]),
+    "dg_rap_contributions": (_I, [C.c_int32, C.c_int64, _P, _P, _P, _P, C.c_int64, _P, _P, C.c_int64, _P]),
 }
 # entry points added by later translation units (bound when present)
 _OPTIONAL = {}
@@ -146,6 +147,25 @@ def p1cg_sparsity(p1cg: np.ndarray, cg_nonods: int):
     ncola = np.zeros(1, dtype=np.int64)
     check(lib().dg_p1cg_sparsity(nele, nc, ptr(p1), cg_nonods, ptr(fina), ptr(cola), cap, ptr(ncola)))
     return fina, cola[:int(ncola[0])].copy()
+
+
+def rap_contributions(ndim: int, p1cg: np.ndarray, nbe: np.ndarray, fina: np.ndarray, cola: np.ndarray):
+    """(ptr, entries) of the direct Galerkin P1CG assembly: entries[ptr[k]:
+    ptr[k+1]] are the (block, a, c) triples of nonzero k (see
+    dg_rap_contributions in include/dgsip.h)."""
+    p1 = np.ascontiguousarray(p1cg, dtype=np.int64)
+    nb = np.ascontiguousarray(nbe, dtype=np.int64)
+    fina = np.ascontiguousarray(fina, dtype=np.int64)
+    cola = np.ascontiguousarray(cola, dtype=np.int64)
+    nele, nc = p1.shape
+    n = fina.size - 1
+    cap = nele * (ndim + 2) * nc * nc
+    ptr_ = np.zeros(int(fina[-1]) + 1, dtype=np.int64)
+    ent = np.zeros((max(cap, 1), 3), dtype=np.int64)
+    cnt = np.zeros(1, dtype=np.int64)
+    check(lib().dg_rap_contributions(ndim, nele, ptr(p1), ptr(nb), ptr(fina), ptr(cola), n, ptr(ptr_), ptr(ent),
+                                     cap, ptr(cnt)))
+    return ptr_, ent[:int(cnt[0])].copy()
 
 
 def color2(fina, cola):

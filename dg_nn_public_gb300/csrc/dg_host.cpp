@@ -189,6 +189,62 @@ int sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double
   return DG_OK;
 }
 
+// Contribution lists of the Galerkin P1CG operator R A P from the stored
+// blocks (R = I_cf, P = I_fc, both weighted 1/#copies as in
+// volume_mf_diff.py:1961-1966, 2010-2013):
+//   RAP[k] = sum over list k of w(e, a) w(nb, c) (P3^T A_{e,nb} P3)[a][c]
+// for the CSR nonzero k = (I, J) of fina / cola, where block (e, slot) couples
+// element e's rows to element nb's columns (slot 0: nb = e; slot 1 + f: the
+// neighbour across face f), I = p1cg[e][a] and J = p1cg[nb][c].  Entries are
+// (block = e * (nface + 1) + slot, a, c), in block order and then (a, c), so a
+// fixed-order sum over a list is deterministic.  The colour-probe operator
+// equals this product (tested on the CPU restatement).
+int rap_contributions(int64_t nele, int ndim, const int64_t* p1cg, const int64_t* nbe, const int64_t* fina,
+                      const int64_t* cola, int64_t n, std::vector<int64_t>& ptr,
+                      std::vector<std::array<int64_t, 3>>& ent) {
+  const int nc = ndim + 1, nf = ndim + 1, ns = nf + 1;
+  const int64_t nnz = fina[n];
+  auto find = [&](int64_t i, int64_t j) -> int64_t {
+    const int64_t* b = cola + fina[i];
+    const int64_t* e = cola + fina[i + 1];
+    const int64_t* q = std::lower_bound(b, e, j);
+    return (q != e && *q == j) ? (int64_t)(q - cola) : -1;
+  };
+  ptr.assign(nnz + 1, 0);
+  // pass 1 counts, pass 2 fills (block order within each list)
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<int64_t> fill;
+    if (pass == 1) {
+      for (int64_t k = 0; k < nnz; ++k) ptr[k + 1] += ptr[k];
+      ent.assign(ptr[nnz], {0, 0, 0});
+      fill.assign(ptr.begin(), ptr.end() - 1);
+    }
+    for (int64_t e = 0; e < nele; ++e)
+      for (int sl = 0; sl < ns; ++sl) {
+        const int64_t nb = sl == 0 ? e : nbe[e * nf + sl - 1];
+        if (nb < 0) continue;
+        if (nb >= nele) return set_thread_error(DG_ERR_MESH, "rap_contributions: neighbour out of range");
+        for (int a = 0; a < nc; ++a)
+          for (int c = 0; c < nc; ++c) {
+            const int64_t i = p1cg[e * nc + a], j = p1cg[nb * nc + c];
+            if (i < 0 || i >= n || j < 0 || j >= n)
+              return set_thread_error(DG_ERR_MESH, "rap_contributions: p1cg vertex out of range");
+            // a face block also couples vertex pairs that share no element;
+            // their contributions cancel (the P1 functions are continuous, so
+            // the face terms vanish in the sum) and the probe assembly does
+            // not read them either
+            const int64_t k = find(i, j);
+            if (k < 0) continue;
+            if (pass == 0)
+              ++ptr[k + 1];
+            else
+              ent[fill[k]++] = {e * ns + sl, a, c};
+          }
+      }
+  }
+  return DG_OK;
+}
+
 // Face connectivity in the reference's internal corner order
 // (mesh_init.py:298-320 face corner lists, :358-401 matching and alignment).
 int face_connectivity(int ndim, int64_t nele, const int64_t* corners, int64_t* nbf, int64_t* alnmt) {
@@ -267,6 +323,24 @@ int dg_color2(int64_t n, const int64_t* fina, const int64_t* cola, int64_t* whic
 }
 
 int32_t dg_nlevel_sfc(int64_t nonods) { return nlevel_sfc(nonods); }
+
+int dg_rap_contributions(int32_t ndim, int64_t nele, const int64_t* p1cg, const int64_t* nbe, const int64_t* fina,
+                         const int64_t* cola, int64_t cg_nonods, int64_t* ptr, int64_t* entries, int64_t cap,
+                         int64_t* count) {
+  if ((ndim != 2 && ndim != 3) || nele < 0 || cg_nonods < 0 || !fina || !ptr || !count ||
+      (nele > 0 && (!p1cg || !nbe || !cola)))
+    return set_thread_error(DG_ERR_ARG, "dg_rap_contributions: bad arguments");
+  std::vector<int64_t> p;
+  std::vector<std::array<int64_t, 3>> ent;
+  int rc = rap_contributions(nele, ndim, p1cg, nbe, fina, cola, cg_nonods, p, ent);
+  if (rc) return rc;
+  *count = (int64_t)ent.size();
+  std::memcpy(ptr, p.data(), sizeof(int64_t) * p.size());
+  if ((int64_t)ent.size() > cap || (!entries && !ent.empty()))
+    return set_thread_error(DG_ERR_ARG, "dg_rap_contributions: entries capacity too small");
+  if (!ent.empty()) std::memcpy(entries, ent.data(), sizeof(int64_t) * 3 * ent.size());
+  return DG_OK;
+}
 
 int dg_sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double* a,
                   const int64_t* sfc_order, int32_t* nlevel, int64_t* level_start, int64_t* row_ptr,

@@ -233,6 +233,19 @@ int32_t dg_nlevel_sfc(int64_t nonods);
 int dg_sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double* a,
                   const int64_t* sfc_order, int32_t* nlevel, int64_t* level_start,
                   int64_t* row_ptr, int64_t* col, double* val, int64_t cap, int64_t* nnz);
+/* Contribution lists of the Galerkin P1CG operator I_cf A I_fc from the
+ * stored blocks, the direct form of the colour-probe assembly of
+ * z06/volume_mf_diff.py:1696-1754: for every P1CG nonzero k (fina / cola),
+ * entries[ptr[k] .. ptr[k+1]) are (block, a, c) triples with block =
+ * e * (nface + 1) + slot (slot 0 = own block, 1 + f = neighbour across face
+ * f, nbe (nele, nface) = neighbour element or -1), so that
+ * RAP[k] = sum w(e, a) w(nb, c) (P^T A_block P)[a][c] with w = 1/#copies
+ * (vertex pairs outside the P1CG sparsity are left out: their face-block
+ * contributions cancel).  ptr has nnz+1 entries; entries capacity cap
+ * triples; *count gets the number of triples. */
+int dg_rap_contributions(int32_t ndim, int64_t nele, const int64_t* p1cg, const int64_t* nbe,
+                         const int64_t* fina, const int64_t* cola, int64_t cg_nonods, int64_t* ptr,
+                         int64_t* entries, int64_t cap, int64_t* count);
 /* Face connectivity of cells in the reference's internal corner order
  * (z06/mesh_init.py:298-401): nbf and alnmt for all nele*nface faces. */
 int dg_face_connectivity(int32_t ndim, int64_t nele, const int64_t* corners /* (nele, ndim+1) */,
