@@ -43,6 +43,9 @@ void parallel_for(int count, Fn fn) {
   for (auto& x : th) x.join();
 }
 
+int rap_contributions(int64_t nele, int ndim, const int64_t* p1cg, const int64_t* nbe, const int64_t* fina,
+                      const int64_t* cola, int64_t n, std::vector<int64_t>& ptr,
+                      std::vector<std::array<int64_t, 3>>& ent);
 int p1cg_sparsity(int64_t nele, int ncorner, const int64_t* p1cg, int64_t n,
                   std::vector<int64_t>& fina, std::vector<int64_t>& cola);
 int color2(int64_t n, const int64_t* fina, const int64_t* cola, std::vector<int64_t>& whichc,

@@ -194,6 +194,60 @@ __global__ void rar_scatter_kernel(double* __restrict__ value, const double* __r
   if (k < cnt) value[spidx[k]] += rarm[colidx[k]];
 }
 
+// Direct Galerkin P1CG operator (the colour-probe result in one pass).
+// G_b = P^T A_b P (NC x NC) for every stored block b, one warp per block:
+// lanes m < N form row m of A_b P, then lanes < NC * NC the products with P^T.
+template <int N, int NC>
+__global__ void __launch_bounds__(128) block_galerkin_kernel(const double* __restrict__ blk,
+                                                             const double* __restrict__ P,
+                                                             double* __restrict__ G, int64_t nb) {
+  constexpr int WPB = 4;
+  __shared__ double Q[WPB][N][NC];
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  const int64_t b = (int64_t)blockIdx.x * WPB + wi;
+  if (b >= nb) return;   // whole warp
+  const double* A = blk + b * N * N;   // A(m, n) at [n * N + m]
+  if (lane < N) {
+    double q[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) q[c] = 0.0;
+    for (int n = 0; n < N; ++n) {
+      const double a = A[n * N + lane];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) q[c] = fma(a, P[n * NC + c], q[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) Q[wi][lane][c] = q[c];
+  }
+  __syncwarp();
+  if (lane < NC * NC) {
+    const int a = lane / NC, c = lane % NC;
+    double g = 0.0;
+    for (int m = 0; m < N; ++m) g = fma(P[m * NC + a], Q[wi][m][c], g);
+    G[b * NC * NC + lane] = g;
+  }
+}
+
+// rar[k] = sum over the contribution list of nonzero k (dg_rap_contributions,
+// packed block * 16 + a * 4 + c) of w(e, a) w(nb, c) G_block[a][c], in list
+// order (deterministic)
+__global__ void rap_gather_kernel(const double* __restrict__ G, const int* __restrict__ ptr,
+                                  const int* __restrict__ ent, const double* __restrict__ wdg,
+                                  const int* __restrict__ nbe, int F, int NC, double* __restrict__ rar,
+                                  int64_t nnz) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nnz) return;
+  double s = 0.0;
+  for (int t = ptr[k]; t < ptr[k + 1]; ++t) {
+    const int v = ent[t];
+    const int bid = v >> 4, a = (v >> 2) & 3, c = v & 3;
+    const int e = bid / (F + 1), sl = bid % (F + 1);
+    const int nb = sl == 0 ? e : nbe[e * F + sl - 1];
+    s += wdg[e * NC + a] * wdg[nb * NC + c] * G[(int64_t)bid * NC * NC + a * NC + c];
+  }
+  rar[k] = s;
+}
+
 // ---------------------------------------------------------------------------
 // SFC levels (multigrid_linearelastic.py:25-172)
 

@@ -67,6 +67,12 @@ struct dg_ctx {
   double* d_ftab = nullptr;
   int fast_build = -1;
   bool general_build = false;
+  // direct Galerkin P1CG operator from the blocks (DG_RAP_DIRECT=1) instead of
+  // the colour probes: contribution lists (dg_rap_contributions, packed) and
+  // the per-block products
+  bool rap_direct = false;
+  int *d_rap_ptr = nullptr, *d_rap_ent = nullptr;
+  double* d_rap_G = nullptr;
   int64_t nface_sh = 0;
   double* d_kappa = nullptr;
   Tables T{};
@@ -782,6 +788,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (lh && lh[0]) c->l2_hint = lh[0] != '0';
     const char* sf = std::getenv("DG_SHARED_FACES");
     if (sf && sf[0]) c->shared_faces = sf[0] != '0';
+    const char* rd = std::getenv("DG_RAP_DIRECT");
+    if (rd && rd[0]) c->rap_direct = rd[0] != '0';
     const char* gb = std::getenv("DG_BUILD_GENERAL");
     if (gb && gb[0]) c->general_build = gb[0] != '0';
     const char* cmg = std::getenv("DG_CHEB_MARGIN");
@@ -1034,6 +1042,20 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     }
     if ((rc = upload_vec(c.get(), &c->d_pos, pos))) return rc;
   }
+  if (c->rap_direct) {
+    std::vector<int64_t> nbe64(nbe.begin(), nbe.end()), rptr;
+    std::vector<std::array<int64_t, 3>> rent;
+    if ((rc = rap_contributions(c->B, D, c->p1cg.data(), nbe64.data(), c->fina.data(), c->cola.data(), c->ncg, rptr,
+                                rent)))
+      return fail(c.get(), rc, g_thread_error);
+    if ((int64_t)c->B * (F + 1) * 16 >= (int64_t)INT32_MAX || (int64_t)rent.size() >= (int64_t)INT32_MAX)
+      return fail(c.get(), DG_ERR_ARG, "mesh too large for the direct P1CG assembly");
+    std::vector<int> rp(rptr.begin(), rptr.end()), re(rent.size());
+    for (size_t t = 0; t < rent.size(); ++t) re[t] = (int)(rent[t][0] * 16 + rent[t][1] * 4 + rent[t][2]);
+    if ((rc = upload_vec(c.get(), &c->d_rap_ptr, rp))) return rc;
+    if ((rc = upload_vec(c.get(), &c->d_rap_ent, re))) return rc;
+    if ((rc = dalloc(c.get(), &c->d_rap_G, (size_t)c->B * (F + 1) * c->NC * c->NC))) return rc;
+  }
   if ((rc = dalloc(c.get(), &c->d_rar, c->cola.size()))) return rc;
   for (double** t : {&c->d_t1, &c->d_t2, &c->d_t3, &c->d_t4, &c->d_t5})
     if ((rc = dalloc(c.get(), t, (size_t)c->nonods))) return rc;
@@ -1088,9 +1110,23 @@ int dg_build_operator(dg_ctx* c, void* stream) {
   if (herr) return fail(c, DG_ERR_MESH, "non-positive element Jacobian (element not positively oriented)");
   c->built = true;   // blocks are usable from here on (the probes below apply them)
   ++c->build_version;
-  // colour-probe Galerkin operator on P1CG (volume_mf_diff.py:1696-1754)
+  // colour-probe Galerkin operator on P1CG (volume_mf_diff.py:1696-1754), or
+  // the same product formed directly from the blocks
   CK(c, cudaMemsetAsync(c->d_rar, 0, sizeof(double) * c->cola.size(), st));
-  for (int col = 1; col <= c->ncolor; ++col) {
+  if (c->rap_direct && c->d_rap_ptr) {
+    const int64_t nb = c->B * (c->F + 1);
+    if (c->D == 3)
+      block_galerkin_kernel<20, 4><<<nblk(nb, 4), 128, 0, st>>>(c->d_blk, c->T.P, c->d_rap_G, nb);
+    else
+      block_galerkin_kernel<10, 3><<<nblk(nb, 4), 128, 0, st>>>(c->d_blk, c->T.P, c->d_rap_G, nb);
+    bump();
+    rap_gather_kernel<<<nblk((int64_t)c->cola.size(), 128), 128, 0, st>>>(
+        c->d_rap_G, c->d_rap_ptr, c->d_rap_ent, c->d_wdg, c->d_nbe, c->F, c->NC, c->d_rar,
+        (int64_t)c->cola.size());
+    bump();
+    CKL(c);
+  }
+  for (int col = 1; col <= ((c->rap_direct && c->d_rap_ptr) ? 0 : c->ncolor); ++col) {
     if ((rc = prolong_cg(c, c->d_t1, nullptr, false, col, false, st))) return rc;
     if ((rc = residual(c, c->d_t1, nullptr, c->d_t2, nullptr, RF_NEG, st))) return rc;   // t2 = A t1
     if ((rc = restrict_cg(c, c->d_t2, c->d_cg1, false, st))) return rc;
