@@ -116,3 +116,18 @@ def test_rap_contributions_give_the_probe_operator(lib, kind, n):
             G = P3.T @ A[e * N:(e + 1) * N, nb * N:(nb + 1) * N] @ P3
             direct[k] += w[e, a] * w[nb, c] * G[a, c]
     assert np.abs(direct - probe).max() <= 1e-12 * np.abs(probe).max()
+
+
+def test_rap_contributions_error_paths(lib):
+    from dg_nn_public_gb300 import _capi
+    p1 = np.array([[0, 1, 2, 3]], dtype=np.int64)
+    fina, cola = _capi.p1cg_sparsity(p1, 4)
+    nbe = -np.ones((1, 4), dtype=np.int64)
+    ptr, ent = _capi.rap_contributions(3, p1, nbe, fina, cola)
+    # one element, own block only: every corner pair once, in (a, c) order
+    assert ent.shape == (16, 3) and np.array_equal(np.diff(ptr), np.ones(16, dtype=np.int64))
+    assert sorted(map(tuple, ent.tolist())) == [(0, a, c) for a in range(4) for c in range(4)]
+    with pytest.raises(_capi.DGError):
+        _capi.rap_contributions(3, p1, np.array([[5, -1, -1, -1]]), fina, cola)   # neighbour out of range
+    with pytest.raises(_capi.DGError):
+        _capi.rap_contributions(4, p1, nbe, fina, cola)                             # bad dimension
