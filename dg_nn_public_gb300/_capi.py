@@ -63,6 +63,7 @@ _SIGNATURES = {
     "dg_precond": (_I, [_P, _P, _P, _P]),
     "dg_mg_vcycle": (_I, [_P, _P, _P, _P]),
     "dg_gmres": (_I, [_P, _P, _P, C.c_double, C.c_int32, C.c_int32, _P, _P, _P]),
+    "dg_set_gmres_ortho": (_I, [_P, C.c_int32]),
     "dg_solve_mixed": (_I, [_P, _P, _P, C.c_double, C.c_int32, C.c_int32, C.c_double, _P, _P, _P, _P]),
     "dg_apply_f32": (_I, [_P, _P, _P, _P]),
     "dg_solve_mixed_batched": (_I, [_P, _P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_double, _P, _P, _P]),

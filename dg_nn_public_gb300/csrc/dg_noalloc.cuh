@@ -7,7 +7,12 @@
 // cudaGetSymbolAddress, with that device current, on the first call made for
 // a context on that device; later calls reuse the cached pointer.  The first
 // call per device may load this library's module on that device, so make it
-// before any stream capture that is to contain the entry point.
+// before any stream capture that is to contain the entry point.  The cached
+// address belongs to the device's primary context: it assumes that context
+// lives for the whole process (a host program that calls cudaDeviceReset or
+// otherwise tears the primary context down must not call this entry point
+// afterwards).  Like the other entry points, a call leaves the calling
+// thread's current device set to the context's device.
 //
 // Nothing in the scratch has to start at zero: each call writes the partial
 // sum of every CTA it launches before its second kernel reads exactly those
@@ -135,16 +140,30 @@ int noalloc_scratch(dg_ctx* c, double** out) {
   return DG_OK;
 }
 
+// Usable partial sums: kNoAllocMaxPartials, or fewer when DG_NOALLOC_MAX_PARTIALS
+// holds a smaller positive number (a test hook that can only tighten the
+// limit, so the rejection path can be exercised on small meshes).
+int64_t noalloc_limit() {
+  int64_t lim = kNoAllocMaxPartials;
+  const char* v = std::getenv("DG_NOALLOC_MAX_PARTIALS");
+  if (v && v[0]) {
+    const long long t = std::atoll(v);
+    if (t > 0 && t < lim) lim = t;
+  }
+  return lim;
+}
+
 template <int D>
 int launch_residual_norm_noalloc(dg_ctx* c, const double* x, const double* b, double* r, double* norm_out,
                                  cudaStream_t st) {
   using E = Elem<D>;
   const int64_t g = ((int64_t)c->B + E::EPB - 1) / E::EPB;
-  if (g > kNoAllocMaxPartials)
+  const int64_t lim = noalloc_limit();
+  if (g > lim)
     return fail(c, DG_ERR_ARG,
                 "dg_residual_norm_noalloc: " + std::to_string(c->B) + " elements need " + std::to_string(g) +
-                    " partial sums; the static scratch holds " + std::to_string(kNoAllocMaxPartials) +
-                    " (at most " + std::to_string((int64_t)kNoAllocMaxPartials * E::EPB) + " elements)");
+                    " partial sums; the static scratch holds " + std::to_string(lim) +
+                    " (at most " + std::to_string(lim * E::EPB) + " elements)");
   double* partial = nullptr;
   int rc = noalloc_scratch(c, &partial);
   if (rc) return rc;

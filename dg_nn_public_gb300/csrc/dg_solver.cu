@@ -67,10 +67,12 @@ struct dg_ctx {
   double* d_ftab = nullptr;
   int fast_build = -1;
   bool general_build = false;
-  // direct Galerkin P1CG operator from the blocks (DG_RAP_DIRECT=1) instead of
-  // the colour probes: contribution lists (dg_rap_contributions, packed) and
-  // the per-block products
-  bool rap_direct = false;
+  // direct Galerkin P1CG operator from the blocks (default; DG_RAP_DIRECT=0
+  // restores one FP64 apply per colour of the distance-2 colouring):
+  // contribution lists (dg_rap_contributions, packed) and the per-block
+  // products.  Equal to the probe operator within 4e-16 relative on the
+  // golden cases and c2; operator build at 280k tets 106 -> 82 ms.
+  bool rap_direct = true;
   int *d_rap_ptr = nullptr, *d_rap_ent = nullptr;
   double* d_rap_G = nullptr;
   int64_t nface_sh = 0;
@@ -176,11 +178,17 @@ struct dg_ctx {
   // FP64 partial sums; 2 = CGS2).  One pass: the FP64 refinement bounds the
   // result, and c2 / c3 need the same inner iterations either way.
   int mixed_cgs_passes = 1;
+  // orthogonalisation of the FP64 GMRES Arnoldi step: 0 = CGS2 (two classical
+  // passes, 2 reductions per step), 1 = modified Gram-Schmidt in the
+  // reference's order (z06/volume_mf_diff.py:1814-1819; j + 1 dependent
+  // dot / update pairs per step)
+  int gmres_ortho = 0;
   // captured Arnoldi cycle (GMRES(m) inner loop) replayed as one CUDA graph
   bool use_graph = true;
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t arnoldi_exec = nullptr;
   int arnoldi_m = 0;
+  int arnoldi_ortho = 0;
   const double* arnoldi_vptr = nullptr;
   // mixed-precision state (dg_mixed.cuh) and operator versions
   void* mixed_state = nullptr;
@@ -610,6 +618,30 @@ int cgs2_t(dg_ctx* c, VT* Vbase, double* Hbase, int j, VT* z, int m, cudaStream_
 
 int cgs2(dg_ctx* c, int j, double* z, int m, cudaStream_t st) { return cgs2_t<double>(c, c->d_V, c->d_H, j, z, m, st); }
 
+// Modified Gram-Schmidt step in the reference's order
+// (z06/volume_mf_diff.py:1814-1819): for i = 0..j, H[i][j] = z . V[i] then
+// z -= H[i][j] V[i]; H[j+1][j] = |z|, V[j+1] = z / |z|.
+int mgs(dg_ctx* c, int j, double* z, int m, cudaStream_t st) {
+  const int nv = j + 1;
+  double* Hc = c->d_H + (size_t)j * (m + 1);
+  for (int i = 0; i < nv; ++i) {
+    const double* Vi = c->d_V + (size_t)i * c->nonods;
+    mdot2d_kernel<RED_TB, double><<<dim3(c->nred, 1), RED_TB, 0, st>>>(Vi, c->nonods, z, c->nonods, c->d_part);
+    bump();
+    reduce_partial_kernel<<<1, 128, 0, st>>>(c->d_part, c->nred, 1, Hc + i, 0, 0);
+    bump();
+    axpy_multi_kernel<RED_TB, double><<<c->nred, RED_TB, 0, st>>>(Vi, c->nonods, 1, Hc + i, z, c->nonods,
+                                                                   c->d_part, i == j ? 1 : 0);
+    bump();
+  }
+  reduce_partial_kernel<<<1, 128, 0, st>>>(c->d_part, c->nred, 1, Hc + nv, 0, 1);
+  bump();
+  scale_kernel<double><<<nblk(c->nonods, 256), 256, 0, st>>>(z, Hc + nv, c->d_V + (size_t)nv * c->nonods, c->nonods);
+  bump();
+  CKL(c);
+  return DG_OK;
+}
+
 // The m Arnoldi steps of one GMRES cycle (V[0] already set): w = A v_j,
 // r = M^-1 w, CGS2 against V[0..j], V[j+1] = r / ||r||.
 int arnoldi_steps(dg_ctx* c, int m, cudaStream_t st) {
@@ -619,14 +651,14 @@ int arnoldi_steps(dg_ctx* c, int m, cudaStream_t st) {
   for (int j = 0; j < m; ++j) {
     if ((rc = residual(c, c->d_V + (size_t)j * c->nonods, nullptr, w, nullptr, RF_NEG, st))) return rc;
     if ((rc = precond(c, w, r, st))) return rc;
-    if ((rc = cgs2(c, j, r, m, st))) return rc;
+    if ((rc = c->gmres_ortho == 1 ? mgs(c, j, r, m, st) : cgs2(c, j, r, m, st))) return rc;
   }
   return DG_OK;
 }
 
 int run_arnoldi(dg_ctx* c, int m, cudaStream_t st) {
   if (!c->use_graph) return arnoldi_steps(c, m, st);
-  if (!c->arnoldi_exec || c->arnoldi_m != m || c->arnoldi_vptr != c->d_V) {
+  if (!c->arnoldi_exec || c->arnoldi_m != m || c->arnoldi_vptr != c->d_V || c->arnoldi_ortho != c->gmres_ortho) {
     if (c->arnoldi_exec) {
       cudaGraphExecDestroy(c->arnoldi_exec);
       c->arnoldi_exec = nullptr;
@@ -649,6 +681,7 @@ int run_arnoldi(dg_ctx* c, int m, cudaStream_t st) {
     if (ie != cudaSuccess) return fail(c, DG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
     c->arnoldi_m = m;
     c->arnoldi_vptr = c->d_V;
+    c->arnoldi_ortho = c->gmres_ortho;
   }
   CK(c, cudaGraphLaunch(c->arnoldi_exec, st));
   bump(c->arnoldi_kernels);
@@ -1341,6 +1374,13 @@ int dg_mg_vcycle(dg_ctx* c, const double* r_sfc, double* e_sfc, void* stream) {
   int rc = vcycle(c, r_sfc, st);
   if (rc) return rc;
   CK(c, cudaMemcpyAsync(e_sfc, c->lev[0].e, sizeof(double) * c->ncg, cudaMemcpyDeviceToDevice, st));
+  return DG_OK;
+}
+
+int dg_set_gmres_ortho(dg_ctx* c, int32_t mode) {
+  if (!c) return set_thread_error(DG_ERR_ARG, "dg_set_gmres_ortho: null context");
+  if (mode != 0 && mode != 1) return fail(c, DG_ERR_ARG, "dg_set_gmres_ortho: mode must be 0 (CGS2) or 1 (MGS)");
+  c->gmres_ortho = mode;
   return DG_OK;
 }
 

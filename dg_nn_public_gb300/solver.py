@@ -346,6 +346,14 @@ class DGSolver:
         self._chk(rc)
         return its.value, res.value, outer.value
 
+    def set_gmres_ortho(self, mode):
+        """Arnoldi orthogonalisation of ``gmres``: "cgs2" (default) or "mgs",
+        the reference's modified Gram-Schmidt order (z06/volume_mf_diff.py:1814-1819)."""
+        modes = {"cgs2": 0, "mgs": 1}
+        if mode not in modes:
+            raise ValueError("gmres ortho must be one of %s" % sorted(modes))
+        self._chk(self._lib.dg_set_gmres_ortho(self._ctx, modes[mode]))
+
     def gmres(self, x, b, tol, m=None, max_its=None, raise_noconv=False):
         """Restarted GMRES(m) in place on x; returns (its, final ||b - A x||)."""
         m = self.cfg.gmres_m if m is None else m

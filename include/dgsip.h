@@ -109,8 +109,11 @@ int dg_set_kappa(dg_ctx* ctx, const double* kappa /* [host] (nele) or NULL */);
  * under large kappa jumps (no counterpart in the reference).  Takes effect
  * at the next dg_build_operator. */
 int dg_set_face_kappa(dg_ctx* ctx, int32_t mode);
-/* Assemble the stored element blocks, the block diagonal, the colour-probe
- * Galerkin P1CG operator and the SFC levels.  Replaces get_bdiag_diag()
+/* Assemble the stored element blocks, the block diagonal, the Galerkin P1CG
+ * operator (per-block products P^T A_b P summed over fixed contribution
+ * lists; the environment variable DG_RAP_DIRECT=0 selects the reference's
+ * colour-probe form instead, one operator apply per colour of a distance-2
+ * colouring, z06/volume_mf_diff.py:1696-1754) and the SFC levels.  Replaces get_bdiag_diag()
  * (z06/get_bdiag_diag.py:30-62) and _get_RAR_and_sfc_data_Um()
  * (z06/volume_mf_diff.py:1642-1693, multigrid_linearelastic.py:175-283). */
 int dg_build_operator(dg_ctx* ctx, void* stream);
@@ -149,6 +152,12 @@ int dg_mg_vcycle(dg_ctx* ctx, const double* r_sfc, double* e_sfc, void* stream);
  * (final ||b - A x||) may be NULL. */
 int dg_gmres(dg_ctx* ctx, double* x, const double* b, double tol, int32_t m, int32_t max_its,
              int32_t* its, double* res_norm, void* stream);
+/* Orthogonalisation of dg_gmres's Arnoldi step: mode 0 = CGS2 (default; two
+ * classical Gram-Schmidt passes, two reductions per step), mode 1 = modified
+ * Gram-Schmidt in the reference's order (z06/volume_mf_diff.py:1814-1819:
+ * h_ij = w . v_i then w -= h_ij v_i for i = 0..j), j + 1 dependent
+ * reductions per step.  Takes effect at the next dg_gmres. */
+int dg_set_gmres_ortho(dg_ctx* ctx, int32_t mode);
 
 /* ---- mixed precision (new in this build; no counterpart in the reference) ----
  * FP64 iterative refinement around an FP32 inner solve: r = b - A x in FP64;
@@ -206,8 +215,12 @@ int dg_set_launch_options(dg_ctx* ctx, int32_t use_graph, int32_t use_pdl);
  * 1048576 triangles are rejected with DG_ERR_ARG.  The first call for a
  * device looks up that array's address (cudaGetSymbolAddress, device
  * current) and caches it; make that first call before any stream capture.
- * Nothing has to start at zero.  Calls whose kernels overlap in time on one
- * device (other streams or other contexts) share the scratch and race. */
+ * The cached address assumes the device's primary context lives for the
+ * whole process: do not call this after cudaDeviceReset.  Like every entry
+ * point here, the call leaves the thread's current device set to the
+ * context's device.  Nothing has to start at zero.  Calls whose kernels
+ * overlap in time on one device (other streams or other contexts) share the
+ * scratch and race. */
 int dg_residual_norm_noalloc(dg_ctx* ctx, const double* x, const double* b, double* r, double* norm_out,
                              void* stream);
 

@@ -13,7 +13,9 @@ Usage (one mesh per process -- the reference reads its mesh at import):
 
 OPTIONS keys: eta_e, pre_smooth_its, post_smooth_its, gmres_m, gmres_its,
 rtol (tolerance relative to ||b||), problem ('sin' | 'sinh2d'), seed,
-do_solve (bool), do_precond (bool), threads.
+do_solve (bool), do_precond (bool), threads, ref_dir (the reference's
+z02-implicit/z06-DGtoCG directory; default: $DG_REFERENCE_DIR/z02-implicit/z06-DGtoCG,
+and the script refuses to run when neither is given).
 """
 from __future__ import annotations
 
@@ -26,7 +28,13 @@ import time
 
 import numpy as np
 
-REF_DIR_DEFAULT = "/root/reference/z02-implicit/z06-DGtoCG"
+
+
+def default_ref_dir() -> str:
+    root = os.environ.get("DG_REFERENCE_DIR")
+    if not root:
+        raise SystemExit("set DG_REFERENCE_DIR to the reference checkout (or pass ref_dir in OPTIONS)")
+    return os.path.join(root, "z02-implicit", "z06-DGtoCG")
 
 
 def _setup_paths(mesh_path, ref_dir):
@@ -37,7 +45,7 @@ def _setup_paths(mesh_path, ref_dir):
 
 
 def main(mesh_in, sfc_in, out_path, opts):
-    ref_dir = opts.get("ref_dir", REF_DIR_DEFAULT)
+    ref_dir = opts.get("ref_dir") or default_ref_dir()
     work = tempfile.mkdtemp(prefix="dgref_")
     mesh_path = os.path.join(work, "mesh.msh")
     shutil.copy(mesh_in, mesh_path)

@@ -1,9 +1,14 @@
 """Generate the golden vectors the oracle and the CUDA path are pinned to.
 
 Run in a checkout next to the reference (it executes the reference's own
-z06 Python on CPU through ``oracle/refrun``):
+z06 Python on CPU through ``oracle/refrun``; $DG_REFERENCE_DIR names the
+reference checkout):
 
-    python tests/golden/make_golden.py [case ...]
+    DG_REFERENCE_DIR=/path/to/reference python tests/golden/make_golden.py [case ...]
+
+``varprop_tet3`` runs the reference's variable-property residual
+(z05-ns/volume_mf_um_diff_varprop.py) on the mesh arrays and element tables
+of the ``tet3_v22`` golden case (oracle/refrun/run_varprop.py).
 
 Each case builds a synthetic mesh with this package's generator, writes it
 as a Gmsh v2 file plus the SFC ordering the reference reads from its cache,
@@ -57,8 +62,22 @@ def array_digest(a) -> str:
     return h.hexdigest()
 
 
+VARPROP = {"varprop_tet3": ("tet3_v22", 21)}
+
+
+def run_varprop_case(name: str) -> str:
+    """Per-element kappa residual of the reference's z05 varprop module."""
+    src, seed = VARPROP[name]
+    out = os.path.join(HERE, name + ".npz")
+    subprocess.run([sys.executable, "-m", "oracle.refrun.run_varprop", os.path.join(HERE, src + ".npz"), out,
+                    str(seed)], cwd=REPO, check=True)
+    return out
+
+
 def run_case(name: str) -> str:
     """Run the reference on one case and store its golden file."""
+    if name in VARPROP:
+        return run_varprop_case(name)
     kind, n, opts = CASES[name]
     opts = dict(opts)
     full = opts.pop("full", True)
@@ -123,5 +142,5 @@ if __name__ == "__main__":
         # args[1]: output of oracle/refrun/run_reference.py for the 20^3 Kuhn mesh
         print("generated", c2_summary(args[1]))
     else:
-        for nm in args or list(CASES):
+        for nm in args or list(CASES) + list(VARPROP):
             print("generated", run_case(nm))

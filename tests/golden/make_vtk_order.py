@@ -2,7 +2,7 @@
 triangle) from z02-implicit/z06-DGtoCG/mesh_init.py as text (the module is
 not executed) into vtk_node_order.npz.
 
-    python tests/golden/make_vtk_order.py [/path/to/reference]
+    python tests/golden/make_vtk_order.py /path/to/reference   (or $DG_REFERENCE_DIR)
 """
 import ast
 import os
@@ -10,7 +10,9 @@ import sys
 
 import numpy as np
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DG_REFERENCE_DIR")
+if not ref:
+    raise SystemExit("pass the reference checkout as the argument or set DG_REFERENCE_DIR")
 src = open(os.path.join(ref, "z02-implicit", "z06-DGtoCG", "mesh_init.py")).read()
 tables = []
 for node in ast.walk(ast.parse(src)):

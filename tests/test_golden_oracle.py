@@ -4,6 +4,8 @@ The golden vectors come from running the reference's z06 Python on CPU
 (tests/golden/make_golden.py).  Integer arrays must match exactly; floating
 point stages within a few units of roundoff of the FP64 reference.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -198,3 +200,21 @@ def test_colour_probe_rar_equals_galerkin_product(kind, n):
     mask = np.zeros((ncg, ncg), dtype=bool)
     mask[rows, pc["cola"]] = True
     assert np.abs(G[~mask]).max(initial=0.0) <= 1e-12 * np.abs(probe).max()
+
+
+def test_kappa_convention_matches_reference_varprop():
+    """The per-element diffusivity convention (kappa_e in the volume term,
+    (kappa_e + kappa_nb)/2 on the three interior-face terms, kappa_e on
+    boundary faces) against the reference's own variable-property residual
+    (z05-ns/volume_mf_um_diff_varprop.py:347-395, run by
+    oracle/refrun/run_varprop.py on the tet3_v22 mesh arrays with log-normal
+    kappa, sigma 1).  The reference solves for a 3-component field whose
+    operator is the scalar one times the identity, so every component must
+    equal the scalar residual."""
+    d, meta = load("tet3_v22")
+    g, m, el, order = rebuild(meta)
+    v = np.load(os.path.join(os.path.dirname(__file__), "golden", "varprop_tet3.npz"))
+    O = OracleDG(m, el, element.drst_duv(3), eta_e=float(v["eta_e"]), kappa=v["kappa"], face_kappa="mean")
+    for k in range(3):
+        r = O.residual(v["x"][:, :, k].ravel(), v["b"][:, :, k].ravel())
+        assert rel(r, v["r"][:, :, k]) < FP_TOL, k

@@ -2,8 +2,9 @@
 
 The reference solved this exact mesh and right-hand side on CPU in FP64
 (tests/golden/make_golden.py, c2_summary); the GPU path must take the same
-number of GMRES iterations and reproduce the solution within 1e-10 relative
-(max-abs over the sampled entries), the operator apply within 1e-12.
+number of GMRES iterations and reproduce the solution within 1e-12 relative
+(max-abs over the sampled entries; both Arnoldi orthogonalisations, the
+error printed), the operator apply within 1e-12.
 """
 import numpy as np
 import pytest
@@ -35,7 +36,8 @@ def test_c2_apply_and_rar(c2):
     assert int(s.info()["ncolor"]) == int(d["ncolor"])
 
 
-def test_c2_solve_matches_reference(c2):
+@pytest.mark.parametrize("ortho", ["cgs2", "mgs"])
+def test_c2_solve_matches_reference(c2, ortho):
     d, meta, m, s = c2
     X = m.x_ref_in
     f = 3 * np.pi ** 2 * np.prod([np.sin(np.pi * X[:, k]) for k in range(3)], axis=0).ravel()
@@ -43,12 +45,18 @@ def test_c2_solve_matches_reference(c2):
     assert abs(float(torch.linalg.norm(b)) - float(d["rhs_norm"])) <= 1e-12 * float(d["rhs_norm"])
     tol = 1e-10 * float(d["rhs_norm"])
     x = torch.zeros_like(b)
-    its, res = s.gmres(x, b, tol)
+    s.set_gmres_ortho(ortho)
+    try:
+        its, res = s.gmres(x, b, tol)
+    finally:
+        s.set_gmres_ortho("cgs2")
     xn = x.cpu().numpy()
+    err = rel(xn[::97], d["x_sub"])
+    print("c2 GMRES solution vs reference: ortho %s its %d max-abs rel err %.3e (sampled every 97th)" % (ortho, its, err))
     assert its == int(d["its"])
     assert res <= tol
-    assert rel(xn[::97], d["x_sub"]) < 1e-10
-    assert abs(np.linalg.norm(xn) - float(d["x_norm"])) <= 1e-10 * float(d["x_norm"])
+    assert err < 1e-12, (ortho, err)
+    assert abs(np.linalg.norm(xn) - float(d["x_norm"])) <= 1e-12 * float(d["x_norm"])
     u = np.prod([np.sin(np.pi * X[:, k]) for k in range(3)], axis=0).ravel()
-    # solutions agreeing to 1e-10 relative move the nodal error by <= ~1e-10
-    assert abs(np.abs(xn - u).max() - float(d["linferr"])) <= 1e-9
+    # solutions agreeing to 1e-12 relative move the nodal error by <= ~1e-12
+    assert abs(np.abs(xn - u).max() - float(d["linferr"])) <= 1e-11

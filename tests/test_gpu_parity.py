@@ -4,8 +4,10 @@ Every stage of the plain FP64 solve is compared on the committed golden
 cases (outputs of the reference itself), then on larger meshes against the
 CPU oracle, and at the 3D benchmark size through size-independent checks.
 Tolerances are relative max-abs errors: 1e-12 for single stages (FP64
-roundoff of a different summation order), 1e-10 for GMRES solutions
-(roundoff amplified by the iteration, bounded by the condition number).
+roundoff of a different summation order) and 1e-12 for the GMRES solutions,
+with both Arnoldi orthogonalisations (CGS2, the default, and modified
+Gram-Schmidt in the reference's order); each solution test prints the
+error it measured.
 """
 import numpy as np
 import pytest
@@ -19,7 +21,11 @@ from oracle.dg_oracle import OracleDG  # noqa: E402
 from golden_util import SMALL_CASES, harness_vectors, load, rebuild, rel  # noqa: E402
 
 STAGE_TOL = 1e-12
-SOL_TOL = 1e-10
+SOL_TOL = 1e-12
+# measured floor of the 2D benchmark mesh (32x32, 2,048 P3 triangles): the
+# GPU solution sits 1.62e-12 (CGS2) / 1.63e-12 (MGS) from the reference's,
+# so the orthogonalisation is not the cause; every other case is <= 3.4e-13
+SOL_FLOOR = {"tri32_c1": 2e-12}
 DEV = "cuda:0"
 
 
@@ -53,6 +59,7 @@ def test_apply_and_smoother(golden):
     name, d, meta, m, el, order, s = golden
     x, b, r_cg, rp = _inputs(name, d, m)
     r = s.residual(T(x), T(b))
+    print("stage apply %s: %.3e" % (name, rel(N(r), d["apply_r"])))
     assert rel(N(r), d["apply_r"]) < STAGE_TOL
     if "smooth_x" in d:
         xs = T(x)
@@ -86,21 +93,57 @@ def test_rhs(golden):
 def test_rar_vcycle_precond(golden):
     name, d, meta, m, el, order, s = golden
     x, b, r_cg, rp = _inputs(name, d, m)
-    assert rel(N(s.rar_values()), d["RARvalues"]) < STAGE_TOL
-    assert rel(N(s.mg_vcycle(T(r_cg))), d["mg_e"]) < STAGE_TOL
-    assert rel(N(s.precond(T(rp))), d["pc_x"]) < STAGE_TOL
+    e_rar = rel(N(s.rar_values()), d["RARvalues"])
+    e_mg = rel(N(s.mg_vcycle(T(r_cg))), d["mg_e"])
+    e_pc = rel(N(s.precond(T(rp))), d["pc_x"])
+    print("stage rar / vcycle / precond %s: %.3e %.3e %.3e" % (name, e_rar, e_mg, e_pc))
+    assert e_rar < STAGE_TOL and e_mg < STAGE_TOL and e_pc < STAGE_TOL
 
 
-def test_gmres_matches_reference(golden):
-    name, d, meta, m, el, order, s = golden
+@pytest.fixture(scope="module")
+def golden_quadrature_build(golden):
+    """The same golden case with the operator blocks from the quadrature
+    build (every element through the isoparametric Jacobian at each
+    quadrature point, the reference's own formula) instead of the affine
+    table build (reference matrices times per-element coefficients)."""
+    import os
+    name, d, meta, m, el, order, _ = golden
+    opts = meta["opts"]
+    cfg = SolverConfig(eta_e=opts.get("eta_e", 90.0), pre_smooth_its=opts.get("pre_smooth_its", 3),
+                       post_smooth_its=opts.get("post_smooth_its", 3))
+    old = os.environ.get("DG_BUILD_GENERAL")
+    os.environ["DG_BUILD_GENERAL"] = "1"
+    try:
+        s = DGSolver(m, order, cfg, el)
+        s.build_operator()
+    finally:
+        if old is None:
+            del os.environ["DG_BUILD_GENERAL"]
+        else:
+            os.environ["DG_BUILD_GENERAL"] = old
+    yield name, d, meta, m, el, order, s
+    s.close()
+
+
+@pytest.mark.parametrize("build", ["affine", "quadrature"])
+@pytest.mark.parametrize("ortho", ["cgs2", "mgs"])
+def test_gmres_matches_reference(golden, golden_quadrature_build, ortho, build):
+    name, d, meta, m, el, order, s = golden if build == "affine" else golden_quadrature_build
     opts = meta["opts"]
     bt = T(d["rhs"])
     tol = opts.get("rtol", 1e-10) * float(np.linalg.norm(d["rhs"]))
     xt = torch.zeros_like(bt)
-    its, res = s.gmres(xt, bt, tol, m=opts.get("gmres_m", 30), max_its=opts.get("gmres_its", 400))
+    s.set_gmres_ortho(ortho)
+    try:
+        its, res = s.gmres(xt, bt, tol, m=opts.get("gmres_m", 30), max_its=opts.get("gmres_its", 400))
+    finally:
+        s.set_gmres_ortho("cgs2")
+    err = rel(N(xt), d["x_solution"])
+    print("GMRES solution vs reference: case %s build %s ortho %s its %d max-abs rel err %.3e"
+          % (name, build, ortho, its, err))
     assert its == int(d["its"])
     assert res <= tol
-    assert rel(N(xt), d["x_solution"]) < SOL_TOL
+    assert err < SOL_FLOOR.get(name, SOL_TOL), (name, build, ortho, err)
 
 
 @pytest.fixture(scope="module")
@@ -179,3 +222,24 @@ def test_affine_block_build_matches_quadrature_build(kind, n, face_kappa, monkey
         s.close()
     for a, c in zip(outs["0"], outs["1"]):
         assert float(torch.abs(a - c).max() / torch.abs(c).max()) < 1e-13
+
+
+def test_kappa_operator_against_reference_varprop():
+    """GPU residual with per-element kappa (reference convention: mean face
+    kappa) against the reference's own variable-property residual
+    (z05-ns/volume_mf_um_diff_varprop.py, golden varprop_tet3), component by
+    component of the reference's 3-component field."""
+    import os
+    d, meta = load("tet3_v22")
+    g, m, el, order = rebuild(meta)
+    v = np.load(os.path.join(os.path.dirname(__file__), "golden", "varprop_tet3.npz"))
+    s = DGSolver(m, order, SolverConfig(eta_e=float(v["eta_e"])), el)
+    s.set_kappa(v["kappa"])
+    s.set_face_kappa("mean")
+    s.build_operator()
+    for k in range(3):
+        r = s.residual(T(v["x"][:, :, k]), T(v["b"][:, :, k]))
+        err = rel(N(r), v["r"][:, :, k])
+        print("kappa residual vs reference varprop, component %d: %.3e" % (k, err))
+        assert err < STAGE_TOL, (k, err)
+    s.close()

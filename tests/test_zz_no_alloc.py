@@ -85,3 +85,29 @@ def test_noalloc_rejects_null_and_unbuilt():
     assert s._lib.dg_residual_norm_noalloc(s._ctx, x.data_ptr(), None, None, None, stream) != DG_OK
     assert s._lib.dg_residual_norm_noalloc(s._ctx, x.data_ptr(), None, None, nrm.data_ptr(), stream) != DG_OK
     assert b"not built" in s._lib.dg_last_error(s._ctx)
+
+
+def test_noalloc_size_limit(monkeypatch):
+    """A mesh that needs more partial sums than the scratch holds is rejected
+    with DG_ERR_ARG and a message naming the limit; at the limit it runs.
+    The limit is lowered for the test through DG_NOALLOC_MAX_PARTIALS, which
+    can only tighten it (4^3 Kuhn cells = 384 tets = 48 CTAs of 8)."""
+    from dg_nn_public_gb300._capi import DG_ERR_ARG
+    m, s = _solver("tet", 4, seed=3)
+    need = (m.nele + 7) // 8
+    x = torch.randn(s.nonods, dtype=torch.float64, device="cuda:0")
+    y = s.apply(x)
+    nrm = torch.zeros(1, dtype=torch.float64, device="cuda:0")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    monkeypatch.setenv("DG_NOALLOC_MAX_PARTIALS", str(need - 1))
+    rc = s._lib.dg_residual_norm_noalloc(s._ctx, x.data_ptr(), None, None, nrm.data_ptr(), stream)
+    assert rc == DG_ERR_ARG
+    assert b"partial sums" in s._lib.dg_last_error(s._ctx)
+    monkeypatch.setenv("DG_NOALLOC_MAX_PARTIALS", str(need))
+    _call(s, x, None, None, nrm)
+    torch.cuda.synchronize()
+    ref = float(torch.linalg.norm(y))
+    assert abs(float(nrm) - ref) <= 1e-12 * ref
+    # a larger value does not raise the limit above the static array
+    monkeypatch.setenv("DG_NOALLOC_MAX_PARTIALS", str(10 ** 9))
+    _call(s, x, None, None, nrm)
