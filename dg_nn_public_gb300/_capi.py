@@ -75,6 +75,7 @@ _SIGNATURES = {
     "dg_p1cg_sparsity": (_I, [C.c_int64, C.c_int32, _P, C.c_int64, _P, _P, C.c_int64, _P]),
     "dg_color2": (_I, [C.c_int64, _P, _P, _P, _P]),
     "dg_nlevel_sfc": (C.c_int32, [C.c_int64]),
+    "dg_sfc_order": (_I, [C.c_int32, C.c_int64, _P, C.c_int32, _P]),
     "dg_sfc_levels": (_I, [C.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_int64, _P]),
     "dg_face_connectivity": (_I, [C.c_int32, C.c_int64, _P, _P, _P]),
     "dg_rap_contributions": (_I, [C.c_int32, C.c_int64, _P, _P, _P, _P, C.c_int64, _P, _P, C.c_int64, _P]),
@@ -177,6 +178,21 @@ def color2(fina, cola):
     nc = np.zeros(1, dtype=np.int32)
     check(lib().dg_color2(n, ptr(fina), ptr(cola), ptr(whichc), ptr(nc)))
     return whichc[:n], int(nc[0])
+
+
+def sfc_order(coords=None, order=None, bits: int = 0, ndim: int = None):
+    """dg_sfc_order: with coords, the Hilbert numbering of the points ((n, 1)
+    int64, 1-based); with order only, check a given numbering (e.g. the
+    reference's cached curve) and return it as (n, 1) int64."""
+    if coords is not None:
+        X = np.ascontiguousarray(coords, dtype=np.float64)
+        n, nd = X.shape
+        out = np.zeros(n, dtype=np.int64)
+        check(lib().dg_sfc_order(nd, n, ptr(X), bits, ptr(out)))
+        return out.reshape(n, 1)
+    o = np.ascontiguousarray(np.asarray(order).reshape(-1), dtype=np.int64)
+    check(lib().dg_sfc_order(ndim or 3, o.size, None, 0, ptr(o)))
+    return o.reshape(-1, 1)
 
 
 def nlevel_sfc(n: int) -> int:

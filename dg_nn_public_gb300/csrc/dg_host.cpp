@@ -2,6 +2,7 @@
 // SFC level hierarchy and face connectivity.  No CUDA calls: these entry
 // points work on machines without a GPU.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -292,11 +293,93 @@ int face_connectivity(int ndim, int64_t nele, const int64_t* corners, int64_t* n
   return DG_OK;
 }
 
+// Hilbert-curve index of integer coordinates q[0..ndim) in [0, 2^bits)
+// (Skilling, "Programming the Hilbert curve", AIP Conf. Proc. 707, 2004:
+// axes to transposed form, Gray decoding, then the bits interleaved most
+// significant first).
+int64_t hilbert_index(const int64_t* q, int ndim, int bits) {
+  int64_t x[3] = {0, 0, 0};
+  for (int i = 0; i < ndim; ++i) x[i] = q[i];
+  const int64_t m = (int64_t)1 << (bits - 1);
+  for (int64_t Q = m; Q > 1; Q >>= 1) {
+    const int64_t P = Q - 1;
+    for (int i = 0; i < ndim; ++i) {
+      if (x[i] & Q) {
+        x[0] ^= P;
+      } else {
+        const int64_t t = (x[0] ^ x[i]) & P;
+        x[0] ^= t;
+        x[i] ^= t;
+      }
+    }
+  }
+  for (int i = 1; i < ndim; ++i) x[i] ^= x[i - 1];
+  int64_t t = 0;
+  for (int64_t Q = m; Q > 1; Q >>= 1)
+    if (x[ndim - 1] & Q) t ^= Q - 1;
+  for (int i = 0; i < ndim; ++i) x[i] ^= t;
+  int64_t h = 0;
+  for (int b = bits - 1; b >= 0; --b)
+    for (int i = 0; i < ndim; ++i) h = (h << 1) | ((x[i] >> b) & 1);
+  return h;
+}
+
+// 1-based curve position of each point: coordinates scaled by the largest
+// extent onto a 2^bits grid (floor, clipped), sorted by Hilbert index with
+// ties by point index.
+int sfc_order_hilbert(int ndim, int64_t n, const double* coords, int bits, int64_t* order) {
+  if (n == 0) return DG_OK;
+  double lo[3], hi[3];
+  for (int d = 0; d < ndim; ++d) {
+    lo[d] = hi[d] = coords[d];
+    for (int64_t i = 1; i < n; ++i) {
+      lo[d] = std::min(lo[d], coords[i * ndim + d]);
+      hi[d] = std::max(hi[d], coords[i * ndim + d]);
+    }
+  }
+  double span = 0.0;
+  for (int d = 0; d < ndim; ++d) span = std::max(span, std::max(hi[d] - lo[d], 1e-300));
+  const double scale = (double)(((int64_t)1 << bits) - 1);
+  const int64_t qmax = ((int64_t)1 << bits) - 1;
+  std::vector<std::pair<int64_t, int64_t>> key(n);
+  for (int64_t i = 0; i < n; ++i) {
+    int64_t q[3] = {0, 0, 0};
+    for (int d = 0; d < ndim; ++d) {
+      const double v = std::floor((coords[i * ndim + d] - lo[d]) / span * scale);
+      q[d] = std::min<int64_t>(std::max<int64_t>((int64_t)v, 0), qmax);
+    }
+    key[i] = {hilbert_index(q, ndim, bits), i};
+  }
+  std::sort(key.begin(), key.end());
+  for (int64_t p = 0; p < n; ++p) order[key[p].second] = p + 1;
+  return DG_OK;
+}
+
 }  // namespace dg
 
 using namespace dg;
 
 extern "C" {
+
+int dg_sfc_order(int32_t ndim, int64_t n, const double* coords, int32_t bits, int64_t* order) {
+  if (n < 0 || !order || (ndim != 2 && ndim != 3))
+    return set_thread_error(DG_ERR_ARG, "dg_sfc_order: bad arguments");
+  if (!coords) {
+    // ordering in: a 1-based permutation, e.g. the reference's cached curve
+    std::vector<char> seen(n, 0);
+    for (int64_t i = 0; i < n; ++i) {
+      const int64_t p = order[i] - 1;
+      if (p < 0 || p >= n || seen[p])
+        return set_thread_error(DG_ERR_ARG, "dg_sfc_order: entry " + std::to_string(i) +
+                                                " is not part of a permutation of 1..n");
+      seen[p] = 1;
+    }
+    return DG_OK;
+  }
+  if (bits <= 0) bits = ndim == 2 ? 20 : 16;
+  if (bits * ndim > 62) return set_thread_error(DG_ERR_ARG, "dg_sfc_order: bits * ndim must be <= 62");
+  return sfc_order_hilbert(ndim, n, coords, bits, order);
+}
 
 int dg_p1cg_sparsity(int64_t nele, int32_t ncorner, const int64_t* p1cg, int64_t cg_nonods,
                      int64_t* fina, int64_t* cola, int64_t cap, int64_t* ncola) {

@@ -56,7 +56,14 @@ def _hilbert_index(q: np.ndarray, bits: int) -> np.ndarray:
 
 
 def hilbert_sfc_order(coords: np.ndarray, bits: int = 0) -> np.ndarray:
-    """1-based curve position of each point, shape (n, 1), ties by index."""
+    """1-based curve position of each point, shape (n, 1), ties by index,
+    computed by the library's host C++ (dg_sfc_order)."""
+    from . import _capi
+    return _capi.sfc_order(np.asarray(coords, dtype=np.float64), bits=bits)
+
+
+def hilbert_sfc_order_numpy(coords: np.ndarray, bits: int = 0) -> np.ndarray:
+    """The same numbering in numpy (cross-check of dg_sfc_order)."""
     coords = np.asarray(coords, dtype=np.float64)
     n, ndim = coords.shape
     if bits <= 0:

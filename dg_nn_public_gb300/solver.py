@@ -148,6 +148,7 @@ class DGSolver:
     def build_operator(self):
         self._chk(self._lib.dg_build_operator(self._ctx, self._stream()))
         self.built = True
+        self.build_count = getattr(self, "build_count", 0) + 1
 
     def bdiag(self):
         torch = _torch()

@@ -77,25 +77,107 @@ def _get_rhs(x_rhs, f, u_bc, alpha_x_i):
     return x_rhs
 
 
+def _host(a):
+    if a is None:
+        return None
+    if hasattr(a, "detach"):
+        return a.detach().cpu().numpy()
+    return np.asarray(a)
+
+
+def bound_p1cg_structures(s=None):
+    """P1CG sparsity (fina, cola, 0-based) and distance-2 colouring (whichc,
+    ncolor) of the bound mesh, as the reference forms them
+    (z06/sparsity.py:102-122, 235-269); host arrays, cached per solver."""
+    from . import _capi
+    s = s or ensure_operator()
+    st = getattr(s, "_p1cg_host", None)
+    if st is None:
+        fina, cola = _capi.p1cg_sparsity(s.mesh.p1cg, s.mesh.cg_nonods)
+        whichc, ncolor = _capi.color2(fina, cola)
+        st = dict(fina=fina, cola=cola, whichc=whichc, ncolor=ncolor)
+        s._p1cg_host = st
+    return st
+
+
+def _require_same(name, given, bound):
+    g = _host(given)
+    if g is None:
+        return
+    b = np.asarray(bound)
+    if g.shape != b.shape and g.size == b.size:
+        g = g.reshape(b.shape)
+    if g.shape != b.shape or not np.array_equal(g, b):
+        raise ValueError("%s differs from the bound mesh's (%s given, %s bound): the GPU operator is assembled "
+                         "for the mesh bound with state.bind(); rebind to use other structures"
+                         % (name, g.shape, b.shape))
+
+
 def _calc_RAR_mf_color(I_fc=None, I_cf=None, whichc=None, ncolor=None, spIdx_for_color=None,
                        colIdx_for_color=None, fina=None, cola=None, ncola=None):
-    """Colour-probe Galerkin P1CG operator values (:1696-1754).  The probe
-    structures are those of the bound mesh; the arguments are accepted for
-    signature compatibility."""
-    return ensure_operator().rar_values()
+    """Galerkin P1CG operator values of the bound mesh (:1696-1754).  The
+    arguments the reference passes are checked against the bound mesh's
+    P1CG structures: a different sparsity, colouring or transfer shape
+    raises ValueError instead of returning the bound operator silently."""
+    s = ensure_operator()
+    st = bound_p1cg_structures(s)
+    _require_same("fina", fina, st["fina"])
+    _require_same("cola", cola, st["cola"])
+    _require_same("whichc", whichc, st["whichc"])
+    if ncolor is not None and int(ncolor) != st["ncolor"]:
+        raise ValueError("ncolor %d differs from the bound mesh's %d" % (int(ncolor), st["ncolor"]))
+    if ncola is not None and int(ncola) != st["cola"].size:
+        raise ValueError("ncola %d differs from the bound mesh's %d" % (int(ncola), st["cola"].size))
+    ncg, ndg = s.mesh.cg_nonods, s.mesh.nele * (s.mesh.ndim + 1)
+    for name, M, shape in (("I_fc", I_fc, (ndg, ncg)), ("I_cf", I_cf, (ncg, ndg))):
+        if M is not None and tuple(M.shape) != shape:
+            raise ValueError("%s has shape %s, the bound mesh's is %s" % (name, tuple(M.shape), shape))
+    return s.rar_values()
+
+
+def _sfc_level_data(s):
+    """variables_sfc in the reference's format (multigrid_linearelastic.py:
+    42-109, 250-283): per level (torch CSR level matrix, diagonal (1, n), n),
+    the coarsest level as (scipy CSR, 0, n); built on the host from the
+    bound operator's P1CG values by the same aggregation the device levels
+    use (compact_fcode.f90 summation order)."""
+    import scipy.sparse as sp
+    import torch
+    from . import _capi
+    st = bound_p1cg_structures(s)
+    order = np.asarray(sf_nd_nb.sfc_data_Um.space_filling_curve_numbering).reshape(-1)
+    nl, start, rowp, col, val = _capi.sfc_levels(st["fina"], st["cola"], s.rar_values().cpu().numpy(), order)
+    out, sizes = [], []
+    for lev in range(nl):
+        r0, r1 = int(start[lev]), int(start[lev + 1])
+        n = r1 - r0
+        crow = rowp[r0:r1 + 1] - rowp[r0]
+        c = col[int(rowp[r0]):int(rowp[r1])]
+        v = val[int(rowp[r0]):int(rowp[r1])]
+        sizes.append(n)
+        if lev == nl - 1:
+            out.append((sp.csr_matrix((v.copy(), c.copy(), crow.copy()), shape=(n, n)), 0, n))
+            continue
+        diag = np.zeros((1, n))
+        rows = np.repeat(np.arange(n), np.diff(crow))
+        on = c == rows
+        diag[0, rows[on]] = v[on]
+        A = torch.sparse_csr_tensor(torch.tensor(crow), torch.tensor(c), torch.tensor(v), size=(n, n),
+                                    dtype=torch.float64)
+        out.append((A, torch.tensor(diag), n))
+    return nl, sizes, out
 
 
 def _get_RAR_and_sfc_data_Um():
-    """Assemble the P1CG operator and the SFC levels (:1642-1693)."""
+    """Assemble the P1CG operator and the SFC levels (:1642-1693); the level
+    data are stored in sf_nd_nb.sfc_data_Um as the reference stores them."""
     s = ensure_operator()
-    info = s.info()
     sd = sf_nd_nb.sfc_data_Um
-    n = int(info["cg_nonods"])
-    sizes = [n]
-    while sizes[-1] > 1:
-        sizes.append((sizes[-1] - 1) // 2 + 1)
-    sd.set_data(nlevel=int(info["nlevel"]), nodes_per_level=sizes,
-                variables_sfc=[(None, None, k) for k in sizes])
+    version = (id(s), s.build_count)
+    if getattr(sd, "_version", None) != version:
+        nl, sizes, levels = _sfc_level_data(s)
+        sd.set_data(nlevel=nl, nodes_per_level=sizes, variables_sfc=levels)
+        sd._version = version
     return 0
 
 

@@ -234,6 +234,18 @@ int dg_p1cg_sparsity(int64_t nele, int32_t ncorner, const int64_t* p1cg, int64_t
 /* Greedy distance-2 colouring in vertex order (z06/sparsity.py:235-269);
  * colours are 1-based. */
 int dg_color2(int64_t n, const int64_t* fina, const int64_t* cola, int64_t* whichc, int32_t* ncolor);
+/* Space-filling-curve numbering of the P1CG vertices, in the format of the
+ * reference's cache file <mesh>fluid_sfc.npy (z06/multigrid_linearelastic.py:
+ * 221-229): order[i] = 1-based position of vertex i along the curve.
+ * Ordering out (coords != NULL, (n, ndim) row-major): the vertices sorted by
+ * the Hilbert index of their coordinates on a 2^bits grid (bits <= 0: 20 in
+ * 2D, 16 in 3D), ties by vertex index -- a geometric curve in place of the
+ * reference's Fortran graph-bisection curve
+ * (z00-fortran-src/combined_fortran_source.f90:10575-10875), which needs a
+ * Fortran compiler.  Ordering in (coords == NULL): order holds a curve read
+ * from the reference's cache and is checked to be a permutation of 1..n;
+ * dg_create accepts it unchanged. */
+int dg_sfc_order(int32_t ndim, int64_t n, const double* coords, int32_t bits, int64_t* order);
 /* Number of SFC grid levels (z00-fortran-src/compact_fcode.f90:229-250). */
 int32_t dg_nlevel_sfc(int64_t nonods);
 /* All SFC grid levels of a CSR matrix (compact_fcode.f90:7-225):

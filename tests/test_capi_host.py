@@ -131,3 +131,29 @@ def test_rap_contributions_error_paths(lib):
         _capi.rap_contributions(3, p1, np.array([[5, -1, -1, -1]]), fina, cola)   # neighbour out of range
     with pytest.raises(_capi.DGError):
         _capi.rap_contributions(4, p1, nbe, fina, cola)                             # bad dimension
+
+
+@pytest.mark.parametrize("kind,n,seed", [("tet", 3, 0), ("tet", 20, 0), ("tri", 32, 0), ("tri", 5, 9)])
+def test_sfc_order_native_equals_numpy(lib, kind, n, seed):
+    """dg_sfc_order (ordering out) gives exactly the numpy Hilbert numbering
+    the golden cases were generated with, in the reference's cache format."""
+    from dg_nn_public_gb300 import mesh, sfc
+    m = mesh.build_mesh(kind, n, seed=seed)
+    a = sfc.hilbert_sfc_order(m.cg_coords)
+    assert a.shape == (m.cg_nonods, 1) and a.dtype == np.int64
+    assert np.array_equal(a, sfc.hilbert_sfc_order_numpy(m.cg_coords))
+    assert np.array_equal(np.sort(a.ravel()), np.arange(1, m.cg_nonods + 1))
+
+
+def test_sfc_order_in_validates_reference_curve(lib):
+    """Ordering in: a curve read from the reference's cache (golden 'sfc') is
+    accepted as is; a non-permutation is rejected with DG_ERR_ARG."""
+    from dg_nn_public_gb300 import _capi
+    d, _ = load("tet3_v22")
+    got = _capi.sfc_order(order=d["sfc"])
+    assert np.array_equal(got, d["sfc"])
+    bad = d["sfc"].copy()
+    bad[0] = bad[1]
+    with pytest.raises(_capi.DGError) as e:
+        _capi.sfc_order(order=bad)
+    assert e.value.code == _capi.DG_ERR_ARG

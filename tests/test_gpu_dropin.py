@@ -130,3 +130,40 @@ def test_bind_from_reference_objects(bound):
     r0 = torch.zeros(m.nele * m.nloc, dtype=torch.float64, device=DEV)
     r, _ = vmd.get_residual_or_smooth(r0, T(d["apply_x"]), T(d["apply_b"]))
     assert rel(r.cpu().numpy(), d["apply_r"]) < 1e-12
+
+
+def test_reference_structures_checked_and_levels_returned(bound):
+    """_calc_RAR_mf_color accepts the reference's own P1CG structures (golden
+    fina / cola / whichc / ncolor) and refuses altered ones; mg_on_P1CG_prep
+    returns the SFC levels in the reference's format with the reference's
+    values; mg_on_P1CG refuses level data other than the bound operator's."""
+    import scipy.sparse as sp
+    d, meta, m = bound
+    rar = vmd._calc_RAR_mf_color(whichc=d["whichc"], ncolor=int(d["ncolor"]), fina=d["fina"], cola=d["cola"],
+                                 ncola=int(d["cola"].size))
+    assert rel(rar.cpu().numpy(), d["RARvalues"]) < 1e-12
+    bad = d["cola"].copy()
+    bad[[0, 1]] = bad[[1, 0]]
+    with pytest.raises(ValueError):
+        vmd._calc_RAR_mf_color(fina=d["fina"], cola=bad)
+    with pytest.raises(ValueError):
+        vmd._calc_RAR_mf_color(ncolor=int(d["ncolor"]) + 1)
+    sfc, variables, nlevel, npl = mg.mg_on_P1CG_prep()
+    assert nlevel == int(d["nlevel"]) and list(npl) == list(d["nodes_per_level"])
+    for lev in range(nlevel - 1):
+        A, diag, n = variables[lev]
+        assert n == npl[lev]
+        assert np.array_equal(A.crow_indices().numpy(), d["lev%d_crow" % lev])
+        assert np.array_equal(A.col_indices().numpy(), d["lev%d_col" % lev])
+        assert rel(A.values().numpy(), d["lev%d_val" % lev]) < 1e-12
+        assert rel(diag.numpy().ravel(), d["lev%d_diag" % lev]) < 1e-12
+    assert isinstance(variables[-1][0], sp.csr_matrix) and variables[-1][2] == npl[-1]
+    e = mg.mg_on_P1CG(T(d["mg_r"]), variables, nlevel, npl, m.cg_nonods)
+    assert rel(e.cpu().numpy(), d["mg_e"]) < 1e-12
+    A0, dg0, n0 = variables[0]
+    altered = [(torch.sparse_csr_tensor(A0.crow_indices(), A0.col_indices(), A0.values() * 2.0, size=A0.shape),
+                dg0, n0)] + list(variables[1:])
+    with pytest.raises(ValueError):
+        mg.mg_on_P1CG(T(d["mg_r"]), altered, nlevel, npl, m.cg_nonods)
+    with pytest.raises(ValueError):
+        mg.mg_on_P1CG(T(d["mg_r"]), variables, nlevel + 1, npl, m.cg_nonods)
