@@ -64,10 +64,15 @@ _SIGNATURES = {
     "dg_mg_vcycle": (_I, [_P, _P, _P, _P]),
     "dg_gmres": (_I, [_P, _P, _P, C.c_double, C.c_int32, C.c_int32, _P, _P, _P]),
     "dg_set_gmres_ortho": (_I, [_P, C.c_int32]),
+    "dg_set_build_mode": (_I, [_P, C.c_int32]),
     "dg_solve_mixed": (_I, [_P, _P, _P, C.c_double, C.c_int32, C.c_int32, C.c_double, _P, _P, _P, _P]),
     "dg_apply_f32": (_I, [_P, _P, _P, _P]),
     "dg_solve_mixed_batched": (_I, [_P, _P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_double, _P, _P, _P]),
     "dg_smooth_pc": (_I, [_P, _P, _P, _P, _P]),
+    "dg_apply_batched": (_I, [_P, _P, _P, _P]),
+    "dg_smooth_pc_batched": (_I, [_P, _P, _P, _P, _P]),
+    "dg_set_batched_kernel": (_I, [_P, C.c_int32]),
+    "dg_batched_tuning": (_I, [_P, _P, C.c_int32, _P]),
     "dg_precond_f32": (_I, [_P, _P, _P, _P]),
     "dg_set_mixed_options": (_I, [_P, C.c_int32, C.c_double, C.c_int32, C.c_int32]),
     "dg_set_launch_options": (_I, [_P, C.c_int32, C.c_int32]),

@@ -666,6 +666,12 @@ __global__ void __launch_bounds__(kBT, kBS) bres_mma_tma_kernel(
   }
 }
 
+}  // namespace
+
+#include "dg_batched_tc.cuh"
+
+namespace {
+
 // ---------------------------------------------------------------------------
 // DG <-> CG P1 transfers and SFC levels on kNR columns (thread per (row, RHS))
 
@@ -1023,9 +1029,30 @@ struct BatchState {
   float* inv = nullptr;
   double* r64 = nullptr;                    // (kNR, nonods) FP64 residuals, RHS-major
   int nblk = 0;
+  // BF16 blocks + smoother matrices in the padded tensor-core layout of
+  // bres_tc05_kernel (5,760 bytes per element), rebuilt per mixed build
+  __nv_bfloat16* tc = nullptr;
+  int tc_version = -1;
+  // smoothing-kernel autotuner: per-variant microseconds of one launch
+  // (-1 = not timed), the mixed build it was taken for
+  float tune_us[kBatchedVariants] = {-1.f, -1.f, -1.f, -1.f, -1.f};
+  int tune_version = -1;
 };
 
 void destroy_batch(void* batch) { delete static_cast<BatchState*>(batch); }
+
+// the padded tensor-core layout of the preconditioner's BF16 blocks
+int ensure_tc_layout(dg_ctx* c, Mixed& M, BatchState& S, cudaStream_t st) {
+  if (S.tc && S.tc_version == c->mixed_version) return DG_OK;
+  int rc;
+  if (!S.tc && (rc = dalloc(c, &S.tc, (size_t)c->B * (kTcElem / 2)))) return rc;
+  const int64_t tot = c->B * (int64_t)(kTcElem / 2);
+  tc_layout_kernel<<<nblk(tot, 256), 256, 0, st>>>(M.blk16, M.W16, S.tc, c->B);
+  bump();
+  CKL(c);
+  S.tc_version = c->mixed_version;
+  return DG_OK;
+}
 
 BatchState& batch_of(Mixed& M) {
   if (!M.batch) M.batch = new BatchState();
@@ -1077,6 +1104,93 @@ int bres(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, 
   return DG_OK;
 }
 
+// One batched smoothing / residual step with the preconditioner's BF16
+// copies, by kernel variant: 0 CUDA cores (one CTA per element), 1 / 2
+// mma.sync with 4 / 8 warps per element, 3 mma.sync persistent bulk-copy,
+// 4 tcgen05 persistent bulk-copy (accumulators in tensor memory)
+int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, const float* b, float* xo, int flags,
+            float* rr1, const float* ws, cudaStream_t st) {
+  switch (variant) {
+    case 0:
+      return bres<__nv_bfloat16>(c, M.blk16, M.W16, xx, b, nullptr, xo, flags, rr1, st, ws);
+    case 1:
+    case 2:
+      if (c->B > 0) {
+        if (variant == 2)
+          bres_mma_kernel<8><<<(unsigned)c->B, 256, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, b, nullptr, xo, c->B,
+                                                             flags, c->T.P, rr1, ws);
+        else
+          bres_mma_kernel<4><<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, b, nullptr, xo, c->B,
+                                                             flags, c->T.P, rr1, ws);
+      }
+      bump();
+      CKL(c);
+      return DG_OK;
+    case 3: {
+      const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kBS);
+      if (g)
+        bres_mma_tma_kernel<<<g, kBT, kBDyn, st>>>(M.blk16, M.W16, c->d_nbe, xx, b, nullptr, xo, c->B, flags, c->T.P,
+                                                   rr1, c->d_err, ws);
+      bump();
+      CKL(c);
+      return DG_OK;
+    }
+    default: {
+      int rc;
+      if ((rc = ensure_tc_layout(c, M, S, st))) return rc;
+      const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kTcCTA);
+      if (g)
+        bres_tc05_kernel<<<g, kTcT, kTcDyn, st>>>(S.tc, c->d_nbe, xx, b, nullptr, xo, c->B, flags, c->T.P, rr1,
+                                                  c->d_err, ws);
+      bump();
+      CKL(c);
+      return DG_OK;
+    }
+  }
+}
+
+// Smoothing-kernel autotuner of the batched solve: times every variant of
+// the full smoothing step (x and b given) on zeroed scratch vectors with
+// CUDA events (one warm launch, then 3 timed) once per mixed build, before
+// any graph capture, and keeps the fastest; DG_BATCHED_KERNEL pins one.
+int autotune_batched(dg_ctx* c, Mixed& M, BatchState& S, cudaStream_t st) {
+  if (c->batched_pinned || S.tune_version == c->mixed_version) return DG_OK;
+  const size_t nv = (size_t)c->nonods * kNR;
+  CK(c, cudaMemsetAsync(S.t1, 0, sizeof(float) * nv, st));
+  CK(c, cudaMemsetAsync(S.t2, 0, sizeof(float) * nv, st));
+  cudaEvent_t e0, e1;
+  CK(c, cudaEventCreate(&e0));
+  CK(c, cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bestv = c->batched_kernel;
+  for (int v = 0; v < kBatchedVariants; ++v) {
+    int rc = bsmooth(c, M, S, v, S.t1, S.t2, S.t6, RF_SMOOTH, nullptr, nullptr, st);
+    if (!rc) CK(c, cudaEventRecord(e0, st));
+    for (int it = 0; it < 3 && !rc; ++it) rc = bsmooth(c, M, S, v, S.t1, S.t2, S.t6, RF_SMOOTH, nullptr, nullptr, st);
+    if (rc) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return rc;
+    }
+    CK(c, cudaEventRecord(e1, st));
+    CK(c, cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    CK(c, cudaEventElapsedTime(&ms, e0, e1));
+    S.tune_us[v] = ms * 1e3f / 3.0f;
+    if (ms < best) {
+      best = ms;
+      bestv = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->batched_kernel = bestv;
+  S.tune_version = c->mixed_version;
+  if (c->verbose)
+    std::fprintf(stderr, "[autotune] batched smoothing kernel %d (%.1f us per launch)\n", bestv, best * 1e3f / 3.0f);
+  return DG_OK;
+}
+
 // batched preconditioner (same schedule as precond32, dense coarse level)
 int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   Mixed& M = mixed_of(c);
@@ -1090,30 +1204,8 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   // DG-level smoothing step k damped like the single-RHS preconditioner
   auto wsk = [&](int k) -> const float* { return (nsm == 2 || c->omegas_set) && k < 4 ? M.d_ws + k : nullptr; };
   auto pc = [&](const float* xx, float* xo, int flags, float* rr1, const float* ws) -> int {
-    if (bf && c->batched_mma && c->batched_tma) {
-      const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kBS);
-      if (g)
-        bres_mma_tma_kernel<<<g, kBT, kBDyn, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B, flags, c->T.P,
-                                                   rr1, c->d_err, ws);
-      bump();
-      CKL(c);
-      return (int)DG_OK;
-    }
-    if (bf && c->batched_mma) {
-      if (c->B > 0) {
-        if (c->batched_warps == 8)
-          bres_mma_kernel<8><<<(unsigned)c->B, 256, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B,
-                                                             flags, c->T.P, rr1, ws);
-        else
-          bres_mma_kernel<4><<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, r, nullptr, xo, c->B,
-                                                             flags, c->T.P, rr1, ws);
-      }
-      bump();
-      CKL(c);
-      return (int)DG_OK;
-    }
-    return bf ? bres<__nv_bfloat16>(c, M.blk16, M.W16, xx, r, nullptr, xo, flags, rr1, st, ws)
-              : bres<float>(c, M.blk, M.W, xx, r, nullptr, xo, flags, rr1, st, ws);
+    if (bf) return bsmooth(c, M, S, c->batched_kernel, xx, r, xo, flags, rr1, ws, st);
+    return bres<float>(c, M.blk, M.W, xx, r, nullptr, xo, flags, rr1, st, ws);
   };
   if ((rc = pc(nullptr, cur, RF_ZEROX | RF_SMOOTH, nullptr, wsk(0)))) return rc;
   for (int it = 1; it < nsm; ++it) {
@@ -1210,6 +1302,8 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
   if (!c->f32_tma) return fail(c, DG_ERR_STATE, "dg_solve_mixed_batched: needs the chunked FP32 block layout");
   if ((rc = ensure_batch(c, m))) return rc;
   CK(c, cudaFuncSetAttribute(bres_mma_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBDyn));
+  CK(c, cudaFuncSetAttribute(bres_tc05_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcDyn));
+  if ((rc = autotune_batched(c, M, batch_of(M), st))) return rc;
   CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));   // bulk-copy wait time-outs land here
   BatchState& S = batch_of(M);
   const int64_t n = c->nonods;
@@ -1353,5 +1447,89 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
     c->err = "batched solve reached the iteration limit";
     return DG_ERR_NOCONV;
   }
+  return DG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Multi-RHS operator stages on RHS-interleaved FP32 vectors (kNR = 64 right-
+// hand sides, x[(e * 20 + n) * 64 + q]), P3 tetrahedra.
+
+namespace {
+
+int batched_prep(dg_ctx* c, const char* name, cudaStream_t st) {
+  if (!c->built) return fail(c, DG_ERR_STATE, std::string(name) + ": operator not built");
+  if (c->D != 3) return fail(c, DG_ERR_ARG, std::string(name) + ": P3 tetrahedra only");
+  CK(c, cudaSetDevice(c->dev));
+  Mixed& M = mixed_of(c);
+  int rc;
+  if (!M.built || c->mixed_version != c->build_version) {
+    if ((rc = build_mixed(c, st))) return rc;
+    c->mixed_version = c->build_version;
+  }
+  if (!M.has5 && (rc = build_blk5(c, st))) return rc;
+  if ((rc = ensure_batch(c, 1))) return rc;
+  CK(c, cudaFuncSetAttribute(bres_mma_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBDyn));
+  CK(c, cudaFuncSetAttribute(bres_tc05_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcDyn));
+  return DG_OK;
+}
+
+}  // namespace
+
+// Y = A X for 64 right-hand sides with the FP32 operator copy (CUDA cores).
+extern "C" int dg_apply_batched(dg_ctx* c, const float* x, float* y, void* stream) {
+  if (!c || !x || !y) return set_thread_error(DG_ERR_ARG, "dg_apply_batched: null argument");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int rc;
+  if ((rc = batched_prep(c, "dg_apply_batched", st))) return rc;
+  Mixed& M = mixed_of(c);
+  return bres<float>(c, M.blk, M.W, x, nullptr, y, nullptr, RF_NEG, nullptr, st);
+}
+
+// One smoothing step of the batched preconditioner with its BF16 copies:
+// X_out = X + W (B - A X) for 64 right-hand sides (X NULL = zero guess),
+// through the batched kernel variant in use (dg_set_batched_kernel).
+extern "C" int dg_smooth_pc_batched(dg_ctx* c, const float* x, const float* b, float* x_out, void* stream) {
+  if (!c || !b || !x_out) return set_thread_error(DG_ERR_ARG, "dg_smooth_pc_batched: null argument");
+  if (x_out == x) return fail(c, DG_ERR_ARG, "dg_smooth_pc_batched: x_out must not alias x");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int rc;
+  if ((rc = batched_prep(c, "dg_smooth_pc_batched", st))) return rc;
+  if (!c->precond_bf16) return fail(c, DG_ERR_STATE, "dg_smooth_pc_batched: needs the BF16 preconditioner copies");
+  Mixed& M = mixed_of(c);
+  CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
+  return bsmooth(c, M, batch_of(M), c->batched_kernel, x, b, x_out, x ? RF_SMOOTH : (RF_SMOOTH | RF_ZEROX), nullptr,
+                 nullptr, st);
+}
+
+// Batched smoothing kernel variant: -1 = timed choice at the next batched
+// solve (default), 0 CUDA cores, 1 / 2 mma.sync per element (4 / 8 warps),
+// 3 mma.sync persistent bulk-copy, 4 tcgen05 persistent bulk-copy.
+// tune_us (may be NULL) receives the last timing per variant (us, -1 = not
+// timed) and *chosen the variant in use.
+extern "C" int dg_set_batched_kernel(dg_ctx* c, int32_t variant) {
+  if (!c) return set_thread_error(DG_ERR_ARG, "dg_set_batched_kernel: null context");
+  if (variant < -1 || variant >= kBatchedVariants)
+    return fail(c, DG_ERR_ARG, "dg_set_batched_kernel: variant must be -1 .. 4");
+  if (variant < 0) {
+    c->batched_pinned = false;
+    batch_of(mixed_of(c)).tune_version = -1;
+  } else {
+    c->batched_kernel = variant;
+    c->batched_pinned = true;
+  }
+  Mixed& M = mixed_of(c);
+  for (auto& g : M.graphs)
+    if (g) cudaGraphExecDestroy(g);
+  M.graphs.clear();
+  M.g_m = 0;
+  return DG_OK;
+}
+
+extern "C" int dg_batched_tuning(const dg_ctx* c, float* tune_us, int32_t n, int32_t* chosen) {
+  if (!c) return set_thread_error(DG_ERR_ARG, "dg_batched_tuning: null context");
+  const Mixed& M = mixed_of(const_cast<dg_ctx*>(c));
+  const BatchState* S = static_cast<const BatchState*>(M.batch);
+  for (int v = 0; tune_us && v < n && v < kBatchedVariants; ++v) tune_us[v] = S ? S->tune_us[v] : -1.0f;
+  if (chosen) *chosen = c->batched_kernel;
   return DG_OK;
 }

@@ -23,6 +23,7 @@ using namespace dg;
 namespace {
 
 constexpr int RED_TB = 256;
+constexpr int kBatchedVariants = 5;   // batched smoothing kernel variants (see dg_ctx::batched_kernel)
 std::atomic<long long> g_launches{0};   // kernels launched by this library
 inline void bump(long long k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
@@ -63,10 +64,16 @@ struct dg_ctx {
   // block of shared block i; nface_sh = interior faces
   int *d_fref5 = nullptr, *d_sfsrc = nullptr;
   // reference matrices of the affine block build; fast_build: -1 not yet
-  // checked, 1 all elements straight-sided, 0 otherwise (quadrature build)
+  // checked, 1 all elements straight-sided, 0 otherwise (quadrature build).
+  // general_build (default): every element through the isoparametric
+  // Jacobian at each quadrature point, the reference's own formula -- the
+  // FP64 solve then stays within 1e-13 of the reference's solution on the
+  // pinned cases (the affine build moves the 2D 32x32 case to 1.6e-12);
+  // dg_set_build_mode(ctx, 1) selects the affine build (~3.4x faster, equal
+  // to rounding) for per-request rebuilds
   double* d_ftab = nullptr;
   int fast_build = -1;
-  bool general_build = false;
+  bool general_build = true;
   // direct Galerkin P1CG operator from the blocks (default; DG_RAP_DIRECT=0
   // restores one FP64 apply per colour of the distance-2 colouring):
   // contribution lists (dg_rap_contributions, packed) and the per-block
@@ -167,6 +174,13 @@ struct dg_ctx {
   // of the per-element latency; kept as a tuning option)
   bool batched_tma = false;
   int batched_warps = 4;   // warps per CTA of the per-element batched smoothing kernel (4 or 8)
+  // batched BF16 smoothing kernel variant (bsmooth): 0 CUDA cores, 1 / 2
+  // mma.sync per element (4 / 8 warps), 3 mma.sync persistent bulk-copy, 4
+  // tcgen05 persistent bulk-copy; chosen by timing at the first batched
+  // solve of each mixed build unless pinned (DG_BATCHED_KERNEL or the older
+  // DG_BATCHED_MMA / _TMA / _WARPS switches)
+  int batched_kernel = 1;
+  bool batched_pinned = false;
   int tma_variant = 0;   // elements per group / stages / CTAs per SM of that kernel
   bool autotune = true;  // pick tma_variant by timing at the first mixed solve after a build
   bool verbose = false;
@@ -758,10 +772,10 @@ int dg_info(const dg_ctx* ctx, int64_t* out, int32_t nout) {
   if (!ctx || !out) return set_thread_error(DG_ERR_ARG, "dg_info: null argument");
   const bool sf = ctx->D == 3 && ctx->shared_faces && ctx->d_fref5 && ctx->f32_tma && ctx->bf16_tma &&
                   ctx->precond_bf16;
-  int64_t v[15] = {ctx->D, ctx->N, ctx->B, ctx->nonods, ctx->ncg, (int64_t)ctx->cola.size(), ctx->ncolor,
+  int64_t v[16] = {ctx->D, ctx->N, ctx->B, ctx->nonods, ctx->ncg, (int64_t)ctx->cola.size(), ctx->ncolor,
                    (int64_t)ctx->lev.size(), ctx->nbf, ctx->built ? 1 : 0, ctx->VG, ctx->SG, ctx->tma_variant,
-                   ctx->batched_tma ? 1 : 0, sf ? ctx->nface_sh : 0};
-  for (int i = 0; i < nout && i < 15; ++i) out[i] = v[i];
+                   ctx->batched_kernel == 3 ? 1 : 0, sf ? ctx->nface_sh : 0, ctx->batched_kernel};
+  for (int i = 0; i < nout && i < 16; ++i) out[i] = v[i];
   return DG_OK;
 }
 
@@ -815,6 +829,17 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (bw && bw[0]) c->batched_warps = std::atoi(bw) == 8 ? 8 : 4;
     const char* bm = std::getenv("DG_BATCHED_MMA");
     if (bm && bm[0]) c->batched_mma = bm[0] != '0';
+    if (bt2 || bw || bm) {
+      if ((bt2 && bt2[0]) || (bw && bw[0]) || (bm && bm[0])) {
+        c->batched_kernel = !c->batched_mma ? 0 : (c->batched_tma ? 3 : (c->batched_warps == 8 ? 2 : 1));
+        c->batched_pinned = true;
+      }
+    }
+    const char* bk = std::getenv("DG_BATCHED_KERNEL");
+    if (bk && bk[0]) {
+      c->batched_kernel = std::min(std::max(std::atoi(bk), 0), kBatchedVariants - 1);
+      c->batched_pinned = true;
+    }
     const char* pd = std::getenv("DG_PDL");
     if (pd && pd[0]) c->use_pdl = pd[0] != '0';
     const char* lh = std::getenv("DG_L2_HINT");
@@ -1374,6 +1399,15 @@ int dg_mg_vcycle(dg_ctx* c, const double* r_sfc, double* e_sfc, void* stream) {
   int rc = vcycle(c, r_sfc, st);
   if (rc) return rc;
   CK(c, cudaMemcpyAsync(e_sfc, c->lev[0].e, sizeof(double) * c->ncg, cudaMemcpyDeviceToDevice, st));
+  return DG_OK;
+}
+
+int dg_set_build_mode(dg_ctx* c, int32_t mode) {
+  if (!c) return set_thread_error(DG_ERR_ARG, "dg_set_build_mode: null context");
+  if (mode != 0 && mode != 1) return fail(c, DG_ERR_ARG, "dg_set_build_mode: mode must be 0 (quadrature) or 1 (affine)");
+  const bool general = mode == 0;
+  if (general != c->general_build) c->built = false;
+  c->general_build = general;
   return DG_OK;
 }
 

@@ -118,6 +118,9 @@ class SolveServer:
         free0, _ = torch.cuda.mem_get_info(self.device)
         s = DGSolver(self.meshes[n], self.orders[n], self.cfg, self.el)
         s.set_mixed_options(dense_max=self.dense_max)
+        # every request rebuilds the operator: the affine block build (equal
+        # to the quadrature build within 1e-13) keeps that rebuild short
+        s.set_build_mode("affine")
         slot = _Slot(s)
         if n not in self.footprint:
             # warm set-up on a unit-kappa problem measures the slot's footprint

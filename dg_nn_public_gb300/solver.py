@@ -310,6 +310,45 @@ class DGSolver:
         self._chk(rc)
         return its, res
 
+    # -- multi-RHS stages (64 right-hand sides, RHS-interleaved FP32) ----
+    BATCHED_KERNELS = ("cuda_cores", "mma_sync4", "mma_sync8", "mma_sync_bulk", "tcgen05_bulk")
+
+    def _check_batched(self, t):
+        torch = _torch()
+        if t is None:
+            return None
+        if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and t.numel() == self.nonods * 64):
+            raise ValueError("expected a contiguous FP32 CUDA tensor of nonods x 64 (RHS-interleaved)")
+        return t.data_ptr()
+
+    def apply_batched(self, x, y=None):
+        """Y = A X for 64 RHS-interleaved FP32 right-hand sides."""
+        y = _torch().empty_like(x) if y is None else y
+        self._chk(self._lib.dg_apply_batched(self._ctx, self._check_batched(x), self._check_batched(y),
+                                             self._stream()))
+        return y
+
+    def smooth_pc_batched(self, x, b, x_out=None):
+        """X_out = X + W (B - A X) with the batched preconditioner's BF16
+        copies (x None = zero guess), through the batched kernel in use."""
+        x_out = _torch().empty_like(b) if x_out is None else x_out
+        self._chk(self._lib.dg_smooth_pc_batched(self._ctx, self._check_batched(x), self._check_batched(b),
+                                                 self._check_batched(x_out), self._stream()))
+        return x_out
+
+    def set_batched_kernel(self, kernel):
+        """Batched smoothing kernel: None / "auto" (timed choice at the next
+        batched solve) or one of BATCHED_KERNELS."""
+        v = -1 if kernel in (None, "auto") else self.BATCHED_KERNELS.index(kernel)
+        self._chk(self._lib.dg_set_batched_kernel(self._ctx, v))
+
+    def batched_tuning(self):
+        """(kernel in use, {kernel: us per launch} of the last timing)."""
+        us = np.full(len(self.BATCHED_KERNELS), -1.0, dtype=np.float32)
+        ch = C.c_int32(0)
+        self._chk(self._lib.dg_batched_tuning(self._ctx, us.ctypes.data, us.size, C.byref(ch)))
+        return self.BATCHED_KERNELS[ch.value], {k: float(u) for k, u in zip(self.BATCHED_KERNELS, us) if u >= 0}
+
     def set_mixed_options(self, smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=2400):
         """Mixed preconditioner: smoother 'jacobi3' (three point-Jacobi sweeps,
         as the reference) or 'blockinv' (smooth_w * A_ee^-1); BF16 block copies
@@ -346,6 +385,17 @@ class DGSolver:
             return its.value, res.value, outer.value
         self._chk(rc)
         return its.value, res.value, outer.value
+
+    def set_build_mode(self, mode):
+        """Element-block assembly: "quadrature" (default; the reference's
+        isoparametric formula at every quadrature point) or "affine"
+        (reference matrices times per-element factors for straight-sided
+        elements: equal to rounding, ~3.4x faster).  Next build_operator."""
+        modes = {"quadrature": 0, "affine": 1}
+        if mode not in modes:
+            raise ValueError("build mode must be one of %s" % sorted(modes))
+        self._chk(self._lib.dg_set_build_mode(self._ctx, modes[mode]))
+        self.built = False
 
     def set_gmres_ortho(self, mode):
         """Arnoldi orthogonalisation of ``gmres``: "cgs2" (default) or "mgs",

@@ -158,8 +158,11 @@ def _sfc_level_data(s):
         if lev == nl - 1:
             out.append((sp.csr_matrix((v.copy(), c.copy(), crow.copy()), shape=(n, n)), 0, n))
             continue
-        diag = np.zeros((1, n))
+        # rows sorted by column, as the reference's torch CSR level matrices
         rows = np.repeat(np.arange(n), np.diff(crow))
+        perm = np.lexsort((c, rows))
+        c, v = c[perm], v[perm]
+        diag = np.zeros((1, n))
         on = c == rows
         diag[0, rows[on]] = v[on]
         A = torch.sparse_csr_tensor(torch.tensor(crow), torch.tensor(c), torch.tensor(v), size=(n, n),

@@ -109,6 +109,14 @@ int dg_set_kappa(dg_ctx* ctx, const double* kappa /* [host] (nele) or NULL */);
  * under large kappa jumps (no counterpart in the reference).  Takes effect
  * at the next dg_build_operator. */
 int dg_set_face_kappa(dg_ctx* ctx, int32_t mode);
+/* Element-block assembly: mode 0 (default) evaluates every element through
+ * the isoparametric Jacobian at each quadrature point, the reference's own
+ * formula (z06/volume_mf_diff.py:487-617, 909-1556); mode 1 forms the blocks
+ * of straight-sided elements from reference matrices times per-element
+ * geometric factors (equal to mode 0 within 1e-13 relative, ~3.4x faster;
+ * curved elements still take mode 0).  Takes effect at the next
+ * dg_build_operator. */
+int dg_set_build_mode(dg_ctx* ctx, int32_t mode);
 /* Assemble the stored element blocks, the block diagonal, the Galerkin P1CG
  * operator (per-block products P^T A_b P summed over fixed contribution
  * lists; the environment variable DG_RAP_DIRECT=0 selects the reference's
@@ -180,6 +188,28 @@ int dg_apply_f32(dg_ctx* ctx, const float* x, float* y, void* stream);
  * The batched counterpart of _gmres_mg_solver (z06/volume_mf_diff.py:1757). */
 int dg_solve_mixed_batched(dg_ctx* ctx, double* x, const double* b, int32_t nrhs, const double* tol, int32_t m,
                            int32_t max_its, double inner_rtol, int32_t* its, double* res_norm, void* stream);
+/* Multi-RHS operator stages on RHS-interleaved FP32 vectors of 64 right-hand
+ * sides (x[(e * 20 + n) * 64 + q], P3 tetrahedra; the layout of the batched
+ * solve), the batched counterparts of get_residual_or_smooth
+ * (z06/volume_mf_diff.py:403-483) with its per-element bmm smoother
+ * (:474-480):
+ *   dg_apply_batched:     Y = A X with the FP32 operator copy;
+ *   dg_smooth_pc_batched: X_out = X + W (B - A X) with the preconditioner's
+ *                         BF16 block copies (X NULL = zero guess), through
+ *                         the batched smoothing kernel in use.
+ * x_out must not alias x. */
+int dg_apply_batched(dg_ctx* ctx, const float* x, float* y, void* stream);
+int dg_smooth_pc_batched(dg_ctx* ctx, const float* x, const float* b, float* x_out, void* stream);
+/* Kernel of the batched BF16 smoothing step (no counterpart in the
+ * reference): -1 = chosen by timing every variant at the next batched solve
+ * (the default, once per operator build), 0 = CUDA cores, 1 / 2 = mma.sync
+ * tensor-core tiles, one element per CTA (4 / 8 warps), 3 = mma.sync in a
+ * persistent bulk-copy pipeline, 4 = tcgen05.mma with tensor-memory
+ * accumulators in a persistent bulk-copy pipeline.  dg_batched_tuning
+ * reports the last timing per variant (microseconds per launch, -1 = not
+ * timed; tune_us may be NULL) and the variant in use. */
+int dg_set_batched_kernel(dg_ctx* ctx, int32_t variant);
+int dg_batched_tuning(const dg_ctx* ctx, float* tune_us, int32_t n, int32_t* chosen);
 /* z = the mixed-precision preconditioner applied once to r (FP32 vectors):
  * the DG->CG SFC V-cycle of dg_precond with the FP32/BF16 block copies and
  * the options of dg_set_mixed_options -- the reduced-precision counterpart
