@@ -380,7 +380,9 @@ def batched_leg(args, s, m, dofs, dev, stream, ws, R64=None, RMX=None):
     rel_b = max(float(torch.linalg.norm(s.residual(Xb[q].contiguous(), Bm[q].contiguous())) / tolb[q] * 1e-10)
                 for q in range(args.nrhs))
     err_b = float(np.abs(Xb.cpu().numpy() - Ub).max() / np.abs(Ub).max())
+    kern, tune_us = s.batched_tuning()
     return {
+        "smoothing_kernel": kern, "smoothing_kernel_us": tune_us,
         "workload": "c4: the %s mesh with %d Fourier right-hand sides (8 modes each, wavenumbers 1..4, "
                     "N(0,1) amplitudes, seed %d), solved together" % (
                         "c2" if args.n == 20 else "n=%d" % args.n, args.nrhs, args.seed + 2),
@@ -391,7 +393,8 @@ def batched_leg(args, s, m, dofs, dev, stream, ws, R64=None, RMX=None):
         "speedup_vs_single_mixed": (ws * args.nrhs * dofs * args.steps / tb) / RMX["value"] if RMX else None,
         "speedup_vs_fp64": (ws * args.nrhs * dofs * args.steps / tb) / R64["value"] if R64 else None,
         "method": "lockstep flexible GMRES(%d) on RHS-interleaved FP32 vectors; BF16 block smoothing on "
-                  "tensor cores (mma.sync m16n8k16, x split into BF16 hi+lo), FP32 apply on CUDA cores; "
+                  "tensor cores (x split into BF16 hi+lo; kernel chosen by the autotuner among CUDA cores, "
+                  "mma.sync tiles, mma.sync bulk-copy and tcgen05 bulk-copy), FP32 apply on CUDA cores; "
                   "per-RHS FP64 refinement" % args.batched_m}
 
 
