@@ -1035,11 +1035,20 @@ struct BatchState {
   int tc_version = -1;
   // smoothing-kernel autotuner: per-variant microseconds of one launch
   // (-1 = not timed), the mixed build it was taken for
-  float tune_us[kBatchedVariants] = {-1.f, -1.f, -1.f, -1.f, -1.f};
+  float tune_us[kBatchedVariants] = {-1.f, -1.f, -1.f, -1.f, -1.f, -1.f};
   int tune_version = -1;
+  // the preconditioner's iterates in the split tensor-core layout (variant 5)
+  unsigned char *xs1 = nullptr, *xs2 = nullptr;
 };
 
 void destroy_batch(void* batch) { delete static_cast<BatchState*>(batch); }
+
+int ensure_split(dg_ctx* c, BatchState& S) {
+  int rc;
+  if (!S.xs1 && (rc = dalloc(c, &S.xs1, (size_t)c->B * kSplit))) return rc;
+  if (!S.xs2 && (rc = dalloc(c, &S.xs2, (size_t)c->B * kSplit))) return rc;
+  return DG_OK;
+}
 
 // the padded tensor-core layout of the preconditioner's BF16 blocks
 int ensure_tc_layout(dg_ctx* c, Mixed& M, BatchState& S, cudaStream_t st) {
@@ -1047,7 +1056,7 @@ int ensure_tc_layout(dg_ctx* c, Mixed& M, BatchState& S, cudaStream_t st) {
   int rc;
   if (!S.tc && (rc = dalloc(c, &S.tc, (size_t)c->B * (kTcElem / 2)))) return rc;
   const int64_t tot = c->B * (int64_t)(kTcElem / 2);
-  tc_layout_kernel<<<nblk(tot, 256), 256, 0, st>>>(M.blk16, M.W16, S.tc, c->B);
+  tc_layout_kernel<<<nblk(tot, 256), 256, 0, st>>>(M.blk16, M.W16, c->d_nbe, S.tc, c->B);
   bump();
   CKL(c);
   S.tc_version = c->mixed_version;
@@ -1104,10 +1113,26 @@ int bres(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, 
   return DG_OK;
 }
 
+// split-x smoothing step (bres_tcs_kernel); x_out is split with RF_OUT_SPLIT
+int btcs(dg_ctx* c, BatchState& S, const unsigned char* xs, const float* b, void* xo, int flags, float* rr1,
+         const float* ws, cudaStream_t st) {
+  if (!S.tc || ((flags & RF_SMOOTH) && !xo) || ((flags & RF_RESTRICT) && !rr1) || !b)
+    return fail(c, DG_ERR_STATE, "batched split-x step: operand buffers not set up");
+  const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kTsCTA);
+  if (g)
+    bres_tcs_kernel<<<g, kTcT, kTsDyn, st>>>(S.tc, c->d_nbe, xs, b, nullptr, xo, c->B, flags | (xs ? 0 : RF_ZEROX),
+                                             c->T.P, rr1, c->d_err, ws);
+  bump();
+  CKL(c);
+  return DG_OK;
+}
+
 // One batched smoothing / residual step with the preconditioner's BF16
 // copies, by kernel variant: 0 CUDA cores (one CTA per element), 1 / 2
 // mma.sync with 4 / 8 warps per element, 3 mma.sync persistent bulk-copy,
-// 4 tcgen05 persistent bulk-copy (accumulators in tensor memory)
+// 4 tcgen05 persistent bulk-copy (accumulators in tensor memory), 5 tcgen05
+// on split x (the iterate already in the operand layout; FP32 x is split
+// first here, bprecond keeps its iterates split)
 int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, const float* b, float* xo, int flags,
             float* rr1, const float* ws, cudaStream_t st) {
   switch (variant) {
@@ -1135,7 +1160,7 @@ int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, co
       CKL(c);
       return DG_OK;
     }
-    default: {
+    case 4: {
       int rc;
       if ((rc = ensure_tc_layout(c, M, S, st))) return rc;
       const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kTcCTA);
@@ -1145,6 +1170,18 @@ int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, co
       bump();
       CKL(c);
       return DG_OK;
+    }
+    default: {
+      // split-x form on FP32 vectors: x converted to the split layout first
+      // (the preconditioner itself keeps its iterates split, bprecond)
+      int rc;
+      if ((rc = ensure_tc_layout(c, M, S, st)) || (rc = ensure_split(c, S))) return rc;
+      if (xx) {
+        const int64_t items = c->B * 20 * (kNR / 4);
+        to_split_kernel<<<nblk(items, 256), 256, 0, st>>>(xx, S.xs1, c->B);
+        bump();
+      }
+      return btcs(c, S, xx ? S.xs1 : nullptr, b, xo, flags & ~RF_OUT_SPLIT, rr1, ws, st);
     }
   }
 }
@@ -1163,10 +1200,18 @@ int autotune_batched(dg_ctx* c, Mixed& M, BatchState& S, cudaStream_t st) {
   CK(c, cudaEventCreate(&e1));
   float best = 1e30f;
   int bestv = c->batched_kernel;
+  if (!c->precond_bf16) return DG_OK;
+  int rc0;
+  if ((rc0 = ensure_tc_layout(c, M, S, st)) || (rc0 = ensure_split(c, S))) return rc0;
+  CK(c, cudaMemsetAsync(S.xs1, 0, (size_t)c->B * kSplit, st));
+  auto one = [&](int v) -> int {
+    if (v == 5) return btcs(c, S, S.xs1, S.t2, S.xs2, RF_SMOOTH | RF_OUT_SPLIT, nullptr, nullptr, st);
+    return bsmooth(c, M, S, v, S.t1, S.t2, S.t6, RF_SMOOTH, nullptr, nullptr, st);
+  };
   for (int v = 0; v < kBatchedVariants; ++v) {
-    int rc = bsmooth(c, M, S, v, S.t1, S.t2, S.t6, RF_SMOOTH, nullptr, nullptr, st);
+    int rc = one(v);
     if (!rc) CK(c, cudaEventRecord(e0, st));
-    for (int it = 0; it < 3 && !rc; ++it) rc = bsmooth(c, M, S, v, S.t1, S.t2, S.t6, RF_SMOOTH, nullptr, nullptr, st);
+    for (int it = 0; it < 3 && !rc; ++it) rc = one(v);
     if (rc) {
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
@@ -1207,12 +1252,29 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
     if (bf) return bsmooth(c, M, S, c->batched_kernel, xx, r, xo, flags, rr1, ws, st);
     return bres<float>(c, M.blk, M.W, xx, r, nullptr, xo, flags, rr1, st, ws);
   };
-  if ((rc = pc(nullptr, cur, RF_ZEROX | RF_SMOOTH, nullptr, wsk(0)))) return rc;
-  for (int it = 1; it < nsm; ++it) {
-    if ((rc = pc(cur, other, RF_SMOOTH, nullptr, wsk(it)))) return rc;
-    std::swap(cur, other);
+  // split-x pipeline: the iterate stays in the tensor-core operand layout
+  // from the first smoothing step to the last, which writes z in FP32
+  const bool split = bf && c->batched_kernel == 5;
+  unsigned char* scur = nullptr;
+  unsigned char* soth = nullptr;
+  if (split) {
+    if ((rc = ensure_tc_layout(c, M, S, st)) || (rc = ensure_split(c, S))) return rc;
+    scur = S.xs1;   // allocated by ensure_split just above
+    soth = S.xs2;
+    if ((rc = btcs(c, S, nullptr, r, scur, RF_ZEROX | RF_SMOOTH | RF_OUT_SPLIT, nullptr, wsk(0), st))) return rc;
+    for (int it = 1; it < nsm; ++it) {
+      if ((rc = btcs(c, S, scur, r, soth, RF_SMOOTH | RF_OUT_SPLIT, nullptr, wsk(it), st))) return rc;
+      std::swap(scur, soth);
+    }
+    if ((rc = btcs(c, S, scur, r, nullptr, RF_RESTRICT, S.r1, nullptr, st))) return rc;
+  } else {
+    if ((rc = pc(nullptr, cur, RF_ZEROX | RF_SMOOTH, nullptr, wsk(0)))) return rc;
+    for (int it = 1; it < nsm; ++it) {
+      if ((rc = pc(cur, other, RF_SMOOTH, nullptr, wsk(it)))) return rc;
+      std::swap(cur, other);
+    }
+    if ((rc = pc(cur, nullptr, RF_RESTRICT, S.r1, nullptr))) return rc;
   }
-  if ((rc = pc(cur, nullptr, RF_RESTRICT, S.r1, nullptr))) return rc;
   bgather_kernel<<<(unsigned)c->ncg, kNR, 0, st>>>(S.r1, c->d_gptr, c->d_gent, c->d_wdg, c->d_pos, S.lr[0],
                                                    (int)c->ncg);
   bump();
@@ -1244,6 +1306,20 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
       bump();
       std::swap(S.le[l], S.le2[l]);
     }
+  }
+  if (split) {
+    bprolong_split_kernel<<<(unsigned)c->B, 20 * (kNR / 4), 0, st>>>(scur, S.le[0], c->d_pos, c->d_p1cg, c->d_wdg,
+                                                                   c->T.P, c->B);
+    bump();
+    for (int it = 0; it < nsm; ++it) {
+      const bool last_step = it == nsm - 1;
+      if ((rc = btcs(c, S, scur, r, last_step ? (void*)z : (void*)soth, RF_SMOOTH | (last_step ? 0 : RF_OUT_SPLIT),
+                     nullptr, wsk(nsm - 1 - it), st)))
+        return rc;
+      std::swap(scur, soth);
+    }
+    CKL(c);
+    return DG_OK;
   }
   bprolong_kernel<<<(unsigned)c->B, 20 * (kNR / 4), 0, st>>>(cur, S.le[0], c->d_pos, c->d_p1cg, c->d_wdg, c->T.P,
                                                              c->B);
@@ -1303,6 +1379,7 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
   if ((rc = ensure_batch(c, m))) return rc;
   CK(c, cudaFuncSetAttribute(bres_mma_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBDyn));
   CK(c, cudaFuncSetAttribute(bres_tc05_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcDyn));
+  CK(c, cudaFuncSetAttribute(bres_tcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTsDyn));
   if ((rc = autotune_batched(c, M, batch_of(M), st))) return rc;
   CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));   // bulk-copy wait time-outs land here
   BatchState& S = batch_of(M);
@@ -1470,6 +1547,7 @@ int batched_prep(dg_ctx* c, const char* name, cudaStream_t st) {
   if ((rc = ensure_batch(c, 1))) return rc;
   CK(c, cudaFuncSetAttribute(bres_mma_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBDyn));
   CK(c, cudaFuncSetAttribute(bres_tc05_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcDyn));
+  CK(c, cudaFuncSetAttribute(bres_tcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTsDyn));
   return DG_OK;
 }
 
@@ -1509,7 +1587,7 @@ extern "C" int dg_smooth_pc_batched(dg_ctx* c, const float* x, const float* b, f
 extern "C" int dg_set_batched_kernel(dg_ctx* c, int32_t variant) {
   if (!c) return set_thread_error(DG_ERR_ARG, "dg_set_batched_kernel: null context");
   if (variant < -1 || variant >= kBatchedVariants)
-    return fail(c, DG_ERR_ARG, "dg_set_batched_kernel: variant must be -1 .. 4");
+    return fail(c, DG_ERR_ARG, "dg_set_batched_kernel: variant must be -1 .. 5");
   if (variant < 0) {
     c->batched_pinned = false;
     batch_of(mixed_of(c)).tune_version = -1;

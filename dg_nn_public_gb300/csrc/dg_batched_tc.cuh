@@ -105,7 +105,7 @@ constexpr uint32_t kTcIdescR = tc_idesc_bf16(128, 24, 0);   // Rop K-major
 // chunk c = rows m 0..19 x BF16 columns 8c .. 8c+7 (columns >= 20 zero);
 // built from the chunked BF16 copies (same values)
 __global__ void tc_layout_kernel(const __nv_bfloat16* __restrict__ blk16, const __nv_bfloat16* __restrict__ W16,
-                                 __nv_bfloat16* __restrict__ tc, int64_t B) {
+                                 const int* __restrict__ nbe, __nv_bfloat16* __restrict__ tc, int64_t B) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B * (kTcElem / 2)) return;
   const int64_t e = i / (kTcElem / 2);
@@ -113,7 +113,9 @@ __global__ void tc_layout_kernel(const __nv_bfloat16* __restrict__ blk16, const 
   const int j = rem / 480, w = rem % 480;        // slot j (0 = W, 1 + b = block b)
   const int ch = w / 160, m = (w % 160) / 8, n = 8 * ch + (w % 8);
   __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
-  if (n < 20) {
+  // boundary faces have no neighbour block: the slot is stored as zeros, so
+  // that a stale x slab in its place contributes nothing
+  if (n < 20 && (j <= 1 || nbe[e * 4 + j - 2] >= 0)) {
     const __nv_bfloat16* src = j == 0 ? W16 + e * 400 : blk16 + (e * 5 + (j - 1)) * 400;
     v = src[chunk20_index(m, n)];
   }
@@ -301,7 +303,7 @@ __global__ void __launch_bounds__(kTcT, kTcCTA) bres_tc05_kernel(
       r1[(e * F + c0) * kNR + q] = p0;
       r1[(e * F + c0 + 1) * kNR + q] = p1;
     }
-    if (smooth) {
+    if (smooth && !abort_flag) {   // abort_flag is uniform here (read after a barrier)
       // residual rows of the K-major operand: row 2q (hi) or 2q+1 (lo),
       // K slots n = 0..19 in groups of 8 (slots 20..31 stay zero)
 #pragma unroll
@@ -372,6 +374,335 @@ __global__ void __launch_bounds__(kTcT, kTcCTA) bres_tc05_kernel(
       (void)mbar_wait_bounded(&full[j % kTcStages], (uint32_t)((j / kTcStages) & 1));
     }
   }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
+}
+
+
+// ---------------------------------------------------------------------------
+// Split-x pipeline: the preconditioner's iterate is kept in global memory in
+// the tensor-core operand layout itself, so the smoothing kernel moves it to
+// shared memory with bulk copies and multiplies without converting.
+//
+// Split layout of one element's x (64 RHS, 20 nodes padded to 24), 6,144
+// bytes: K group kg = n / 8 (2,048 bytes) x M group mi = q / 4 (128 bytes) x
+// node row n % 8 (16 bytes) x (RHS q % 4) x (BF16 high part, BF16 rounding
+// of the remainder); nodes 20..23 are zero.  It is exactly one element's
+// three K groups of the MN-major operand, so the five slabs of an element
+// and its face neighbours, copied back to back, form the whole A operand.
+constexpr int kSplit = 6144;
+constexpr int RF_OUT_SPLIT = 32;                  // x_out in the split layout (else FP32 interleaved)
+constexpr int kTsStages = 2;
+constexpr int kTsCTA = 2;
+// stage: [W | blocks | zero chunk | x slabs (own, 4 faces) | zero K group | b slab]
+constexpr int kTsW = 0, kTsA = kTcWBytes, kTsZ = kTcElem, kTsX = kTcElem + kTcChunk;
+constexpr int kTsXZ = kTsX + 5 * kSplit, kTsB = kTsXZ + kTcLBO;
+constexpr int kTsStage = kTsB + 20 * kNR * 4;     // 43,968 bytes
+constexpr int kTsDyn = kTsStages * kTsStage + kTcRop + kSplit;
+
+__device__ __forceinline__ int split_off(int n, int q) {
+  return (n >> 3) * kTcLBO + (q >> 2) * 128 + (n & 7) * 16 + (q & 3) * 4;
+}
+
+__device__ __forceinline__ uint32_t split_pack(float v) {
+  const float h = __bfloat162float(__float2bfloat16_rn(v));
+  return pack_bf16x2(h, v - h);
+}
+
+__device__ __forceinline__ float split_value(uint32_t w) {
+  return __uint_as_float(w << 16) + __uint_as_float(w & 0xFFFF0000u);
+}
+
+__device__ __forceinline__ void bulk_store_s2g(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+               "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// FP32 interleaved -> split (one thread per (element, node, 4 RHS))
+__global__ void to_split_kernel(const float* __restrict__ x, unsigned char* __restrict__ xs, int64_t B) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= B * 20 * (kNR / 4)) return;
+  const int64_t e = t / (20 * (kNR / 4));
+  const int rem = (int)(t - e * (20 * (kNR / 4)));
+  const int n = rem / (kNR / 4), q4 = rem % (kNR / 4);
+  const float4 v = reinterpret_cast<const float4*>(x + (e * 20 + n) * kNR)[q4];
+  *reinterpret_cast<uint4*>(xs + e * kSplit + split_off(n, 4 * q4)) = split_hilo4(v);
+}
+
+// x (split) += P (w * ecg) at the element's corners: the P1 -> P3 coarse
+// correction of bprolong_kernel on the split layout
+__global__ void __launch_bounds__(320) bprolong_split_kernel(unsigned char* __restrict__ xs,
+                                                             const float* __restrict__ ecg, const int* __restrict__ pos,
+                                                             const int* __restrict__ p1cg,
+                                                             const double* __restrict__ wdg,
+                                                             const double* __restrict__ P, int64_t B) {
+  __shared__ int vp[4];
+  __shared__ float wc[4];
+  __shared__ float Ps[20][4];
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x;
+  if (tid < 4) {
+    vp[tid] = pos[p1cg[e * 4 + tid]];
+    wc[tid] = (float)wdg[e * 4 + tid];
+  }
+  if (tid < 80) Ps[tid / 4][tid % 4] = (float)P[tid];
+  __syncthreads();
+  const int n = tid / (kNR / 4), q4 = tid % (kNR / 4);
+  float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float4 ev = reinterpret_cast<const float4*>(ecg + (int64_t)vp[c] * kNR)[q4];
+    const float f = Ps[n][c] * wc[c];
+    v.x += f * ev.x;
+    v.y += f * ev.y;
+    v.z += f * ev.z;
+    v.w += f * ev.w;
+  }
+  uint4* p = reinterpret_cast<uint4*>(xs + e * kSplit + split_off(n, 4 * q4));
+  const uint4 w = *p;
+  const float4 xv = make_float4(split_value(w.x) + v.x, split_value(w.y) + v.y, split_value(w.z) + v.z,
+                                split_value(w.w) + v.w);
+  *p = split_hilo4(xv);
+}
+
+// The batched smoothing / residual step on split x: flags as bres_kernel
+// plus RF_OUT_SPLIT; x (split) of the element and its face neighbours, its
+// blocks, smoother matrix and b slab arrive by bulk copies into a ring of
+// kTsStages stages; D = Aop * Bop on the tensor cores (Aop = the copied x
+// slabs, no conversion); epilogue as bres_tc05_kernel, with x_out written in
+// the split layout through a staging buffer and one bulk store per element,
+// or as FP32.
+__global__ void __launch_bounds__(kTcT, kTsCTA) bres_tcs_kernel(
+    const __nv_bfloat16* __restrict__ tcblk, const int* __restrict__ nbe, const unsigned char* __restrict__ xs,
+    const float* __restrict__ b, float* __restrict__ r, void* __restrict__ x_out, int64_t B, int flags,
+    const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const float* __restrict__ wsp) {
+  constexpr int N = 20, F = 4;
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  unsigned char* stages = tsm;
+  unsigned char* Rop = tsm + kTsStages * kTsStage;
+  unsigned char* Out = Rop + kTcRop;
+  __shared__ __align__(8) uint64_t full[kTsStages];
+  __shared__ __align__(8) uint64_t mma_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ float Ps[N][F];
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const bool zerox = flags & RF_ZEROX;
+  const bool smooth = flags & RF_SMOOTH;
+  const bool restrict_ = flags & RF_RESTRICT;
+  const bool out_split = flags & RF_OUT_SPLIT;
+  const float ws = wsp ? *wsp : 1.0f;
+  const float sgn = (flags & RF_NEG) ? -1.0f : 1.0f;
+  const int64_t stride = gridDim.x;
+  for (int i = tid; i < kTsDyn / 16; i += kTcT) reinterpret_cast<uint4*>(tsm)[i] = make_uint4(0u, 0u, 0u, 0u);
+  for (int i = tid; i < N * F; i += kTcT) Ps[i / F][i % F] = (float)P[i];
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < kTsStages; ++s) mbar_init(&full[s], 1);
+    mbar_init(&mma_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  fence_async_smem();
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                 "r"(kTcCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+
+  auto issue = [&](int64_t k) {
+    const int64_t e = blockIdx.x + k * stride;
+    if (e >= B) return;
+    const int s = (int)(k % kTsStages);
+    unsigned char* st = stages + (size_t)s * kTsStage;
+    const unsigned char* src = reinterpret_cast<const unsigned char*>(tcblk) + (size_t)e * kTcElem;
+    int nb[F] = {-1, -1, -1, -1};
+    uint32_t bytes = 0;
+    if (smooth) bytes += kTcWBytes;
+    if (!zerox) {
+      const int4 n4 = reinterpret_cast<const int4*>(nbe)[e];
+      nb[0] = n4.x;
+      nb[1] = n4.y;
+      nb[2] = n4.z;
+      nb[3] = n4.w;
+      bytes += kTcABytes + kSplit;
+      for (int f = 0; f < F; ++f)
+        if (nb[f] >= 0) bytes += kSplit;
+    }
+    if (b) bytes += 20 * kNR * 4;
+    mbar_expect_tx(&full[s], bytes);
+    if (smooth && !zerox)
+      bulk_copy_g2s(st + kTsW, src, kTcElem, &full[s]);
+    else if (smooth)
+      bulk_copy_g2s(st + kTsW, src, kTcWBytes, &full[s]);
+    else if (!zerox)
+      bulk_copy_g2s(st + kTsA, src + kTcWBytes, kTcABytes, &full[s]);
+    if (!zerox) {
+      bulk_copy_g2s(st + kTsX, xs + e * kSplit, kSplit, &full[s]);
+      for (int f = 0; f < F; ++f)   // a boundary face keeps a stale slab: its block is zero
+        if (nb[f] >= 0) bulk_copy_g2s(st + kTsX + (1 + f) * kSplit, xs + (int64_t)nb[f] * kSplit, kSplit, &full[s]);
+    }
+    if (b) bulk_copy_g2s(st + kTsB, b + e * (int64_t)N * kNR, 20 * kNR * 4, &full[s]);
+  };
+  if (tid == 0)
+    for (int k = 0; k < kTsStages; ++k) issue(k);
+
+  const int q = tid >> 1, part = tid & 1;
+  uint32_t mma_phase = 0;
+  int64_t k = 0;
+  for (int64_t e = blockIdx.x; e < B; e += stride, ++k) {
+    const int s = (int)(k % kTsStages);
+    unsigned char* st = stages + (size_t)s * kTsStage;
+    if (!mbar_wait_bounded(&full[s], (uint32_t)((k / kTsStages) & 1))) abort_flag = 1;
+    __syncthreads();
+    if (abort_flag) {
+      if (tid == 0) atomicExch(err, 3);
+      break;
+    }
+    float v[24];
+#pragma unroll
+    for (int i = 0; i < 24; ++i) v[i] = 0.0f;
+    if (!zerox) {
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t a0 = smem_addr(st + kTsX), b0 = smem_addr(st + kTsA);
+#pragma unroll
+        for (int ks = 0; ks < 8; ++ks)
+          tc_mma(tmem, tc_sdesc(a0 + ks * 2 * kTcLBO, kTcLBO, 128), tc_sdesc(b0 + ks * 2 * kTcChunk, kTcChunk, 128),
+                 kTcIdescA, ks > 0 ? 1u : 0u);
+        tc_commit(&mma_bar);
+        if (!mbar_wait_bounded(&mma_bar, mma_phase)) {
+          atomicExch(err, 3);
+          abort_flag = 1;
+        }
+      }
+      mma_phase ^= 1u;
+      __syncthreads();
+      tc_fence_after();
+      if (!abort_flag) {
+        float t8[8];
+#pragma unroll
+        for (int c8 = 0; c8 < 3; ++c8) {
+          tc_ld8(lane_base + 8 * c8, t8);
+          tc_wait_ld();
+#pragma unroll
+          for (int i = 0; i < 8; ++i) v[8 * c8 + i] = t8[i];
+        }
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < N; ++n) v[n] += __shfl_xor_sync(0xffffffffu, v[n], 1);
+    const float* bst = reinterpret_cast<const float*>(st + kTsB);
+    float res[N];
+#pragma unroll
+    for (int n = 0; n < N; ++n) res[n] = (b ? bst[n * kNR + q] : 0.0f) - v[n];
+    if (r) {
+#pragma unroll
+      for (int n0 = 0; n0 < N; n0 += 2) r[(e * N + n0 + part) * kNR + q] = sgn * (part ? res[n0 + 1] : res[n0]);
+    }
+    if (restrict_) {
+      float p0 = 0.f, p1 = 0.f;
+      const int c0 = 2 * part;
+#pragma unroll
+      for (int n = 0; n < N; ++n) {
+        p0 = fmaf(Ps[n][c0], res[n], p0);
+        p1 = fmaf(Ps[n][c0 + 1], res[n], p1);
+      }
+      r1[(e * F + c0) * kNR + q] = p0;
+      r1[(e * F + c0 + 1) * kNR + q] = p1;
+    }
+    if (smooth && !abort_flag) {   // abort_flag is uniform here (read after a barrier)
+#pragma unroll
+      for (int g = 0; g < 3; ++g) {
+        uint32_t wv[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int n0 = 8 * g + 2 * h;
+          float a0 = n0 < N ? res[n0] : 0.0f, a1 = n0 + 1 < N ? res[n0 + 1] : 0.0f;
+          if (part) {
+            a0 -= __bfloat162float(__float2bfloat16_rn(a0));
+            a1 -= __bfloat162float(__float2bfloat16_rn(a1));
+          }
+          wv[h] = pack_bf16x2(a0, a1);
+        }
+        *reinterpret_cast<uint4*>(Rop + g * kTcLBO + (tid >> 3) * 128 + (tid & 7) * 16) =
+            make_uint4(wv[0], wv[1], wv[2], wv[3]);
+      }
+      if (tid == 0 && out_split) bulk_wait_read();   // the staging buffer's previous store has been read
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t a0 = smem_addr(Rop), b0 = smem_addr(st + kTsW);
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks)
+          tc_mma(tmem + 32, tc_sdesc(a0 + ks * 2 * kTcLBO, kTcLBO, 128),
+                 tc_sdesc(b0 + ks * 2 * kTcChunk, kTcChunk, 128), kTcIdescR, ks > 0 ? 1u : 0u);
+        tc_commit(&mma_bar);
+        if (!mbar_wait_bounded(&mma_bar, mma_phase)) {
+          atomicExch(err, 3);
+          abort_flag = 1;
+        }
+      }
+      mma_phase ^= 1u;
+      __syncthreads();
+      tc_fence_after();
+      if (!abort_flag) {
+        float c[24], t8[8];
+#pragma unroll
+        for (int c8 = 0; c8 < 3; ++c8) {
+          tc_ld8(lane_base + 32 + 8 * c8, t8);
+          tc_wait_ld();
+#pragma unroll
+          for (int i = 0; i < 8; ++i) c[8 * c8 + i] = t8[i];
+        }
+#pragma unroll
+        for (int n = 0; n < N; ++n) c[n] += __shfl_xor_sync(0xffffffffu, c[n], 1);
+        const unsigned char* xo_own = st + kTsX;
+#pragma unroll
+        for (int n0 = 0; n0 < N; n0 += 2) {
+          const int n = n0 + part;
+          const float xv = zerox ? 0.0f : split_value(*reinterpret_cast<const uint32_t*>(xo_own + split_off(n, q)));
+          const float xo = xv + ws * (part ? c[n0 + 1] : c[n0]);
+          if (out_split)
+            *reinterpret_cast<uint32_t*>(Out + split_off(n, q)) = split_pack(xo);
+          else
+            reinterpret_cast<float*>(x_out)[(e * N + n) * kNR + q] = xo;
+        }
+        if (out_split) {
+          fence_async_smem();
+          __syncthreads();
+          if (tid == 0) bulk_store_s2g(reinterpret_cast<unsigned char*>(x_out) + e * kSplit, Out, kSplit);
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();   // stage s, Rop and the accumulators are free again
+    if (abort_flag) break;
+    if (tid == 0) {
+      fence_async_smem();
+      issue(k + kTsStages);
+    }
+  }
+  if (abort_flag && tid == 0) {
+    for (int64_t j = k; j < k + kTsStages; ++j) {
+      if (blockIdx.x + j * stride >= B) break;
+      (void)mbar_wait_bounded(&full[j % kTsStages], (uint32_t)((j / kTsStages) & 1));
+    }
+  }
+  if (tid == 0) bulk_wait_all();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();

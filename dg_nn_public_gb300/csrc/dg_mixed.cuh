@@ -83,6 +83,10 @@ struct Mixed {
   // nblk4 = ceil(nonods / 4 / 256) blocks, KMAXV sums per block
   double* part = nullptr;
   int nblk4 = 0;
+  // arrival counters of the fused Gram-Schmidt kernels (the last CTA of a
+  // launch reduces the partial sums and resets its counter): [0, 32) one per
+  // grid row of the dots, [32] the update's norm
+  unsigned* gs_cnt = nullptr;
   // batched (multi-RHS) solve state (dg_batched.cuh)
   void* batch = nullptr;
 };
@@ -1430,6 +1434,8 @@ int ensure_krylov32(dg_ctx* c, int m) {
   if (!M.part) {
     M.nblk4 = (int)((c->nonods / 4 + RED_TB - 1) / RED_TB);
     if ((rc = dalloc(c, &M.part, (size_t)std::max(M.nblk4, 1) * KMAXV))) return rc;
+    if ((rc = dalloc(c, &M.gs_cnt, 64))) return rc;
+    CK(c, cudaMemset(M.gs_cnt, 0, sizeof(unsigned) * 64));
   }
   if (!M.gv) {   // sized for the largest restart length (256)
     if ((rc = dalloc(c, &M.gv, (size_t)3 * 256 + 2))) return rc;
@@ -1590,6 +1596,136 @@ __global__ void scale4_f32_kernel(const float* __restrict__ z, const float* __re
   reinterpret_cast<float4*>(v)[k] = a;
 }
 
+// The same dots with the block reduction fused: each CTA writes its partial
+// sums, and the last CTA of a grid row (arrival counter) adds the rows'
+// partials in block order -- warp q sums vector q's partials, lanes strided,
+// then a fixed shuffle tree -- and writes h[i0 + q]; it resets the counter
+// for the next launch.  One launch per step instead of two.
+template <int TB>
+__global__ void __launch_bounds__(TB) mdot8r_f32_kernel(const float* __restrict__ V, int64_t ld, int nv,
+                                                        const float* __restrict__ z, int64_t n4,
+                                                        double* __restrict__ partial, double* __restrict__ h,
+                                                        unsigned* __restrict__ cnt_arr) {
+  pdl_wait_then_trigger();
+  __shared__ float red[TB / 32][8];
+  __shared__ bool last;
+  const int i0 = blockIdx.y * 8;
+  const int cnt = min(8, nv - i0);
+  float acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = 0.0f;
+  const float4* z4 = reinterpret_cast<const float4*>(z);
+  for (int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x; k < n4; k += (int64_t)gridDim.x * TB) {
+    const float4 zv = z4[k];
+    float4 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      v[q] = q < cnt ? reinterpret_cast<const float4*>(V + (size_t)(i0 + q) * ld)[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      acc[q] = fmaf(v[q].x, zv.x, acc[q]);
+      acc[q] = fmaf(v[q].y, zv.y, acc[q]);
+      acc[q] = fmaf(v[q].z, zv.z, acc[q]);
+      acc[q] = fmaf(v[q].w, zv.w, acc[q]);
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const float a = warp_sum_f(acc[q]);
+    if (lane == 0) red[wid][q] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x < cnt) {
+    double s = 0.0;
+    for (int w = 0; w < TB / 32; ++w) s += (double)red[w][threadIdx.x];
+    partial[(int64_t)blockIdx.x * KMAXV + i0 + threadIdx.x] = s;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&cnt_arr[blockIdx.y], 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (wid < cnt) {
+    double s = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&partial[(int64_t)b * KMAXV + i0 + wid]);
+    s = warp_sum(s);
+    if (lane == 0) h[i0 + wid] = s;
+  }
+  if (threadIdx.x == 0) cnt_arr[blockIdx.y] = 0u;
+}
+
+// z -= sum_i V[i] h[i] with |z_new|^2, and in the last CTA (arrival
+// counter) the Hessenberg column: Hc[i] = h1[i] (+ h2[i]), Hc[nv] = |z|,
+// *inv = 1 / |z| -- the update and cgs_finish_kernel in one launch.
+template <int TB>
+__global__ void __launch_bounds__(TB) axpy8f_f32_kernel(const float* __restrict__ V, int64_t ld, int nv,
+                                                        const double* __restrict__ h, float* __restrict__ z,
+                                                        int64_t n4, double* __restrict__ partial,
+                                                        const double* __restrict__ h1, const double* __restrict__ h2,
+                                                        double* __restrict__ Hc, float* __restrict__ inv,
+                                                        unsigned* __restrict__ cnt) {
+  pdl_wait_then_trigger();
+  __shared__ float hs[256];
+  __shared__ float red[TB / 32];
+  __shared__ bool last;
+  for (int i = threadIdx.x; i < nv; i += TB) hs[i] = (float)h[i];
+  __syncthreads();
+  float acc = 0.0f;
+  float4* z4 = reinterpret_cast<float4*>(z);
+  for (int64_t k = (int64_t)blockIdx.x * TB + threadIdx.x; k < n4; k += (int64_t)gridDim.x * TB) {
+    float4 zv = z4[k];
+    for (int i0 = 0; i0 < nv; i0 += 8) {
+      float4 v[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        v[q] = (i0 + q < nv) ? reinterpret_cast<const float4*>(V + (size_t)(i0 + q) * ld)[k]
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float hq = (i0 + q < nv) ? hs[i0 + q] : 0.0f;
+        zv.x -= v[q].x * hq;
+        zv.y -= v[q].y * hq;
+        zv.z -= v[q].z * hq;
+        zv.w -= v[q].w * hq;
+      }
+    }
+    z4[k] = zv;
+    acc = fmaf(zv.x, zv.x, acc);
+    acc = fmaf(zv.y, zv.y, acc);
+    acc = fmaf(zv.z, zv.z, acc);
+    acc = fmaf(zv.w, zv.w, acc);
+  }
+  const float a = warp_sum_f(acc);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < TB / 32; ++w) s += (double)red[w];
+    partial[(int64_t)blockIdx.x * KMAXV] = s;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int i = threadIdx.x; i < nv; i += TB) Hc[i] = h2 ? h1[i] + h2[i] : h1[i];
+  if (wid == 0) {
+    double s = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&partial[(int64_t)b * KMAXV]);
+    s = warp_sum(s);
+    if (lane == 0) {
+      const double t = sqrt(s);
+      Hc[nv] = t;
+      *inv = (float)(1.0 / t);
+      *cnt = 0u;
+    }
+  }
+}
+
 // h[0..nv) = V^T z with the float4 kernels (nv <= KMAXV per call)
 int mdot4_f32(dg_ctx* c, const float* V, int nv, const float* z, double* h, cudaStream_t st) {
   const int64_t n4 = c->nonods / 4;
@@ -1597,6 +1733,13 @@ int mdot4_f32(dg_ctx* c, const float* V, int nv, const float* z, double* h, cuda
     const int cnt = std::min(KMAXV, nv - off);
     int rc;
     Mixed& M = mixed_of(c);
+    if (c->gs_fused) {
+      if ((rc = launch_k2(c, mdot8r_f32_kernel<RED_TB>, dim3(M.nblk4, (cnt + 7) / 8), RED_TB, 0, st,
+                          (const float*)(V + (size_t)off * c->nonods), (int64_t)c->nonods, cnt, z, n4, M.part,
+                          h + off, M.gs_cnt)))
+        return rc;
+      continue;
+    }
     if ((rc = launch_k2(c, mdot8_f32_kernel<RED_TB>, dim3(M.nblk4, (cnt + 7) / 8), RED_TB, 0, st,
                         (const float*)(V + (size_t)off * c->nonods), (int64_t)c->nonods, cnt, z, n4, M.part)))
       return rc;
@@ -1620,18 +1763,26 @@ int cgs2_32(dg_ctx* c, int j, float* w, int m, cudaStream_t st) {
   float* inv = reinterpret_cast<float*>(c->d_scal + 1);
   int rc;
   if ((rc = mdot4_f32(c, M.V, nv, w, c->d_h1, st))) return rc;
-  if ((rc = launch_k(c, axpy8_f32_kernel<RED_TB>, M.nblk4, RED_TB, 0, st, (const float*)M.V, (int64_t)c->nonods, nv,
-                     (const double*)c->d_h1, w, n4, M.part, two ? 0 : 1)))
-    return rc;
   if (two) {
-    if ((rc = mdot4_f32(c, M.V, nv, w, c->d_h2, st))) return rc;
     if ((rc = launch_k(c, axpy8_f32_kernel<RED_TB>, M.nblk4, RED_TB, 0, st, (const float*)M.V, (int64_t)c->nonods,
-                       nv, (const double*)c->d_h2, w, n4, M.part, 1)))
+                       nv, (const double*)c->d_h1, w, n4, M.part, 0)))
+      return rc;
+    if ((rc = mdot4_f32(c, M.V, nv, w, c->d_h2, st))) return rc;
+  }
+  if (c->gs_fused) {
+    // the last update with |w|^2 and the Hessenberg column in one launch
+    if ((rc = launch_k(c, axpy8f_f32_kernel<RED_TB>, M.nblk4, RED_TB, 0, st, (const float*)M.V, (int64_t)c->nonods,
+                       nv, (const double*)(two ? c->d_h2 : c->d_h1), w, n4, M.part, (const double*)c->d_h1,
+                       two ? (const double*)c->d_h2 : (const double*)nullptr, Hc, inv, M.gs_cnt + 32)))
+      return rc;
+  } else {
+    if ((rc = launch_k(c, axpy8_f32_kernel<RED_TB>, M.nblk4, RED_TB, 0, st, (const float*)M.V, (int64_t)c->nonods,
+                       nv, (const double*)(two ? c->d_h2 : c->d_h1), w, n4, M.part, 1)))
+      return rc;
+    if ((rc = launch_k(c, cgs_finish_kernel, 1, 256, 0, st, (const double*)M.part, M.nblk4, (const double*)c->d_h1,
+                       two ? (const double*)c->d_h2 : (const double*)nullptr, nv, Hc, inv)))
       return rc;
   }
-  if ((rc = launch_k(c, cgs_finish_kernel, 1, 256, 0, st, (const double*)M.part, M.nblk4, (const double*)c->d_h1,
-                     two ? (const double*)c->d_h2 : (const double*)nullptr, nv, Hc, inv)))
-    return rc;
   if ((rc = launch_k(c, scale4_f32_kernel, nblk(n4, 256), 256, 0, st, (const float*)w, (const float*)inv,
                      M.V + (size_t)nv * c->nonods, n4)))
     return rc;

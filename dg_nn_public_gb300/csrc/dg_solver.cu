@@ -23,7 +23,7 @@ using namespace dg;
 namespace {
 
 constexpr int RED_TB = 256;
-constexpr int kBatchedVariants = 5;   // batched smoothing kernel variants (see dg_ctx::batched_kernel)
+constexpr int kBatchedVariants = 6;   // batched smoothing kernel variants (see dg_ctx::batched_kernel)
 std::atomic<long long> g_launches{0};   // kernels launched by this library
 inline void bump(long long k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
@@ -176,7 +176,7 @@ struct dg_ctx {
   int batched_warps = 4;   // warps per CTA of the per-element batched smoothing kernel (4 or 8)
   // batched BF16 smoothing kernel variant (bsmooth): 0 CUDA cores, 1 / 2
   // mma.sync per element (4 / 8 warps), 3 mma.sync persistent bulk-copy, 4
-  // tcgen05 persistent bulk-copy; chosen by timing at the first batched
+  // tcgen05 persistent bulk-copy, 5 tcgen05 on split x; chosen by timing at the first batched
   // solve of each mixed build unless pinned (DG_BATCHED_KERNEL or the older
   // DG_BATCHED_MMA / _TMA / _WARPS switches)
   int batched_kernel = 1;
@@ -192,6 +192,9 @@ struct dg_ctx {
   // FP64 partial sums; 2 = CGS2).  One pass: the FP64 refinement bounds the
   // result, and c2 / c3 need the same inner iterations either way.
   int mixed_cgs_passes = 1;
+  // Gram-Schmidt of the inner Arnoldi with the reductions fused into the
+  // last CTA of the dot and update kernels (3 launches per step instead of 5)
+  bool gs_fused = true;
   // orthogonalisation of the FP64 GMRES Arnoldi step: 0 = CGS2 (two classical
   // passes, 2 reductions per step), 1 = modified Gram-Schmidt in the
   // reference's order (z06/volume_mf_diff.py:1814-1819; j + 1 dependent
@@ -880,6 +883,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     }
     const char* at = std::getenv("DG_AUTOTUNE");
     if (at && at[0]) c->autotune = at[0] != '0';
+    const char* gf = std::getenv("DG_GS_FUSED");
+    if (gf && gf[0]) c->gs_fused = gf[0] != '0';
     const char* mc = std::getenv("DG_MIXED_CGS");
     if (mc && mc[0]) c->mixed_cgs_passes = std::atoi(mc) == 1 ? 1 : 2;
   }

@@ -205,7 +205,11 @@ int dg_smooth_pc_batched(dg_ctx* ctx, const float* x, const float* b, float* x_o
  * (the default, once per operator build), 0 = CUDA cores, 1 / 2 = mma.sync
  * tensor-core tiles, one element per CTA (4 / 8 warps), 3 = mma.sync in a
  * persistent bulk-copy pipeline, 4 = tcgen05.mma with tensor-memory
- * accumulators in a persistent bulk-copy pipeline.  dg_batched_tuning
+ * accumulators in a persistent bulk-copy pipeline, 5 = the same on an
+ * iterate kept in the tensor-core operand layout (BF16 high + low parts,
+ * bulk-copied straight into the MMA operand; the batched preconditioner
+ * keeps its iterates in that layout and writes its output in FP32).
+ * dg_batched_tuning
  * reports the last timing per variant (microseconds per launch, -1 = not
  * timed; tune_us may be NULL) and the variant in use. */
 int dg_set_batched_kernel(dg_ctx* ctx, int32_t variant);
