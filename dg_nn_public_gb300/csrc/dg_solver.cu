@@ -193,8 +193,10 @@ struct dg_ctx {
   // result, and c2 / c3 need the same inner iterations either way.
   int mixed_cgs_passes = 1;
   // Gram-Schmidt of the inner Arnoldi with the reductions fused into the
-  // last CTA of the dot and update kernels (3 launches per step instead of 5)
-  bool gs_fused = true;
+  // last CTA of the dot and update kernels (3 launches per step instead of
+  // 5); measured slower on c2 (25.9 -> 26.9 ms per solve: the last CTA's
+  // reduction of ~940 partials is a serial tail), so off by default
+  bool gs_fused = false;
   // orthogonalisation of the FP64 GMRES Arnoldi step: 0 = CGS2 (two classical
   // passes, 2 reductions per step), 1 = modified Gram-Schmidt in the
   // reference's order (z06/volume_mf_diff.py:1814-1819; j + 1 dependent
