@@ -2115,8 +2115,21 @@ extern "C" int dg_solve_mixed(dg_ctx* c, double* x, const double* b, double tol,
       CK(c, cudaMemsetAsync(M.kdone, 0, sizeof(int), st));
       int k = 0;
       bool conv = false, ok = true;
-      for (int j0 = 0; j0 < m; j0 += chunk) {
-        const int cnt = std::min(chunk, m - j0);
+      // least-squares residual after the previous chunk (k_last steps); with
+      // adaptive chunks a chunk that the observed rate says ends past the
+      // target is cut to the predicted step count, so a refinement step
+      // stops within a step of its target instead of up to chunk - 1 past it
+      double est_last = beta;
+      int k_last = 0;
+      for (int j0 = 0; j0 < m;) {
+        int cnt = std::min(chunk, m - j0);
+        if (c->adaptive_chunk && k_last > 0 && est_last > target * beta0) {
+          const double rate = std::pow(est_last / beta, 1.0 / k_last);
+          if (rate > 0.0 && rate < 1.0) {
+            const double need = std::ceil(std::log(target * beta0 / est_last) / std::log(rate));
+            if (need >= 1.0 && need < (double)cnt) cnt = (int)need;
+          }
+        }
         int mode = 0, kd = 0;
         if ((rc = run_arnoldi32(c, j0, cnt, m, chunk, st, &mode))) return rc;
         CK(c, cudaMemcpyAsync(Hh.data(), M.H, sizeof(double) * Hh.size(), cudaMemcpyDeviceToHost, st));
@@ -2136,6 +2149,9 @@ extern "C" int dg_solve_mixed(dg_ctx* c, double* x, const double* b, double tol,
           break;
         }
         if (its >= max_its) break;
+        est_last = est;
+        k_last = k;
+        j0 += cnt;
       }
       if (!ok) {
         status = DG_ERR_NUMERIC;

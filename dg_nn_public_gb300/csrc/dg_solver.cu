@@ -164,7 +164,16 @@ struct dg_ctx {
   // chunk - 1 steps past its target (c2 with the Chebyshev smoothing:
   // chunk 10 / 5 / 4 / 3 -> 90 / 85 / 80 / 81 steps, 27.4 / 25.9 / 24.6 /
   // 25.0 ms; c3: chunk 10 / 5 -> 212 / 202 ms)
-  int mixed_chunk = 4;
+  // (with the adaptive cut below, c2: chunk 4 / 5 / 6 / 8 -> 24.73 / 24.61 /
+  // 24.51 / 24.78 ms at 80 / 80 / 80 / 81 steps)
+  int mixed_chunk = 6;
+  // cut a chunk that would run past the inner target to the step count the
+  // observed convergence rate predicts (its remaining steps run as direct
+  // launches); DG_ADAPTIVE_CHUNK=0 keeps whole chunks.  c2: 84 -> 80 steps
+  // (25.86 -> 24.73 ms) with the quadrature build, c3: 94 -> 90 (201 ->
+  // 192 ms); whole chunks stop up to chunk - 1 steps past the target, so
+  // the step count jumped with rounding-level changes of the operator
+  bool adaptive_chunk = true;
   // link the kernels of an inner Arnoldi step by programmatic dependent launch
   bool use_pdl = true;
   // batched solve: BF16 preconditioner steps on the tensor cores (mma.sync)
@@ -885,6 +894,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     }
     const char* at = std::getenv("DG_AUTOTUNE");
     if (at && at[0]) c->autotune = at[0] != '0';
+    const char* ac = std::getenv("DG_ADAPTIVE_CHUNK");
+    if (ac && ac[0]) c->adaptive_chunk = ac[0] != '0';
     const char* gf = std::getenv("DG_GS_FUSED");
     if (gf && gf[0]) c->gs_fused = gf[0] != '0';
     const char* mc = std::getenv("DG_MIXED_CGS");
