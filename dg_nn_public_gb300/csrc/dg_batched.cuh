@@ -853,6 +853,153 @@ __global__ void __launch_bounds__(256) bmdot_kernel(const float* __restrict__ V,
   }
 }
 
+// Low-register forms of the per-RHS Gram-Schmidt kernels (the float4 forms
+// above hold 16 or 32 float4 loads per thread: 112 / 255 registers, a
+// quarter / an eighth of the SM's warps).  A thread handles 4 RHS of one row
+// per iteration and at most 8 basis vectors at a time (~64 registers), 256
+// threads per block and 4 blocks per SM, so a block row streams with half
+// the SM's warps, each with 8 16-byte loads in flight.
+__global__ void __launch_bounds__(256, 4) bmdot2_kernel(const float* __restrict__ V, int64_t ld, int nv,
+                                                       const float* __restrict__ z, int64_t n,
+                                                       double* __restrict__ partial) {
+  __shared__ float4 red[16][8][kNR / 4];
+  const int q4 = threadIdx.x % 16, lane = threadIdx.x / 16;
+  const int j0 = blockIdx.y * 8;
+  const int cnt = min(8, nv - j0);
+  float4 acc[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) acc[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t row = (int64_t)blockIdx.x * 16 + lane; row < n; row += (int64_t)gridDim.x * 16) {
+    const float4 zv = reinterpret_cast<const float4*>(z + row * kNR)[q4];
+    float4 v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      v[j] = j < cnt ? reinterpret_cast<const float4*>(V + (size_t)(j0 + j) * ld + row * kNR)[q4]
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      acc[j].x = fmaf(v[j].x, zv.x, acc[j].x);
+      acc[j].y = fmaf(v[j].y, zv.y, acc[j].y);
+      acc[j].z = fmaf(v[j].z, zv.z, acc[j].z);
+      acc[j].w = fmaf(v[j].w, zv.w, acc[j].w);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) red[lane][j][q4] = acc[j];
+  __syncthreads();
+  for (int o = threadIdx.x; o < cnt * kNR; o += 256) {
+    const int j = o / kNR, q = o % kNR;
+    double sum = 0.0;
+    for (int l = 0; l < 16; ++l) sum += (double)reinterpret_cast<const float*>(&red[l][j][0])[q];
+    partial[((int64_t)blockIdx.x * 32 + j0 + j) * kNR + q] = sum;
+  }
+}
+
+__global__ void __launch_bounds__(256, 4) baxpy2_kernel(const float* __restrict__ V, int64_t ld, int nv,
+                                                       const double* __restrict__ h, float* __restrict__ z,
+                                                       int64_t n, double* __restrict__ partial) {
+  __shared__ float4 hs[32][kNR / 4];
+  __shared__ float4 red[16][kNR / 4];
+  const int q4 = threadIdx.x % 16, lane = threadIdx.x / 16;
+  for (int o = threadIdx.x; o < 32 * kNR; o += 256)
+    reinterpret_cast<float*>(&hs[0][0])[o] = o < nv * kNR ? (float)h[o] : 0.0f;
+  __syncthreads();
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int64_t row = (int64_t)blockIdx.x * 16 + lane; row < n; row += (int64_t)gridDim.x * 16) {
+    float4* zp = reinterpret_cast<float4*>(z + row * kNR) + q4;
+    float4 zv = *zp;
+    for (int i0 = 0; i0 < nv; i0 += 8) {
+      float4 v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        v[j] = i0 + j < nv ? reinterpret_cast<const float4*>(V + (size_t)(i0 + j) * ld + row * kNR)[q4]
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float4 hv = hs[(i0 + j) & 31][q4];
+        zv.x -= v[j].x * hv.x;
+        zv.y -= v[j].y * hv.y;
+        zv.z -= v[j].z * hv.z;
+        zv.w -= v[j].w * hv.w;
+      }
+    }
+    *zp = zv;
+    acc.x = fmaf(zv.x, zv.x, acc.x);
+    acc.y = fmaf(zv.y, zv.y, acc.y);
+    acc.z = fmaf(zv.z, zv.z, acc.z);
+    acc.w = fmaf(zv.w, zv.w, acc.w);
+  }
+  red[lane][q4] = acc;
+  __syncthreads();
+  if (threadIdx.x < kNR) {
+    double sum = 0.0;
+    for (int l = 0; l < 16; ++l) sum += (double)reinterpret_cast<const float*>(&red[l][0])[threadIdx.x];
+    partial[(int64_t)blockIdx.x * kNR + threadIdx.x] = sum;
+  }
+}
+
+// h[j * kNR + q] = sum over blocks of partial[(blk * 32 + j) * kNR + q]:
+// block (j, RHS group of 16) of 1024 threads = 64 lanes x 16 RHS; lane l
+// sums blocks l, l + 64, ... with eight loads in flight, then the 64 lane
+// sums in a fixed tree
+__global__ void __launch_bounds__(1024) breduce2_kernel(const double* __restrict__ partial, int nblk,
+                                                         double* __restrict__ h) {
+  __shared__ double red[64][16];
+  const int j = blockIdx.x, qi = threadIdx.x % 16, lane = threadIdx.x / 16;
+  const int q = blockIdx.y * 16 + qi;
+  double sum = 0.0;
+  for (int b0 = lane; b0 < nblk; b0 += 64 * 8) {
+    double v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int bk = b0 + 64 * i;
+      v[i] = bk < nblk ? partial[((int64_t)bk * 32 + j) * kNR + q] : 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sum += v[i];
+  }
+  red[lane][qi] = sum;
+  __syncthreads();
+  for (int w = 32; w >= 1; w >>= 1) {
+    if (lane < w) red[lane][qi] += red[lane + w][qi];
+    __syncthreads();
+  }
+  if (lane == 0) h[j * kNR + q] = red[0][qi];
+}
+
+// bfinish_kernel with the norm partials summed by 1024 threads (16 lanes x
+// 64 RHS, eight loads in flight per lane, fixed tree)
+__global__ void __launch_bounds__(1024) bfinish2_kernel(const double* __restrict__ partial, int nblk,
+                                                         const double* __restrict__ h, int nv, int j, int m,
+                                                         double* __restrict__ H, float* __restrict__ inv) {
+  __shared__ double red[16][kNR];
+  const int q = threadIdx.x % kNR, lane = threadIdx.x / kNR;
+  double sum = 0.0;
+  for (int b0 = lane; b0 < nblk; b0 += 16 * 8) {
+    double v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int bk = b0 + 16 * i;
+      v[i] = bk < nblk ? partial[(int64_t)bk * kNR + q] : 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sum += v[i];
+  }
+  red[lane][q] = sum;
+  __syncthreads();
+  for (int w = 8; w >= 1; w >>= 1) {
+    if (lane < w) red[lane][q] += red[lane + w][q];
+    __syncthreads();
+  }
+  if (lane == 0) {
+    double* Hq = H + (size_t)q * (m + 1) * m + (size_t)j * (m + 1);
+    for (int i = 0; i < nv; ++i) Hq[i] = h[i * kNR + q];
+    const double t = sqrt(red[0][q]);
+    Hq[nv] = t;
+    inv[q] = t > 0.0 ? (float)(1.0 / t) : 0.0f;
+  }
+}
+
 // h[j * kNR + q] = sum over blocks of partial[(blk * 32 + j) * kNR + q]
 __global__ void breduce_kernel(const double* __restrict__ partial, int nblk, int nv, double* __restrict__ h) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1078,7 +1225,8 @@ int ensure_batch(dg_ctx* c, int m) {
       if ((rc = dalloc(c, t, nv))) return rc;
     if ((rc = dalloc(c, &S.r1, (size_t)c->B * 4 * kNR))) return rc;
     S.nblk = 2 * c->nsm;
-    if ((rc = dalloc(c, &S.part, (size_t)S.nblk * 32 * kNR))) return rc;
+    // partial sums for up to 4 * nsm blocks (the low-register Gram-Schmidt)
+    if ((rc = dalloc(c, &S.part, (size_t)4 * c->nsm * 32 * kNR))) return rc;
     if ((rc = dalloc(c, &S.h, (size_t)32 * kNR))) return rc;
     if ((rc = dalloc(c, &S.nrm, (size_t)kNR))) return rc;
     if ((rc = dalloc(c, &S.scl, (size_t)kNR))) return rc;
@@ -1340,10 +1488,19 @@ int bcgs(dg_ctx* c, int j, float* w, int m, cudaStream_t st) {
   BatchState& S = batch_of(M);
   const int nv = j + 1;
   const int64_t ld = c->nonods * kNR;
-  bmdot_kernel<<<dim3(S.nblk, (nv + 7) / 8), 256, 0, st>>>(S.V, ld, nv, w, c->nonods, S.part);
-  breduce_kernel<<<nblk((int64_t)nv * kNR, 256), 256, 0, st>>>(S.part, S.nblk, nv, S.h);
-  baxpy_kernel<<<S.nblk, 256, 0, st>>>(S.V, ld, nv, S.h, w, c->nonods, S.part);
-  bfinish_kernel<<<1, kNR, 0, st>>>(S.part, S.nblk, S.h, nv, j, m, S.H, S.inv);
+  if (c->batched_gs2) {
+    // low-register forms, 4 blocks per SM
+    const int g = 4 * c->nsm;
+    bmdot2_kernel<<<dim3(g, (nv + 7) / 8), 256, 0, st>>>(S.V, ld, nv, w, c->nonods, S.part);
+    breduce2_kernel<<<dim3(nv, kNR / 16), 1024, 0, st>>>(S.part, g, S.h);
+    baxpy2_kernel<<<g, 256, 0, st>>>(S.V, ld, nv, S.h, w, c->nonods, S.part);
+    bfinish2_kernel<<<1, 1024, 0, st>>>(S.part, g, S.h, nv, j, m, S.H, S.inv);
+  } else {
+    bmdot_kernel<<<dim3(S.nblk, (nv + 7) / 8), 256, 0, st>>>(S.V, ld, nv, w, c->nonods, S.part);
+    breduce_kernel<<<nblk((int64_t)nv * kNR, 256), 256, 0, st>>>(S.part, S.nblk, nv, S.h);
+    baxpy_kernel<<<S.nblk, 256, 0, st>>>(S.V, ld, nv, S.h, w, c->nonods, S.part);
+    bfinish_kernel<<<1, kNR, 0, st>>>(S.part, S.nblk, S.h, nv, j, m, S.H, S.inv);
+  }
   bscale_kernel<<<nblk(ld / 4, 256), 256, 0, st>>>(w, S.inv, S.V + (size_t)nv * ld, ld);
   bump(5);
   CKL(c);
@@ -1444,7 +1601,10 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
       first_cycle = false;
       if (!any) break;
       int k = 0;
-      std::vector<char> conv(kNR, 0);
+      // host checks of the least-squares residuals: every 5 steps, and
+      // (adaptive) at the step where the slowest active RHS is predicted to
+      // reach its target from its observed convergence rate
+      int next_check = std::min(5, m);
       for (int j = 0; j < m && total < max_its; ++j) {
         float* zj = S.Z + (size_t)j * ld;
         if ((rc = bprecond(c, S.V + (size_t)j * ld, zj, st))) return rc;
@@ -1454,19 +1614,28 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
         k = j + 1;
         for (int q = 0; q < kNR; ++q)
           if (active[q]) ++its[q];
-        if (k % 5 == 0 || k == m) {
+        if (k >= next_check || k == m) {
           CK(c, cudaMemcpyAsync(Hh.data(), S.H, sizeof(double) * Hh.size(), cudaMemcpyDeviceToHost, st));
           CK(c, cudaStreamSynchronize(st));
           bool all = true;
+          int need_max = 0;
           for (int q = 0; q < kNR; ++q) {
             if (!active[q] || nrm[q] <= target[q] * beta0[q]) continue;
             std::vector<double> Hq(Hh.begin() + (size_t)q * (m + 1) * m, Hh.begin() + (size_t)(q + 1) * (m + 1) * m);
             std::vector<double> yq;
             bool ok = true;
             const double est = hessenberg_ls(Hq, m, k, nrm[q], yq, ok);
-            if (!ok || !(est <= target[q] * beta0[q])) all = false;
+            if (!ok || !(est <= target[q] * beta0[q])) {
+              all = false;
+              int need = 5;
+              const double rate = std::pow(est / nrm[q], 1.0 / k);
+              if (ok && rate > 0.0 && rate < 1.0)
+                need = (int)std::ceil(std::log(target[q] * beta0[q] / est) / std::log(rate));
+              need_max = std::max(need_max, std::max(need, 1));
+            }
           }
           if (all) break;
+          next_check = c->adaptive_chunk ? k + std::min(need_max, 5) : k + 5;
         }
       }
       // per-RHS least squares over the k steps, d += Z y

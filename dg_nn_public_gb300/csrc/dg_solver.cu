@@ -189,6 +189,9 @@ struct dg_ctx {
   // solve of each mixed build unless pinned (DG_BATCHED_KERNEL or the older
   // DG_BATCHED_MMA / _TMA / _WARPS switches)
   int batched_kernel = 1;
+  // batched Gram-Schmidt with one thread per (row lane, RHS) (bmdot2 /
+  // baxpy2); DG_BATCHED_GS2=0 keeps the float4 forms
+  bool batched_gs2 = true;
   bool batched_pinned = false;
   int tma_variant = 0;   // elements per group / stages / CTAs per SM of that kernel
   bool autotune = true;  // pick tma_variant by timing at the first mixed solve after a build
@@ -894,6 +897,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     }
     const char* at = std::getenv("DG_AUTOTUNE");
     if (at && at[0]) c->autotune = at[0] != '0';
+    const char* bg = std::getenv("DG_BATCHED_GS2");
+    if (bg && bg[0]) c->batched_gs2 = bg[0] != '0';
     const char* ac = std::getenv("DG_ADAPTIVE_CHUNK");
     if (ac && ac[0]) c->adaptive_chunk = ac[0] != '0';
     const char* gf = std::getenv("DG_GS_FUSED");
