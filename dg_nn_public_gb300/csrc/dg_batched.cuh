@@ -1182,7 +1182,7 @@ struct BatchState {
   int tc_version = -1;
   // smoothing-kernel autotuner: per-variant microseconds of one launch
   // (-1 = not timed), the mixed build it was taken for
-  float tune_us[kBatchedVariants] = {-1.f, -1.f, -1.f, -1.f, -1.f, -1.f};
+  float tune_us[kBatchedVariants] = {-1.f, -1.f, -1.f, -1.f, -1.f, -1.f, -1.f};
   int tune_version = -1;
   // the preconditioner's iterates in the split tensor-core layout (variant 5)
   unsigned char *xs1 = nullptr, *xs2 = nullptr;
@@ -1266,6 +1266,15 @@ int btcs(dg_ctx* c, BatchState& S, const unsigned char* xs, const float* b, void
          const float* ws, cudaStream_t st) {
   if (!S.tc || ((flags & RF_SMOOTH) && !xo) || ((flags & RF_RESTRICT) && !rr1) || !b)
     return fail(c, DG_ERR_STATE, "batched split-x step: operand buffers not set up");
+  if (c->batched_kernel == 6) {   // warp-specialized, one CTA per SM
+    const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm);
+    if (g)
+      bres_tcw_kernel<<<g, kTwT, kTwDyn, st>>>(S.tc, c->d_nbe, xs, b, xo, c->B, flags | (xs ? 0 : RF_ZEROX), c->T.P,
+                                               rr1, c->d_err, ws);
+    bump();
+    CKL(c);
+    return DG_OK;
+  }
   const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kTsCTA);
   if (g)
     bres_tcs_kernel<<<g, kTcT, kTsDyn, st>>>(S.tc, c->d_nbe, xs, b, nullptr, xo, c->B, flags | (xs ? 0 : RF_ZEROX),
@@ -1280,7 +1289,7 @@ int btcs(dg_ctx* c, BatchState& S, const unsigned char* xs, const float* b, void
 // mma.sync with 4 / 8 warps per element, 3 mma.sync persistent bulk-copy,
 // 4 tcgen05 persistent bulk-copy (accumulators in tensor memory), 5 tcgen05
 // on split x (the iterate already in the operand layout; FP32 x is split
-// first here, bprecond keeps its iterates split)
+// first here, bprecond keeps its iterates split), 6 the same warp-specialized
 int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, const float* b, float* xo, int flags,
             float* rr1, const float* ws, cudaStream_t st) {
   switch (variant) {
@@ -1352,8 +1361,14 @@ int autotune_batched(dg_ctx* c, Mixed& M, BatchState& S, cudaStream_t st) {
   int rc0;
   if ((rc0 = ensure_tc_layout(c, M, S, st)) || (rc0 = ensure_split(c, S))) return rc0;
   CK(c, cudaMemsetAsync(S.xs1, 0, (size_t)c->B * kSplit, st));
+  const int keep = c->batched_kernel;
   auto one = [&](int v) -> int {
-    if (v == 5) return btcs(c, S, S.xs1, S.t2, S.xs2, RF_SMOOTH | RF_OUT_SPLIT, nullptr, nullptr, st);
+    if (v >= 5) {   // split-iterate forms: btcs follows c->batched_kernel
+      c->batched_kernel = v;
+      const int rc2 = btcs(c, S, S.xs1, S.t2, S.xs2, RF_SMOOTH | RF_OUT_SPLIT, nullptr, nullptr, st);
+      c->batched_kernel = keep;
+      return rc2;
+    }
     return bsmooth(c, M, S, v, S.t1, S.t2, S.t6, RF_SMOOTH, nullptr, nullptr, st);
   };
   for (int v = 0; v < kBatchedVariants; ++v) {
@@ -1402,7 +1417,7 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   };
   // split-x pipeline: the iterate stays in the tensor-core operand layout
   // from the first smoothing step to the last, which writes z in FP32
-  const bool split = bf && c->batched_kernel == 5;
+  const bool split = bf && c->batched_kernel >= 5;
   unsigned char* scur = nullptr;
   unsigned char* soth = nullptr;
   if (split) {
@@ -1537,6 +1552,7 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
   CK(c, cudaFuncSetAttribute(bres_mma_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBDyn));
   CK(c, cudaFuncSetAttribute(bres_tc05_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcDyn));
   CK(c, cudaFuncSetAttribute(bres_tcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTsDyn));
+  CK(c, cudaFuncSetAttribute(bres_tcw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTwDyn));
   if ((rc = autotune_batched(c, M, batch_of(M), st))) return rc;
   CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));   // bulk-copy wait time-outs land here
   BatchState& S = batch_of(M);
@@ -1717,6 +1733,7 @@ int batched_prep(dg_ctx* c, const char* name, cudaStream_t st) {
   CK(c, cudaFuncSetAttribute(bres_mma_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBDyn));
   CK(c, cudaFuncSetAttribute(bres_tc05_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcDyn));
   CK(c, cudaFuncSetAttribute(bres_tcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTsDyn));
+  CK(c, cudaFuncSetAttribute(bres_tcw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTwDyn));
   return DG_OK;
 }
 
@@ -1756,7 +1773,7 @@ extern "C" int dg_smooth_pc_batched(dg_ctx* c, const float* x, const float* b, f
 extern "C" int dg_set_batched_kernel(dg_ctx* c, int32_t variant) {
   if (!c) return set_thread_error(DG_ERR_ARG, "dg_set_batched_kernel: null context");
   if (variant < -1 || variant >= kBatchedVariants)
-    return fail(c, DG_ERR_ARG, "dg_set_batched_kernel: variant must be -1 .. 5");
+    return fail(c, DG_ERR_ARG, "dg_set_batched_kernel: variant must be -1 .. 6");
   if (variant < 0) {
     c->batched_pinned = false;
     batch_of(mixed_of(c)).tune_version = -1;

@@ -709,4 +709,320 @@ __global__ void __launch_bounds__(kTcT, kTsCTA) bres_tcs_kernel(
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols));
 }
 
+
+// ---------------------------------------------------------------------------
+// Warp-specialized form of bres_tcs_kernel (same arithmetic, one CTA per SM):
+//   warp 0      bulk copies of the next elements into a ring of kTwStages
+//               stages (waits for a stage to be released);
+//   warp 1      one thread issues the MMAs, software-pipelined: the block
+//               product D1 of element k, then the smoothing product D2 of
+//               element k - 1 (whose residual operand Rop the epilogue has
+//               written meanwhile);
+//   warps 2..9  the epilogue on TMEM lane quadrant (warp % 4) and half of the
+//               block rows (warps 2..5 rows 0..9, warps 6..9 rows 10..19),
+//               also pipelined: the residual half of element k (D1 -> res ->
+//               Rop), then the update half of element k - 1 (D2 -> x_out).
+// Three accumulator sets (t = k % 3) and three Rop buffers let the MMAs of
+// one element run while the epilogue works on the two before it.  The roles
+// meet only at mbarriers; every wait is bounded (on a time-out the kernel
+// records error 3 and every role leaves its loop).
+constexpr int kTwT = 320;
+constexpr int kTwStages = 4;
+constexpr int kTwNT = 3;                          // accumulator sets / Rop buffers
+constexpr int kTwDyn = kTwStages * kTsStage + kTwNT * kTcRop + 2 * kSplit;
+constexpr uint32_t kTwCols = 256;                 // set t: D1 at 64 t, D2 at 64 t + 32
+
+__device__ __forceinline__ void mbar_arrive1(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
+
+__global__ void __launch_bounds__(kTwT, 1) bres_tcw_kernel(
+    const __nv_bfloat16* __restrict__ tcblk, const int* __restrict__ nbe, const unsigned char* __restrict__ xs,
+    const float* __restrict__ b, void* __restrict__ x_out, int64_t B, int flags, const double* __restrict__ P,
+    float* __restrict__ r1, int* __restrict__ err, const float* __restrict__ wsp) {
+  constexpr int N = 20, F = 4, S = kTwStages, NT = kTwNT;
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  unsigned char* stages = tsm;
+  unsigned char* Rop = tsm + S * kTsStage;           // NT buffers
+  unsigned char* Out = Rop + NT * kTcRop;            // two buffers
+  __shared__ __align__(8) uint64_t full[S], empty[S], d1full[NT], ropfull[NT], d2full[NT], tfree[NT];
+  __shared__ uint32_t tmem_slot;
+  __shared__ float Ps[N][F];
+  __shared__ float red1[2][F][kNR];
+  __shared__ volatile int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool zerox = flags & RF_ZEROX;
+  const bool smooth = flags & RF_SMOOTH;
+  const bool restrict_ = flags & RF_RESTRICT;
+  const bool out_split = flags & RF_OUT_SPLIT;
+  const int64_t stride = gridDim.x;
+  const int64_t nmine = blockIdx.x < B ? (B - 1 - blockIdx.x) / stride + 1 : 0;
+  for (int i = tid; i < kTwDyn / 16; i += kTwT) reinterpret_cast<uint4*>(tsm)[i] = make_uint4(0u, 0u, 0u, 0u);
+  for (int i = tid; i < N * F; i += kTwT) Ps[i / F][i % F] = (float)P[i];
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int i = 0; i < S; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < NT; ++i) {
+      mbar_init(&d1full[i], 1);
+      mbar_init(&ropfull[i], 1);
+      mbar_init(&d2full[i], 1);
+      mbar_init(&tfree[i], 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  fence_async_smem();
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                 "r"(kTwCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  auto wait = [&](uint64_t* bar, uint32_t parity) -> bool {
+    for (uint32_t it = 0; it < kTmaSpinLimit; ++it) {
+      if (mbar_try_wait(bar, parity)) return true;
+      if (abort_flag) return false;
+    }
+    abort_flag = 1;
+    atomicExch(err, 3);
+    return false;
+  };
+  // the u-th use of a ring slot completes phase u: parity u & 1
+  auto par = [](int64_t use) -> uint32_t { return (uint32_t)(use & 1); };
+  int64_t issued = 0;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- producer ----
+      for (int64_t k = 0; k < nmine && !abort_flag; ++k) {
+        const int s = (int)(k % S);
+        if (k >= S && !wait(&empty[s], par(k / S - 1))) break;
+        const int64_t e = blockIdx.x + k * stride;
+        unsigned char* st = stages + (size_t)s * kTsStage;
+        const unsigned char* src = reinterpret_cast<const unsigned char*>(tcblk) + (size_t)e * kTcElem;
+        int nb[F] = {-1, -1, -1, -1};
+        uint32_t bytes = 0;
+        if (smooth) bytes += kTcWBytes;
+        if (!zerox) {
+          const int4 n4 = reinterpret_cast<const int4*>(nbe)[e];
+          nb[0] = n4.x;
+          nb[1] = n4.y;
+          nb[2] = n4.z;
+          nb[3] = n4.w;
+          bytes += kTcABytes + kSplit;
+          for (int f = 0; f < F; ++f)
+            if (nb[f] >= 0) bytes += kSplit;
+        }
+        if (b) bytes += 20 * kNR * 4;
+        mbar_expect_tx(&full[s], bytes);
+        if (smooth && !zerox)
+          bulk_copy_g2s(st + kTsW, src, kTcElem, &full[s]);
+        else if (smooth)
+          bulk_copy_g2s(st + kTsW, src, kTcWBytes, &full[s]);
+        else if (!zerox)
+          bulk_copy_g2s(st + kTsA, src + kTcWBytes, kTcABytes, &full[s]);
+        if (!zerox) {
+          bulk_copy_g2s(st + kTsX, xs + e * kSplit, kSplit, &full[s]);
+          for (int f = 0; f < F; ++f)   // a boundary face keeps a stale slab: its block is zero
+            if (nb[f] >= 0)
+              bulk_copy_g2s(st + kTsX + (1 + f) * kSplit, xs + (int64_t)nb[f] * kSplit, kSplit, &full[s]);
+        }
+        if (b) bulk_copy_g2s(st + kTsB, b + e * (int64_t)N * kNR, 20 * kNR * 4, &full[s]);
+        issued = k + 1;
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer: D1(k), then D2(k - 1) ----
+      auto mma2 = [&](int64_t j) -> bool {
+        const int tj = (int)(j % NT);
+        if (!wait(&ropfull[tj], par(j / NT))) return false;
+        tc_fence_after();
+        const uint32_t a0 = smem_addr(Rop + tj * kTcRop), b0 = smem_addr(stages + (size_t)(j % S) * kTsStage + kTsW);
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks)
+          tc_mma(tmem + 64u * tj + 32u, tc_sdesc(a0 + ks * 2 * kTcLBO, kTcLBO, 128),
+                 tc_sdesc(b0 + ks * 2 * kTcChunk, kTcChunk, 128), kTcIdescR, ks > 0 ? 1u : 0u);
+        tc_commit(&d2full[tj]);
+        return true;
+      };
+      bool ok = true;
+      for (int64_t k = 0; k < nmine && ok && !abort_flag; ++k) {
+        const int s = (int)(k % S), t = (int)(k % NT);
+        if (!wait(&full[s], par(k / S))) break;
+        if (k >= NT && !wait(&tfree[t], par(k / NT - 1))) break;
+        tc_fence_after();
+        if (!zerox) {
+          unsigned char* st = stages + (size_t)s * kTsStage;
+          const uint32_t a0 = smem_addr(st + kTsX), b0 = smem_addr(st + kTsA);
+#pragma unroll
+          for (int ks = 0; ks < 8; ++ks)
+            tc_mma(tmem + 64u * t, tc_sdesc(a0 + ks * 2 * kTcLBO, kTcLBO, 128),
+                   tc_sdesc(b0 + ks * 2 * kTcChunk, kTcChunk, 128), kTcIdescA, ks > 0 ? 1u : 0u);
+        }
+        tc_commit(&d1full[t]);
+        if (smooth && k >= 1) ok = mma2(k - 1);
+      }
+      if (ok && smooth && nmine > 0 && !abort_flag) (void)mma2(nmine - 1);
+    }
+  } else {
+    // ---- epilogue: 8 warps, residual half of k then update half of k - 1 ----
+    const int lq = warp & 3;                          // TMEM lane quadrant of this warp
+    const int half = (warp - 2) >> 2;                 // block rows 0..9 or 10..19
+    const int r = 32 * lq + lane, q = r >> 1, part = r & 1;
+    const int n0 = 10 * half;
+    const bool elected = warp == 2 && lane == 0;
+    const float ws = wsp ? *wsp : 1.0f;
+    const uint32_t lane_off = (uint32_t)(32 * lq) << 16;
+    // 10 rows n0 .. n0+9 of accumulator column base col0 (columns 8 half ..)
+    auto ld10 = [&](uint32_t col0, float (&v)[10]) {
+      float a[8], c8[8];
+      tc_ld8(tmem + lane_off + col0 + 8 * half, a);
+      tc_ld8(tmem + lane_off + col0 + 8 * half + 8, c8);
+      tc_wait_ld();
+#pragma unroll
+      for (int i = 0; i < 10; ++i) {   // row n0 + i sits at column offset i + 2 half
+        const float lo = i < 8 ? a[i] : c8[i - 8];
+        const float hi = i + 2 < 8 ? a[i + 2] : c8[i - 6];
+        v[i] = half ? hi : lo;
+      }
+#pragma unroll
+      for (int i = 0; i < 10; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], 1);
+    };
+    // residual half of element k: D1 -> res -> (r1) -> Rop[t]
+    auto first = [&](int64_t k) -> bool {
+      const int s = (int)(k % S), t = (int)(k % NT);
+      const int64_t e = blockIdx.x + k * stride;
+      unsigned char* st = stages + (size_t)s * kTsStage;
+      wait(&full[s], par(k / S));
+      wait(&d1full[t], par(k / NT));
+      epi_sync();   // every epilogue thread sees the same abort_flag
+      if (abort_flag) return false;
+      tc_fence_after();
+      float v[10];
+      if (zerox) {
+#pragma unroll
+        for (int i = 0; i < 10; ++i) v[i] = 0.0f;
+      } else {
+        ld10(64u * t, v);
+      }
+      const float* bst = reinterpret_cast<const float*>(st + kTsB);
+      float res[10];
+#pragma unroll
+      for (int i = 0; i < 10; ++i) res[i] = (b ? bst[(n0 + i) * kNR + q] : 0.0f) - v[i];
+      if (restrict_) {
+        if (part == 0) {
+#pragma unroll
+          for (int c = 0; c < F; ++c) {
+            float p = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 10; ++i) p = fmaf(Ps[n0 + i][c], res[i], p);
+            red1[half][c][q] = p;
+          }
+        }
+        epi_sync();
+        if (half == 0 && part == 0)
+#pragma unroll
+          for (int c = 0; c < F; ++c) r1[(e * F + c) * kNR + q] = red1[0][c][q] + red1[1][c][q];
+      }
+      if (smooth) {
+        // rows of the K-major residual operand: high (part 0) or low
+        // (part 1) BF16 part of res[q][n] in K slot n
+        uint32_t w[5];
+#pragma unroll
+        for (int h = 0; h < 5; ++h) {
+          float a0 = res[2 * h], a1 = res[2 * h + 1];
+          if (part) {
+            a0 -= __bfloat162float(__float2bfloat16_rn(a0));
+            a1 -= __bfloat162float(__float2bfloat16_rn(a1));
+          }
+          w[h] = pack_bf16x2(a0, a1);
+        }
+        unsigned char* row = Rop + t * kTcRop + (r >> 3) * 128 + (r & 7) * 16;
+        if (half == 0) {   // slots 0..9: group 0 (0..7), group 1 (8, 9)
+          *reinterpret_cast<uint4*>(row) = make_uint4(w[0], w[1], w[2], w[3]);
+          *reinterpret_cast<uint32_t*>(row + kTcLBO) = w[4];
+        } else {           // slots 10..19: group 1 (10..15), group 2 (16..19)
+          *reinterpret_cast<uint32_t*>(row + kTcLBO + 4) = w[0];
+          *reinterpret_cast<uint2*>(row + kTcLBO + 8) = make_uint2(w[1], w[2]);
+          *reinterpret_cast<uint2*>(row + 2 * kTcLBO) = make_uint2(w[3], w[4]);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        epi_sync();
+        if (elected) mbar_arrive1(&ropfull[t]);
+      } else {
+        tc_fence_before();
+        epi_sync();   // res read from D1 and the stage: release both
+        if (elected) {
+          mbar_arrive1(&tfree[t]);
+          mbar_arrive1(&empty[s]);
+        }
+      }
+      return true;
+    };
+    // update half of element j: D2 -> x_out; releases its stage and set
+    auto second = [&](int64_t j) -> bool {
+      const int s = (int)(j % S), t = (int)(j % NT);
+      const int64_t e = blockIdx.x + j * stride;
+      unsigned char* st = stages + (size_t)s * kTsStage;
+      unsigned char* ob = Out + (int)(j & 1) * kSplit;
+      if (elected && out_split) bulk_wait_read1();   // this buffer's store of element j - 2 has been read
+      wait(&d2full[t], par(j / NT));
+      epi_sync();
+      if (abort_flag) return false;
+      tc_fence_after();
+      float c[10];
+      ld10(64u * t + 32u, c);
+      const unsigned char* xo_own = st + kTsX;
+#pragma unroll
+      for (int i0 = 0; i0 < 10; i0 += 2) {   // the pair splits the rows: part 0 even, part 1 odd
+        const int n = n0 + i0 + part;
+        const float cv = part ? c[i0 + 1] : c[i0];
+        const float xv = zerox ? 0.0f : split_value(*reinterpret_cast<const uint32_t*>(xo_own + split_off(n, q)));
+        const float xo = xv + ws * cv;
+        if (out_split)
+          *reinterpret_cast<uint32_t*>(ob + split_off(n, q)) = split_pack(xo);
+        else
+          reinterpret_cast<float*>(x_out)[(e * N + n) * kNR + q] = xo;
+      }
+      if (out_split) fence_async_smem();
+      tc_fence_before();
+      epi_sync();
+      if (elected) {
+        if (out_split) bulk_store_s2g(reinterpret_cast<unsigned char*>(x_out) + e * kSplit, ob, kSplit);
+        mbar_arrive1(&tfree[t]);
+        mbar_arrive1(&empty[s]);
+      }
+      return true;
+    };
+    bool ok = true;
+    for (int64_t k = 0; k < nmine && ok; ++k) {
+      ok = first(k);
+      if (ok && smooth && k >= 1) ok = second(k - 1);
+    }
+    if (ok && smooth && nmine > 0) (void)second(nmine - 1);
+    if (elected) bulk_wait_all();
+  }
+  __syncthreads();
+  if (warp == 0 && lane == 0 && abort_flag) {
+    // copies issued and possibly still in flight: wait (bounded) for each
+    // stage's outstanding phase
+    for (int64_t k = issued > S ? issued - S : 0; k < issued; ++k)
+      (void)mbar_wait_bounded(&full[k % S], par(k / S));
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTwCols));
+}
+
 }  // namespace

@@ -23,7 +23,7 @@ using namespace dg;
 namespace {
 
 constexpr int RED_TB = 256;
-constexpr int kBatchedVariants = 6;   // batched smoothing kernel variants (see dg_ctx::batched_kernel)
+constexpr int kBatchedVariants = 7;   // batched smoothing kernel variants (see dg_ctx::batched_kernel)
 std::atomic<long long> g_launches{0};   // kernels launched by this library
 inline void bump(long long k = 1) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
@@ -185,7 +185,8 @@ struct dg_ctx {
   int batched_warps = 4;   // warps per CTA of the per-element batched smoothing kernel (4 or 8)
   // batched BF16 smoothing kernel variant (bsmooth): 0 CUDA cores, 1 / 2
   // mma.sync per element (4 / 8 warps), 3 mma.sync persistent bulk-copy, 4
-  // tcgen05 persistent bulk-copy, 5 tcgen05 on split x; chosen by timing at the first batched
+  // tcgen05 persistent bulk-copy, 5 tcgen05 on split x, 6 the same
+  // warp-specialized; chosen by timing at the first batched
   // solve of each mixed build unless pinned (DG_BATCHED_KERNEL or the older
   // DG_BATCHED_MMA / _TMA / _WARPS switches)
   int batched_kernel = 1;

@@ -311,7 +311,8 @@ class DGSolver:
         return its, res
 
     # -- multi-RHS stages (64 right-hand sides, RHS-interleaved FP32) ----
-    BATCHED_KERNELS = ("cuda_cores", "mma_sync4", "mma_sync8", "mma_sync_bulk", "tcgen05_bulk", "tcgen05_split")
+    BATCHED_KERNELS = ("cuda_cores", "mma_sync4", "mma_sync8", "mma_sync_bulk", "tcgen05_bulk", "tcgen05_split",
+                       "tcgen05_ws")
 
     def _check_batched(self, t):
         torch = _torch()

@@ -208,7 +208,9 @@ int dg_smooth_pc_batched(dg_ctx* ctx, const float* x, const float* b, float* x_o
  * accumulators in a persistent bulk-copy pipeline, 5 = the same on an
  * iterate kept in the tensor-core operand layout (BF16 high + low parts,
  * bulk-copied straight into the MMA operand; the batched preconditioner
- * keeps its iterates in that layout and writes its output in FP32).
+ * keeps its iterates in that layout and writes its output in FP32), 6 = the
+ * same in one warp-specialized CTA per SM (a copy warp, an MMA-issuing
+ * thread and eight epilogue warps on double-buffered accumulators).
  * dg_batched_tuning
  * reports the last timing per variant (microseconds per launch, -1 = not
  * timed; tune_us may be NULL) and the variant in use. */

@@ -82,7 +82,7 @@ def _modes(m, nrhs, seed):
     return F
 
 
-@pytest.mark.parametrize("kernel", ["tcgen05_bulk", "tcgen05_split"])
+@pytest.mark.parametrize("kernel", ["tcgen05_bulk", "tcgen05_split", "tcgen05_ws"])
 def test_batched_solve_with_tcgen05_kernel(kernel):
     """The kernel pinned before the first batched solve (the autotuner does
     not run): for the split form the preconditioner keeps its iterates in
