@@ -1186,6 +1186,16 @@ struct BatchState {
   int tune_version = -1;
   // the preconditioner's iterates in the split tensor-core layout (variant 5)
   unsigned char *xs1 = nullptr, *xs2 = nullptr;
+  // one CUDA graph per inner Arnoldi step index j (preconditioner, apply,
+  // Gram-Schmidt), the kernels each one launches, and the state it was
+  // captured for: any change of that state drops them all
+  std::vector<cudaGraphExec_t> step_graph;
+  std::vector<int> step_kern;
+  std::vector<const void*> step_key;
+  ~BatchState() {
+    for (auto& g : step_graph)
+      if (g) cudaGraphExecDestroy(g);
+  }
 };
 
 void destroy_batch(void* batch) { delete static_cast<BatchState*>(batch); }
@@ -1357,7 +1367,11 @@ int autotune_batched(dg_ctx* c, Mixed& M, BatchState& S, cudaStream_t st) {
   CK(c, cudaEventCreate(&e1));
   float best = 1e30f;
   int bestv = c->batched_kernel;
-  if (!c->precond_bf16) return DG_OK;
+  if (!c->precond_bf16) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return DG_OK;
+  }
   int rc0;
   if ((rc0 = ensure_tc_layout(c, M, S, st)) || (rc0 = ensure_split(c, S))) return rc0;
   CK(c, cudaMemsetAsync(S.xs1, 0, (size_t)c->B * kSplit, st));
@@ -1522,6 +1536,85 @@ int bcgs(dg_ctx* c, int j, float* w, int m, cudaStream_t st) {
   return DG_OK;
 }
 
+// Inner Arnoldi step j of the batched flexible GMRES: z_j = P(v_j),
+// w = -A z_j, Gram-Schmidt of w against v_0..v_j into H column j and v_j+1.
+int bstep(dg_ctx* c, int j, int m, cudaStream_t st) {
+  Mixed& M = mixed_of(c);
+  BatchState& S = batch_of(M);
+  const int64_t ld = c->nonods * kNR;
+  float* zj = S.Z + (size_t)j * ld;
+  int rc;
+  if ((rc = bprecond(c, S.V + (size_t)j * ld, zj, st))) return rc;
+  if ((rc = bres<float>(c, M.blk, M.W, zj, nullptr, S.t1, nullptr, RF_NEG, nullptr, st))) return rc;
+  return bcgs(c, j, S.t1, m, st);
+}
+
+// Runs step j as one CUDA graph launch.  The graph of each j is captured at
+// its first use and replayed in every later restart cycle and solve; its
+// kernel arguments are fixed device pointers (basis column j, scratch,
+// operator copies), so it is kept while the state in `key` below holds and
+// captured again after any change (restart length, reallocated basis,
+// kernel variant, operator rebuild, preconditioner options).  Buffers that
+// the step would allocate or lay out on first use are set up before the
+// capture, so the graph holds kernels only.
+int run_bstep(dg_ctx* c, int j, int m, cudaStream_t st) {
+  if (!c->use_graph) return bstep(c, j, m, st);
+  Mixed& M = mixed_of(c);
+  BatchState& S = batch_of(M);
+  auto tag = [](int64_t v) { return reinterpret_cast<const void*>(static_cast<intptr_t>(v)); };
+  const std::vector<const void*> key = {
+      tag(m),
+      tag(c->batched_kernel),
+      tag(c->mixed_version),
+      tag(c->precond_bf16),
+      tag(c->batched_gs2),
+      tag(c->cfg.pre_smooth_its),
+      tag(c->cfg.post_smooth_its),
+      tag(c->omegas_set),
+      tag(M.dense_l),
+      S.V,
+      S.Z,
+      M.blk,
+      M.blk16,
+      M.dense_inv,
+  };
+  if (key != S.step_key) {
+    for (auto& g : S.step_graph)
+      if (g) cudaGraphExecDestroy(g);
+    S.step_graph.assign(m, nullptr);
+    S.step_kern.assign(m, 0);
+    S.step_key = key;
+  }
+  if (!S.step_graph[j]) {
+    int rc;
+    if (c->precond_bf16 && c->batched_kernel >= 4 && (rc = ensure_tc_layout(c, M, S, st))) return rc;
+    if (c->precond_bf16 && c->batched_kernel >= 5 && (rc = ensure_split(c, S))) return rc;
+    if (!c->cap_stream) CK(c, cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
+    CK(c, cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const long long k0 = g_launches.load();
+    rc = bstep(c, j, m, c->cap_stream);
+    const int nk = (int)(g_launches.load() - k0);
+    g_launches.fetch_sub(nk);   // captured, not launched
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(c->cap_stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ee != cudaSuccess) return fail(c, DG_ERR_CUDA, std::string("batched step capture: ") + cudaGetErrorString(ee));
+    const cudaError_t ie = cudaGraphInstantiate(&S.step_graph[j], g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      S.step_graph[j] = nullptr;
+      return fail(c, DG_ERR_CUDA, std::string("batched step instantiate: ") + cudaGetErrorString(ie));
+    }
+    S.step_kern[j] = nk;
+  }
+  CK(c, cudaGraphLaunch(S.step_graph[j], st));
+  bump(S.step_kern[j]);
+  return DG_OK;
+}
+
 }  // namespace
 
 // Batched mixed-precision solve of nrhs <= 64 systems A x_q = b_q on one
@@ -1622,10 +1715,7 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
       // reach its target from its observed convergence rate
       int next_check = std::min(5, m);
       for (int j = 0; j < m && total < max_its; ++j) {
-        float* zj = S.Z + (size_t)j * ld;
-        if ((rc = bprecond(c, S.V + (size_t)j * ld, zj, st))) return rc;
-        if ((rc = bres<float>(c, M.blk, M.W, zj, nullptr, S.t1, nullptr, RF_NEG, nullptr, st))) return rc;
-        if ((rc = bcgs(c, j, S.t1, m, st))) return rc;
+        if ((rc = run_bstep(c, j, m, st))) return rc;
         ++total;
         k = j + 1;
         for (int q = 0; q < kNR; ++q)

@@ -125,3 +125,47 @@ def test_autotuner_times_every_variant():
     assert set(us) == set(KERNELS)
     assert us[chosen] == min(us.values())
     s.close()
+
+
+@pytest.mark.parametrize("kernel", ["mma_sync4", "tcgen05_ws"])
+def test_batched_step_graphs_match_direct_launches(kernel):
+    """Each inner Arnoldi step of the batched solve is replayed as one CUDA
+    graph (captured at its first use): the solve must give the same
+    iterates as direct launches, count the same kernels, and capture again
+    when the smoothing kernel changes between solves."""
+    from dg_nn_public_gb300 import _capi
+    m = mesh.build_mesh("tet", 5, seed=3)
+    s = DGSolver(m, sfc.hilbert_sfc_order(m.cg_coords), SolverConfig(pre_smooth_its=2, post_smooth_its=2),
+                 element.p3_element(3))
+    s.build_operator()
+    nrhs = 6
+    F = _modes(m, nrhs, seed=8)
+    Bm = torch.stack([s.rhs(torch.tensor(F[q], device="cuda:0")) for q in range(nrhs)]).contiguous()
+    tol = 1e-10 * torch.linalg.norm(Bm, dim=1).cpu().numpy()
+
+    def run(graph, k):
+        s.set_launch_options(use_graph=graph)
+        s.set_batched_kernel(k)
+        X = torch.zeros_like(Bm)
+        torch.cuda.synchronize()
+        l0 = _capi.launch_count()
+        its, res = s.solve_mixed_batched(X, Bm, tol, raise_noconv=True)
+        torch.cuda.synchronize()
+        return X, its, _capi.launch_count() - l0
+
+    other = "cuda_cores"
+    run(False, kernel)                    # first solve: builds the mixed operator copies
+    Xd, itd, nd = run(False, kernel)
+    Xg, itg, ng = run(True, kernel)       # captures
+    Xr, itr, nr = run(True, kernel)       # replays
+    Xo, ito, _ = run(True, other)         # new kernel: captured again
+    Xod, itod, _ = run(False, other)
+    print("%s: its %s, kernels direct %d / graph %d / replay %d" % (kernel, itd.tolist(), nd, ng, nr))
+    assert itg.tolist() == itd.tolist() and itr.tolist() == itd.tolist()
+    assert nd == ng == nr
+    for Xa in (Xg, Xr):
+        assert float(torch.abs(Xa - Xd).max() / torch.abs(Xd).max()) < 1e-12
+    assert ito.tolist() == itod.tolist()
+    assert float(torch.abs(Xo - Xod).max() / torch.abs(Xod).max()) < 1e-12
+    s.set_launch_options(use_graph=True)
+    s.close()
