@@ -76,6 +76,7 @@ _SIGNATURES = {
     "dg_precond_f32": (_I, [_P, _P, _P, _P]),
     "dg_set_mixed_options": (_I, [_P, C.c_int32, C.c_double, C.c_int32, C.c_int32]),
     "dg_set_launch_options": (_I, [_P, C.c_int32, C.c_int32]),
+    "dg_set_vcycle_cluster": (_I, [_P, C.c_int32, C.POINTER(C.c_int32)]),
     "dg_residual_norm_noalloc": (_I, [_P, _P, _P, _P, _P, _P]),
     "dg_p1cg_sparsity": (_I, [C.c_int64, C.c_int32, _P, C.c_int64, _P, _P, C.c_int64, _P]),
     "dg_color2": (_I, [C.c_int64, _P, _P, _P, _P]),

@@ -256,6 +256,10 @@ __global__ void rap_gather_kernel(const double* __restrict__ G, const int* __res
 // LPR lanes share a row (strided over its entries, shuffle-reduced) so the
 // dependent loads of a row are spread over lanes instead of chained.
 constexpr int LPR = 8;
+// explicit fused multiply-add (the cluster V-cycle repeats these operations
+// bit for bit)
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
 template <typename T = double>
 __global__ void lev_jacobi_kernel(const int* __restrict__ rowptr, const int* __restrict__ col,
                                   const T* __restrict__ val, const T* __restrict__ diag,
@@ -285,14 +289,14 @@ __global__ void lev_jacobi_kernel(const int* __restrict__ rowptr, const int* __r
   if (i < n && e_in) {
 #pragma unroll
     for (int q = 0; q < PRE; ++q)
-      if (k0 + q * LPR < k1) s += vpre[q] * e_in[cpre[q]];
-    for (int k = k0 + PRE * LPR; k < k1; k += LPR) s += val[k] * e_in[col[k]];
+      if (k0 + q * LPR < k1) s = fma_t(vpre[q], e_in[cpre[q]], s);
+    for (int k = k0 + PRE * LPR; k < k1; k += LPR) s = fma_t(val[k], e_in[col[k]], s);
   }
 #pragma unroll
   for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
   if (i >= n || lane != 0) return;
   const T rr = b[i] - s;
-  e_out[i] = (e_in ? e_in[i] : (T)0) + rr / diag[i] * (T)w;
+  e_out[i] = fma_t(rr / diag[i], (T)w, e_in ? e_in[i] : (T)0);
   if (rr_out) rr_out[i] = rr;
 }
 

@@ -89,6 +89,16 @@ struct Mixed {
   unsigned* gs_cnt = nullptr;
   // batched (multi-RHS) solve state (dg_batched.cuh)
   void* batch = nullptr;
+  // cluster V-cycle (dg_vcycle_cluster.cuh): CTAs per cluster (0 = the
+  // launch chain) and dynamic shared memory per CTA, set per mixed build
+  int vc_cs = 0;
+  size_t vc_smem = 0;
+  // per level: rows per CTA slice, shared-memory word offsets of the slice
+  // vectors and of the image's row offsets / diagonal / entries
+  std::vector<int> vc_ch, vc_off, vc_rpo, vc_dgo, vc_eno;
+  int vc_vwords = 0, vc_iwords = 0;   // words of slice vectors / of one CTA's image
+  int32_t* vc_img = nullptr;          // the images of all CTAs
+  size_t vc_img_cap = 0;
 };
 
 void destroy_batch(void* batch);   // dg_batched.cuh
@@ -144,8 +154,17 @@ int launch_k2(dg_ctx* c, void (*kern)(KArgs...), dim3 grid, unsigned block, size
 // the fixed inverse is read into registers (float4, up to 20 per lane, i.e.
 // n <= 2560 without a second pass) before the programmatic-launch wait, so
 // the 21.5 MB read overlaps the previous kernel; r is read after the wait.
+// With rr_src, r is formed on the fly as the pair sums of the finer level's
+// residual (r[k] = rr_src[2k] + rr_src[2k+1], zero pad at n_src: the SFC
+// restriction, lev_restrict_kernel), so the restriction needs no launch.
+__device__ __forceinline__ float dense_r(const float* __restrict__ r, const float* __restrict__ rr, int n_src,
+                                         int k) {
+  if (!rr) return r[k];
+  return rr[2 * k] + (2 * k + 1 < n_src ? rr[2 * k + 1] : 0.0f);
+}
+
 __global__ void dense_matvec_kernel(const float* __restrict__ Ainv, const float* __restrict__ r,
-                                    float* __restrict__ e, int n) {
+                                    float* __restrict__ e, int n, const float* __restrict__ rr_src, int n_src) {
   constexpr int PRE = 20;
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
@@ -178,28 +197,92 @@ __global__ void dense_matvec_kernel(const float* __restrict__ Ainv, const float*
     for (int q = 0; q < PRE; ++q) {
       const int k4 = lane + 32 * q;
       if (k4 < n4) {
-        const float4 rv = reinterpret_cast<const float4*>(r)[k4];
-        s += a[q].x * rv.x + a[q].y * rv.y + a[q].z * rv.z + a[q].w * rv.w;
+        s = __fmaf_rn(a[q].x, dense_r(r, rr_src, n_src, 4 * k4), s);
+        s = __fmaf_rn(a[q].y, dense_r(r, rr_src, n_src, 4 * k4 + 1), s);
+        s = __fmaf_rn(a[q].z, dense_r(r, rr_src, n_src, 4 * k4 + 2), s);
+        s = __fmaf_rn(a[q].w, dense_r(r, rr_src, n_src, 4 * k4 + 3), s);
       }
     }
     for (int k4 = lane + 32 * PRE; k4 < n4; k4 += 32) {
-      const float4 av = reinterpret_cast<const float4*>(ar)[k4], rv = reinterpret_cast<const float4*>(r)[k4];
-      s += av.x * rv.x + av.y * rv.y + av.z * rv.z + av.w * rv.w;
+      const float4 av = reinterpret_cast<const float4*>(ar)[k4];
+      s = __fmaf_rn(av.x, dense_r(r, rr_src, n_src, 4 * k4), s);
+      s = __fmaf_rn(av.y, dense_r(r, rr_src, n_src, 4 * k4 + 1), s);
+      s = __fmaf_rn(av.z, dense_r(r, rr_src, n_src, 4 * k4 + 2), s);
+      s = __fmaf_rn(av.w, dense_r(r, rr_src, n_src, 4 * k4 + 3), s);
     }
   } else {
 #pragma unroll
     for (int q = 0; q < PRE; ++q) {
       const int k = lane + 128 * q;
-      if (k < n) s += a[q].x * r[k];
-      if (k + 32 < n) s += a[q].y * r[k + 32];
-      if (k + 64 < n) s += a[q].z * r[k + 64];
-      if (k + 96 < n) s += a[q].w * r[k + 96];
+      if (k < n) s = __fmaf_rn(a[q].x, dense_r(r, rr_src, n_src, k), s);
+      if (k + 32 < n) s = __fmaf_rn(a[q].y, dense_r(r, rr_src, n_src, k + 32), s);
+      if (k + 64 < n) s = __fmaf_rn(a[q].z, dense_r(r, rr_src, n_src, k + 64), s);
+      if (k + 96 < n) s = __fmaf_rn(a[q].w, dense_r(r, rr_src, n_src, k + 96), s);
     }
-    for (int k = lane + 128 * PRE; k < n; k += 32) s += ar[k] * r[k];
+    for (int k = lane + 128 * PRE; k < n; k += 32) s = __fmaf_rn(ar[k], dense_r(r, rr_src, n_src, k), s);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if (lane == 0) e[row] = s;
+}
+
+// SFC-level Jacobi sweep (lev_jacobi_kernel, FP32, LPR lanes per row) whose
+// input iterate is formed on the fly from the neighbouring level, so that
+// the transfer between levels needs no launch of its own:
+//   MODE 1 (restriction in): e_in[j] = ea[2j] + ea[2j+1] and
+//     r[i] = eb[2i] + eb[2i+1] (zero pad at n_src; lev_restrict_kernel),
+//     r is stored for the level's later sweeps;
+//   MODE 2 (prolongation in): e_in[j] = ea[j] + eb[up[j]]
+//     (lev_prolong_kernel), r read as given.
+// Then rr = r - A e_in, e_out = e_in + rr / diag * w, rr_out = rr (if set):
+// the same operations as the transfer launch followed by the sweep.
+template <int MODE>
+__global__ void lev_jacobi_x_kernel(const int* __restrict__ rowptr, const int* __restrict__ col,
+                                    const float* __restrict__ val, const float* __restrict__ diag,
+                                    const float* __restrict__ ea, const float* __restrict__ eb,
+                                    const int* __restrict__ up, int n_src, float* __restrict__ r,
+                                    float* __restrict__ e_out, float* __restrict__ rr_out, int n, float w) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / LPR, lane = t % LPR;
+  constexpr int PRE = 4;
+  int k0 = 0, k1 = 0;
+  int cpre[PRE];
+  float vpre[PRE];
+  if (i < n) {
+    k0 = rowptr[i] + lane;
+    k1 = rowptr[i + 1];
+  }
+#pragma unroll
+  for (int q = 0; q < PRE; ++q) {
+    const int k = k0 + q * LPR;
+    cpre[q] = k < k1 ? col[k] : 0;
+    vpre[q] = k < k1 ? val[k] : 0.0f;
+  }
+  pdl_wait_then_trigger();
+  auto ein = [&](int j) -> float {
+    if (MODE == 1) return ea[2 * j] + (2 * j + 1 < n_src ? ea[2 * j + 1] : 0.0f);
+    return ea[j] + eb[up[j]];
+  };
+  float s = 0.0f;
+  if (i < n) {
+#pragma unroll
+    for (int q = 0; q < PRE; ++q)
+      if (k0 + q * LPR < k1) s = __fmaf_rn(vpre[q], ein(cpre[q]), s);
+    for (int k = k0 + PRE * LPR; k < k1; k += LPR) s = __fmaf_rn(val[k], ein(col[k]), s);
+  }
+#pragma unroll
+  for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, LPR);
+  if (i >= n || lane != 0) return;
+  float ri;
+  if (MODE == 1) {
+    ri = eb[2 * i] + (2 * i + 1 < n_src ? eb[2 * i + 1] : 0.0f);
+    r[i] = ri;
+  } else {
+    ri = r[i];
+  }
+  const float rr = ri - s;
+  e_out[i] = __fmaf_rn(rr / diag[i], w, ein(i));
+  if (rr_out) rr_out[i] = rr;
 }
 
 // ---------------------------------------------------------------------------
@@ -945,9 +1028,14 @@ __global__ void __launch_bounds__(160) prolong_cg32_kernel(float* __restrict__ x
 
 // vertex gather of the element P1 restrictions (mixed path): one warp per
 // vertex, lanes over the vertex's DG copies, shuffle-reduced
+// With e_out, also the first Jacobi sweep of SFC level 0 from a zero guess
+// (lev_jacobi_kernel with e_in = NULL: rr = r, e_out = fma(rr / diag, w, 0),
+// rr_out = rr if set), so that sweep needs no launch of its own.
 __global__ void gather_cg32_kernel(const float* __restrict__ r1, const int* __restrict__ gptr,
                                    const int* __restrict__ gent, const double* __restrict__ wdg,
-                                   const int* __restrict__ pos, float* __restrict__ out, int ncg) {
+                                   const int* __restrict__ pos, float* __restrict__ out, int ncg,
+                                   const float* __restrict__ diag0, float* __restrict__ e_out,
+                                   float* __restrict__ rr_out, float w) {
   const int i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
   int k0 = 0, k1 = 0;
@@ -960,11 +1048,18 @@ __global__ void gather_cg32_kernel(const float* __restrict__ r1, const int* __re
   float acc = 0.0f;
   for (int k = k0 + lane; k < k1; k += 32) {
     const int ent = gent[k];
-    acc += (float)wdg[ent] * r1[ent];
+    acc = __fmaf_rn((float)wdg[ent], r1[ent], acc);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if (lane == 0) out[pos[i]] = acc;
+  if (lane != 0) return;
+  const int p = pos[i];
+  out[p] = acc;
+  if (e_out) {
+    const float rr = acc - 0.0f;
+    e_out[p] = __fmaf_rn(rr / diag0[p], w, 0.0f);
+    if (rr_out) rr_out[p] = rr;
+  }
 }
 
 template <int D>
@@ -993,6 +1088,272 @@ int launch_transfer32(dg_ctx* c, const float* r, float* cg_out, float* x_add, co
 int transfer32(dg_ctx* c, const float* r, float* cg_out, float* x_add, const float* e_sfc, cudaStream_t st) {
   return c->D == 3 ? launch_transfer32<3>(c, r, cg_out, x_add, e_sfc, st)
                    : launch_transfer32<2>(c, r, cg_out, x_add, e_sfc, st);
+}
+
+#include "dg_vcycle_cluster.cuh"
+
+// Picks the cluster size of the V-cycle legs for this mixed build and
+// lays out their shared memory: the request (dg_ctx::vc32_cluster), limited
+// to kVcMaxLev levels above the dense level, to what fits in kVcSmemMax
+// bytes per CTA and to what the device can schedule.  Per CTA: the slice
+// vectors of every level above the dense one (4 x rows per CTA words each),
+// then the matrix image of its rows (row offsets, diagonal, entries as
+// (owner << 20 | slice index of the column, value bits)), built here from
+// the device's FP32 level matrices and uploaded once per build.
+int setup_vcycle_cluster(dg_ctx* c, cudaStream_t st) {
+  Mixed& M = mixed_of(c);
+  M.vc_cs = 0;
+  M.vc_smem = 0;
+  const int lc = M.dense_l;
+  if (c->vc32_cluster == 0 || lc < 1 || lc > kVcMaxLev) return DG_OK;
+  // the FP32 level matrices as the chain's kernels read them
+  std::vector<std::vector<int>> rp(lc), cl(lc);
+  std::vector<std::vector<float>> vl(lc), dg(lc);
+  for (int l = 0; l < lc; ++l) {
+    const Lev32& L = M.lev[l];
+    rp[l].resize(L.n + 1);
+    CK(c, cudaMemcpyAsync(rp[l].data(), L.rowptr, sizeof(int) * (L.n + 1), cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    const int nnz = rp[l][L.n];
+    cl[l].resize(nnz);
+    vl[l].resize(nnz);
+    dg[l].resize(L.n);
+    CK(c, cudaMemcpyAsync(cl[l].data(), L.col, sizeof(int) * nnz, cudaMemcpyDeviceToHost, st));
+    CK(c, cudaMemcpyAsync(vl[l].data(), L.val, sizeof(float) * nnz, cudaMemcpyDeviceToHost, st));
+    CK(c, cudaMemcpyAsync(dg[l].data(), L.diag, sizeof(float) * L.n, cudaMemcpyDeviceToHost, st));
+  }
+  CK(c, cudaStreamSynchronize(st));
+  auto pad = [](int64_t x, int64_t m) { return (x + m - 1) / m * m; };
+  for (int cs : {16, 8}) {
+    if (c->vc32_cluster > 0 && cs != c->vc32_cluster) continue;
+    std::vector<int> ch(lc + 1), off(lc, 0), rpo(lc), dgo(lc), eno(lc);
+    int64_t vwords = 0, iwords = 0;
+    bool fits = true;
+    for (int l = 0; l <= lc; ++l) ch[l] = (int)((M.lev[l].n + cs - 1) / cs);
+    for (int l = 0; l < lc; ++l) {
+      if (ch[l] >= (1 << kVcLocalBits)) fits = false;
+      off[l] = (int)vwords;
+      vwords += 4 * (int64_t)ch[l];
+      int64_t maxnnz = 0;
+      for (int r = 0; r < cs; ++r) {
+        const int s0 = std::min(M.lev[l].n, r * ch[l]), s1 = std::min(M.lev[l].n, s0 + ch[l]);
+        maxnnz = std::max<int64_t>(maxnnz, rp[l][s1] - rp[l][s0]);
+      }
+      rpo[l] = (int)iwords;
+      iwords += pad(ch[l] + 1, 2);
+      dgo[l] = (int)iwords;
+      iwords += pad(ch[l], 2);
+      eno[l] = (int)iwords;
+      iwords += 2 * maxnnz;
+    }
+    vwords = pad(vwords, 4);
+    iwords = pad(iwords, 4);
+    if (!fits || (vwords + iwords) * 4 > kVcSmemMax) continue;
+    const size_t smem = (size_t)(vwords + iwords) * 4;
+    bool ok = true;
+    for (auto k : {vcycle_down_kernel, vcycle_up_kernel}) {
+      // the same limit for every context of the process (the attribute is
+      // per kernel); each launch asks for its own size
+      ok = ok && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kVcSmemMax) == cudaSuccess;
+      if (cs > 8) ok = ok && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+    }
+    int ncl = 0;
+    if (ok) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(cs);
+      cfg.blockDim = dim3(kVcThreads);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      ok = cudaOccupancyMaxActiveClusters(&ncl, vcycle_down_kernel, &cfg) == cudaSuccess && ncl >= 1;
+    }
+    cudaGetLastError();
+    if (!ok) continue;
+    // the images of all CTAs, one after another
+    std::vector<int32_t> img((size_t)cs * iwords, 0);
+    for (int r = 0; r < cs; ++r) {
+      int32_t* I = img.data() + (size_t)r * iwords;
+      for (int l = 0; l < lc; ++l) {
+        const int n = M.lev[l].n;
+        const int s0 = std::min(n, r * ch[l]), s1 = std::min(n, s0 + ch[l]);
+        const int kb = rp[l][s0];
+        for (int i = s0; i <= s1; ++i) I[rpo[l] + (i - s0)] = rp[l][i] - kb;
+        for (int i = s0; i < s1; ++i) std::memcpy(&I[dgo[l] + (i - s0)], &dg[l][i], 4);
+        for (int k = kb; k < rp[l][s1]; ++k) {
+          const int col = cl[l][k];
+          const int o = col / ch[l], loc = col - o * ch[l];
+          I[eno[l] + 2 * (k - kb)] = (o << kVcLocalBits) | loc;
+          std::memcpy(&I[eno[l] + 2 * (k - kb) + 1], &vl[l][k], 4);
+        }
+      }
+    }
+    if (M.vc_img_cap < img.size()) {
+      int rc;
+      if ((rc = dalloc(c, &M.vc_img, img.size()))) return rc;
+      M.vc_img_cap = img.size();
+    }
+    CK(c, cudaMemcpyAsync(M.vc_img, img.data(), sizeof(int32_t) * img.size(), cudaMemcpyHostToDevice, st));
+    CK(c, cudaStreamSynchronize(st));
+    M.vc_cs = cs;
+    M.vc_smem = smem;
+    M.vc_ch = ch;
+    M.vc_off = off;
+    M.vc_rpo = rpo;
+    M.vc_dgo = dgo;
+    M.vc_eno = eno;
+    M.vc_vwords = (int)vwords;
+    M.vc_iwords = (int)iwords;
+    break;
+  }
+  if (c->verbose)
+    std::fprintf(stderr, "[mixed] V-cycle legs: %s (cluster %d, %zu B shared per CTA)\n",
+                 M.vc_cs ? "cluster launches" : "launch chain", M.vc_cs, M.vc_smem);
+  return DG_OK;
+}
+
+int launch_vc(dg_ctx* c, void (*kern)(const VcParams), const VcParams& p, cudaStream_t st) {
+  Mixed& M = mixed_of(c);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(M.vc_cs);
+  cfg.blockDim = dim3(kVcThreads);
+  cfg.dynamicSmemBytes = M.vc_smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[2];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = M.vc_cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[1].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = c->use_pdl ? 2 : 1;
+  CK(c, cudaLaunchKernelEx(&cfg, kern, p));
+  bump();
+  return DG_OK;
+}
+
+// The FP32 V-cycle with the dense coarse level as three launches: the
+// cluster down leg (the vertex gather of M.r1 included), the dense mat-vec,
+// the cluster up leg.  Same operations and result buffer (M.lev[0].e) as
+// gather_cg32_kernel + vcycle32.
+int vcycle32_cluster(dg_ctx* c, cudaStream_t st) {
+  Mixed& M = mixed_of(c);
+  const int lc = M.dense_l;
+  VcParams p = {};
+  const int V = M.vc_vwords;
+  for (int l = 0; l <= lc; ++l) {
+    const Lev32& L = M.lev[l];
+    const int ch = M.vc_ch[l];
+    const bool sl = l < lc;
+    p.lev[l] = VcLevel{L.up, L.e, L.r, L.n, ch, sl ? M.vc_off[l] : 0, sl ? V + M.vc_rpo[l] : 0,
+                       sl ? V + M.vc_dgo[l] : 0, sl ? V + M.vc_eno[l] : 0, 1.0f / (float)ch};
+  }
+  p.lc = lc;
+  p.npre = c->mixed_lev_sweeps >= 0 ? c->mixed_lev_sweeps : c->cfg.pre_smooth_its;
+  p.npost = c->mixed_lev_sweeps >= 0 ? c->mixed_lev_sweeps : c->cfg.post_smooth_its;
+  p.w = (float)c->cfg.jac_wei;
+  p.img = reinterpret_cast<const int4*>(M.vc_img);
+  p.img_words = M.vc_iwords;
+  p.img_off = V;
+  p.r1 = M.r1;
+  p.gptr = c->d_gptr;
+  p.gent = c->d_gent;
+  p.wdg = c->d_wdg;
+  p.pos = c->d_pos;
+  p.ncg = (int)c->ncg;
+  int rc;
+  if ((rc = launch_vc(c, vcycle_down_kernel, p, st))) return rc;
+  {
+    Lev32& L = M.lev[lc];
+    if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, 0, st, (const float*)M.dense_inv,
+                       (const float*)L.r, L.e, L.n, (const float*)nullptr, 0)))
+      return rc;
+  }
+  if ((rc = launch_vc(c, vcycle_up_kernel, p, st))) return rc;
+  CKL(c);
+  return DG_OK;
+}
+
+// The FP32 V-cycle with the dense coarse level (dense_l >= 1) as a launch
+// chain in which no transfer between levels has a launch of its own: the
+// vertex gather also runs level 0's first sweep (zero guess), each coarser
+// level's first sweep restricts its input on the fly (lev_jacobi_x_kernel
+// mode 1), the dense mat-vec restricts its right-hand side on the fly, and
+// each level's first post-sweep adds the prolonged coarse correction on the
+// fly (mode 2).  Same operations, buffers and e / e2 swaps as
+// gather_cg32_kernel + vcycle32; c2: 11 launches instead of 17.
+int vcycle32_fused(dg_ctx* c, cudaStream_t st) {
+  Mixed& M = mixed_of(c);
+  const int lc = M.dense_l;
+  const float w = (float)c->cfg.jac_wei;
+  const int TB = 128;
+  const int npre = c->mixed_lev_sweeps >= 0 ? c->mixed_lev_sweeps : c->cfg.pre_smooth_its;
+  const int npost = c->mixed_lev_sweeps >= 0 ? c->mixed_lev_sweeps : c->cfg.post_smooth_its;
+  int rc;
+  {
+    Lev32& L = M.lev[0];
+    if ((rc = launch_k(c, gather_cg32_kernel, nblk(c->ncg, 8), 256, 0, st, (const float*)M.r1,
+                       (const int*)c->d_gptr, (const int*)c->d_gent, (const double*)c->d_wdg, (const int*)c->d_pos,
+                       L.r, (int)c->ncg, (const float*)L.diag, L.e2, npre == 0 ? L.rr : (float*)nullptr, w)))
+      return rc;
+    std::swap(L.e, L.e2);
+  }
+  for (int l = 0; l < lc; ++l) {
+    Lev32& L = M.lev[l];
+    const unsigned gj = nblk((int64_t)L.n * LPR, TB);
+    for (int it = l == 0 ? 1 : 0; it <= npre; ++it) {
+      float* keep = it == npre ? L.rr : nullptr;
+      if (it == 0) {
+        const Lev32& P = M.lev[l - 1];
+        rc = launch_k(c, lev_jacobi_x_kernel<1>, gj, TB, 0, st, (const int*)L.rowptr, (const int*)L.col,
+                      (const float*)L.val, (const float*)L.diag, (const float*)P.e, (const float*)P.rr,
+                      (const int*)nullptr, P.n, L.r, L.e2, keep, L.n, w);
+      } else {
+        rc = launch_k(c, lev_jacobi_kernel<float>, gj, TB, 0, st, (const int*)L.rowptr, (const int*)L.col,
+                      (const float*)L.val, (const float*)L.diag, (const float*)L.e, (const float*)L.r, L.e2, keep,
+                      L.n, (double)c->cfg.jac_wei);
+      }
+      if (rc) return rc;
+      std::swap(L.e, L.e2);
+    }
+  }
+  {
+    Lev32& L = M.lev[lc];
+    const Lev32& P = M.lev[lc - 1];
+    if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, 0, st, (const float*)M.dense_inv,
+                       (const float*)nullptr, L.e, L.n, (const float*)P.rr, P.n)))
+      return rc;
+  }
+  for (int l = lc - 1; l >= 0; --l) {
+    Lev32& L = M.lev[l];
+    const float* enext = M.lev[l + 1].e;
+    const unsigned gj = nblk((int64_t)L.n * LPR, TB);
+    if (npost == 0) {
+      if ((rc = launch_k(c, lev_prolong_kernel<float>, nblk(L.n, TB), TB, 0, st, L.e, enext, (const int*)L.up, L.n)))
+        return rc;
+      continue;
+    }
+    for (int it = 0; it < npost; ++it) {
+      if (it == 0)
+        rc = launch_k(c, lev_jacobi_x_kernel<2>, gj, TB, 0, st, (const int*)L.rowptr, (const int*)L.col,
+                      (const float*)L.val, (const float*)L.diag, (const float*)L.e, enext, (const int*)L.up, 0, L.r,
+                      L.e2, (float*)nullptr, L.n, w);
+      else
+        rc = launch_k(c, lev_jacobi_kernel<float>, gj, TB, 0, st, (const int*)L.rowptr, (const int*)L.col,
+                      (const float*)L.val, (const float*)L.diag, (const float*)L.e, (const float*)L.r, L.e2,
+                      (float*)nullptr, L.n, (double)c->cfg.jac_wei);
+      if (rc) return rc;
+      std::swap(L.e, L.e2);
+    }
+  }
+  CKL(c);
+  return DG_OK;
 }
 
 // FP32 SFC V-cycle (same schedule as vcycle() down to the coarse level,
@@ -1039,7 +1400,7 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
     {
       Lev32& L = M.lev[lc];
       if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, 0, st, (const float*)M.dense_inv,
-                         (const float*)L.r, L.e, L.n)))
+                         (const float*)L.r, L.e, L.n, (const float*)nullptr, 0)))
         return rc;
     }
     for (int l = lc - 1; l >= 0; --l) {
@@ -1131,11 +1492,18 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
     CK(c, cudaMemsetAsync(cur, 0, sizeof(float) * c->nonods, st));
   }
   if ((rc = residual_pc(c, cur, r, nullptr, nullptr, RF_RESTRICT, st))) return rc;   // -> M.r1
-  float* cg_dst = M.dense_l > 0 ? M.lev[0].r : M.cg1;
-  if ((rc = launch_k(c, gather_cg32_kernel, nblk(c->ncg, 8), 256, 0, st, (const float*)M.r1, (const int*)c->d_gptr,
-                     (const int*)c->d_gent, (const double*)c->d_wdg, (const int*)c->d_pos, cg_dst, (int)c->ncg)))
-    return rc;
-  if ((rc = vcycle32(c, cg_dst, st))) return rc;
+  if (M.vc_cs > 0) {
+    if ((rc = vcycle32_cluster(c, st))) return rc;   // gather included
+  } else if (M.dense_l > 0 && c->vc32_fused) {
+    if ((rc = vcycle32_fused(c, st))) return rc;     // gather included
+  } else {
+    float* cg_dst = M.dense_l > 0 ? M.lev[0].r : M.cg1;
+    if ((rc = launch_k(c, gather_cg32_kernel, nblk(c->ncg, 8), 256, 0, st, (const float*)M.r1,
+                       (const int*)c->d_gptr, (const int*)c->d_gent, (const double*)c->d_wdg, (const int*)c->d_pos,
+                       cg_dst, (int)c->ncg, (const float*)nullptr, (float*)nullptr, (float*)nullptr, 0.0f)))
+      return rc;
+    if ((rc = vcycle32(c, cg_dst, st))) return rc;
+  }
   if ((rc = transfer32(c, nullptr, nullptr, cur, M.lev[0].e, st))) return rc;
   for (int it = 0; it < nsm; ++it) {
     float* out = (it == nsm - 1) ? z : other;
@@ -1408,6 +1776,7 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
     }
   }
   CKL(c);
+  if ((rc = setup_vcycle_cluster(c, st))) return rc;
   M.built = true;
   if (!M.d_ws && (rc = dalloc(c, &M.d_ws, 4))) return rc;
   if (!c->omegas_set && c->mixed_smoother == 1) {
@@ -2213,6 +2582,26 @@ extern "C" int dg_apply_f32(dg_ctx* c, const float* x, float* y, void* stream) {
     c->mixed_version = c->build_version;
   }
   return residual32(c, x, nullptr, y, nullptr, RF_NEG, st);
+}
+
+// V-cycle legs of the mixed preconditioner as cluster launches (-1 = auto,
+// 0 = the launch chain, 8 / 16 = that cluster size when it fits).  Takes
+// effect at once for a built mixed operator; cached graphs are dropped.
+extern "C" int dg_set_vcycle_cluster(dg_ctx* c, int32_t cluster, int32_t* chosen) {
+  if (!c) return set_thread_error(DG_ERR_ARG, "dg_set_vcycle_cluster: null context");
+  if (cluster != -1 && cluster != 0 && cluster != 8 && cluster != 16)
+    return fail(c, DG_ERR_ARG, "dg_set_vcycle_cluster: cluster must be -1, 0, 8 or 16");
+  CK(c, cudaSetDevice(c->dev));
+  c->vc32_cluster = cluster;
+  Mixed& M = mixed_of(c);
+  for (auto& g : M.graphs)
+    if (g) cudaGraphExecDestroy(g);
+  M.graphs.clear();
+  M.g_m = 0;
+  int rc;
+  if (M.built && (rc = setup_vcycle_cluster(c, nullptr))) return rc;
+  if (chosen) *chosen = M.built ? M.vc_cs : -1;
+  return DG_OK;
 }
 
 // z = the mixed preconditioner (FP32 V-cycle with the BF16/FP32 block copies)

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <string>
 #include <type_traits>
@@ -142,6 +143,14 @@ struct dg_ctx {
   // correction and Jacobi sweeps on the SFC levels (-1 = the configured
   // pre_smooth_its, as in the FP64 preconditioner)
   int mixed_sweeps = -1, mixed_lev_sweeps = -1;
+  // FP32 SFC V-cycle legs of the mixed preconditioner as thread-block-
+  // cluster launches: -1 = the largest cluster (16, else 8) that the device
+  // schedules, 0 = the launch chain (default: measured faster at c2),
+  // 8 / 16 = that cluster size (dg_set_vcycle_cluster, DG_MIXED_VC_CLUSTER)
+  int vc32_cluster = 0;
+  // the launch chain of that V-cycle without launches of its own for the
+  // transfers between levels (vcycle32_fused; DG_MIXED_VC_FUSED=0: off)
+  bool vc32_fused = true;
   // mixed preconditioner with two DG-level smoothing steps: step k damped by
   // mixed_smooth_w * mixed_wscale[k] (pre-smoothing k = 0, 1; post-smoothing
   // in reverse), a degree-2 Chebyshev polynomial smoother whose factors are
@@ -891,6 +900,10 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (msw && msw[0]) c->mixed_sweeps = std::atoi(msw);
     const char* mlw = std::getenv("DG_MIXED_LEV_SWEEPS");
     if (mlw && mlw[0]) c->mixed_lev_sweeps = std::atoi(mlw);
+    const char* vcc = std::getenv("DG_MIXED_VC_CLUSTER");
+    if (vcc && vcc[0]) c->vc32_cluster = std::atoi(vcc);
+    const char* vcf = std::getenv("DG_MIXED_VC_FUSED");
+    if (vcf && vcf[0]) c->vc32_fused = vcf[0] != '0';
     const char* tv = std::getenv("DG_TMA_VARIANT");
     if (tv && tv[0]) {
       c->tma_variant = std::atoi(tv);

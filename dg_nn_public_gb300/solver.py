@@ -366,6 +366,16 @@ class DGSolver:
         launches inside a mixed inner step (both on by default)."""
         self._chk(self._lib.dg_set_launch_options(self._ctx, 1 if use_graph else 0, 1 if use_pdl else 0))
 
+    def set_vcycle_cluster(self, cluster=-1):
+        """SFC V-cycle legs of the mixed preconditioner as thread-block-cluster
+        launches: -1 = auto (16 CTAs, else 8), 0 = the launch chain (the
+        default), 8 / 16.  Returns the cluster size in use (0 = chain), or -1
+        before the first mixed solve."""
+        import ctypes as C
+        out = C.c_int32(-1)
+        self._chk(self._lib.dg_set_vcycle_cluster(self._ctx, int(cluster), C.byref(out)))
+        return out.value
+
     # library defaults of the mixed preconditioner (dg_create)
     mixed_options = dict(smoother="blockinv", smooth_w=0.8, precond_bf16=True, dense_max=2400)
 

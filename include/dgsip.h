@@ -243,6 +243,16 @@ int dg_set_mixed_options(dg_ctx* ctx, int32_t smoother, double smooth_w, int32_t
  * again at the next solve. */
 int dg_set_launch_options(dg_ctx* ctx, int32_t use_graph, int32_t use_pdl);
 
+/* SFC V-cycle of the mixed preconditioner (no counterpart in the reference):
+ * cluster = -1 runs its down and up legs each as one thread-block-cluster
+ * launch of 16 CTAs (8 where 16 is not schedulable), 0 as the chain of
+ * per-sweep launches (default: faster at c2), 8 / 16 with that cluster size.
+ * Both give the same bits.  *chosen (may be NULL) receives the size in use,
+ * 0 for the chain (also when a CTA's share of the levels does not fit its
+ * shared memory), -1 before the first mixed build.  Cached graphs are
+ * captured again at the next solve. */
+int dg_set_vcycle_cluster(dg_ctx* ctx, int32_t cluster, int32_t* chosen);
+
 /* Allocation-free residual norm (no counterpart in the reference):
  * r = b - A x and *norm_out = ||r||_2, both written on the device (r may be
  * NULL for the norm alone; b NULL means b = 0).  It allocates nothing: its

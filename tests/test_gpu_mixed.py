@@ -179,3 +179,49 @@ def test_chunk_graphs_match_direct_launches(cond, monkeypatch):
         outs[ng] = (x.cpu(), its)
     assert torch.equal(outs["0"][0], outs["1"][0])
     assert outs["0"][1] <= outs["1"][1]
+
+
+@pytest.mark.parametrize("kind,n,fits", [("tet", 14, True), ("tet", 20, True), ("tet", 28, False),
+                                         ("tri", 64, True)])
+def test_cluster_vcycle_matches_launch_chain(kind, n, fits):
+    """The SFC V-cycle legs as two thread-block-cluster launches (16 and 8
+    CTAs) against the chain of per-sweep launches: the same operations in
+    the same order, so the FP32 preconditioner agrees bit for bit; the mixed
+    solve then takes the same iterations.  1 to 4 levels above the dense
+    coarse level (3,375 to 24,389 P1 vertices); where a CTA's share of the
+    levels does not fit in its shared memory the chain runs (chosen 0)."""
+    m = mesh.build_mesh(kind, n, seed=1)
+    s = DGSolver(m, sfc.hilbert_sfc_order(m.cg_coords), SolverConfig(pre_smooth_its=2, post_smooth_its=2),
+                 element.p3_element(m.ndim))
+    s.set_kappa(np.exp(0.5 * np.random.default_rng(5).standard_normal(m.nele)))
+    s.build_operator()
+    g = torch.Generator(device="cuda:0").manual_seed(3)
+    b = torch.randn(s.nonods, dtype=torch.float32, device="cuda:0", generator=g)
+    assert s.set_vcycle_cluster(0) == -1          # before the first mixed build
+    z_chain = s.precond_f32(b).clone()
+    outs = {}
+    for cs in (16, 8, -1):
+        chosen = s.set_vcycle_cluster(cs)
+        assert chosen in ((cs, 0) if cs > 0 else (16, 8, 0)), (cs, chosen)
+        if cs == -1:
+            assert (chosen > 0) == fits, chosen
+        outs[cs] = s.precond_f32(b).clone()
+        again = s.precond_f32(b)
+        assert torch.equal(outs[cs], again)
+    torch.cuda.synchronize()
+    for cs, z in outs.items():
+        assert torch.equal(z, z_chain), cs
+    X = m.x_ref_in
+    u = np.prod([np.sin(np.pi * X[:, k]) for k in range(m.ndim)], axis=0).ravel()
+    bb = s.rhs(torch.tensor(m.ndim * np.pi ** 2 * u, device="cuda:0"))
+    tol = 1e-10 * float(torch.linalg.norm(bb))
+    res = {}
+    for cs in (0, -1):
+        s.set_vcycle_cluster(cs)
+        x = torch.zeros_like(bb)
+        its, r, outer = s.solve_mixed(x, bb, tol)
+        assert r <= tol
+        res[cs] = (its, outer, x)
+    assert res[0][:2] == res[-1][:2]
+    assert torch.equal(res[0][2], res[-1][2])
+    s.close()
