@@ -798,6 +798,84 @@ __global__ void __launch_bounds__(128) bdense_kernel(const float* __restrict__ A
   if (row0 + rr < n) reinterpret_cast<float4*>(E + (int64_t)(row0 + rr) * kNR)[q4] = acc;
 }
 
+// The same product with the k loop staged by asynchronous copies: CTA tile
+// 16 rows x 64 RHS (one CTA per SM at ~2,300 rows), 128 threads of 2 rows x
+// 4 RHS each, k tiles of 128 double-buffered in shared memory (cp.async,
+// 16-byte pieces).  Each output is one FMA chain over k = 0, 1, ..., n-1, as
+// in bdense_kernel, so both give the same bits.
+constexpr int kDnRows = 16, kDnK = 128;
+constexpr int kDnSmem = 2 * (kDnRows * kDnK + kDnK * kNR) * 4;   // 81,920 bytes
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool full) {
+  // full = false: zero-fill the 16 bytes (src-size 0), src stays in bounds
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(src), "r"(full ? 16 : 0)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(128) bdense2_kernel(const float* __restrict__ Ainv, const float* __restrict__ R,
+                                                      float* __restrict__ E, int n) {
+  extern __shared__ __align__(16) float dn_smem[];
+  float* As = dn_smem;                                // [2][kDnRows][kDnK]
+  float* Rs = dn_smem + 2 * kDnRows * kDnK;           // [2][kDnK][kNR]
+  const int row0 = blockIdx.x * kDnRows;
+  const int tid = threadIdx.x;
+  const int ty = tid / 16, tx = tid % 16;             // rows 2 ty, 2 ty + 1; RHS 4 tx .. 4 tx + 3
+  const bool vec = (n & 3) == 0;                      // 16-byte aligned rows of Ainv
+  auto stage = [&](int buf, int k0) {
+    float* as = As + buf * kDnRows * kDnK;
+    float* rs = Rs + buf * kDnK * kNR;
+    for (int i = tid; i < kDnRows * (kDnK / 4); i += 128) {
+      const int r = i / (kDnK / 4), k4 = i % (kDnK / 4);
+      const int row = row0 + r, k = k0 + 4 * k4;
+      if (vec) {
+        const bool ok = row < n && k < n;
+        cp_async16(as + r * kDnK + 4 * k4, Ainv + (ok ? (int64_t)row * n + k : 0), ok);
+      } else {
+        for (int u = 0; u < 4; ++u)
+          as[r * kDnK + 4 * k4 + u] = (row < n && k + u < n) ? Ainv[(int64_t)row * n + k + u] : 0.0f;
+      }
+    }
+    for (int i = tid; i < kDnK * (kNR / 4); i += 128) {
+      const int k = i / (kNR / 4), q4 = i % (kNR / 4);
+      const bool ok = k0 + k < n;
+      cp_async16(rs + k * kNR + 4 * q4, R + (ok ? (int64_t)(k0 + k) * kNR + 4 * q4 : 0), ok);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  float4 acc0 = make_float4(0.f, 0.f, 0.f, 0.f), acc1 = acc0;
+  const int nt = (n + kDnK - 1) / kDnK;
+  stage(0, 0);
+  for (int it = 0; it < nt; ++it) {
+    const int buf = it & 1;
+    if (it + 1 < nt) {
+      stage(buf ^ 1, (it + 1) * kDnK);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();
+    const float* as = As + buf * kDnRows * kDnK;
+    const float* rs = Rs + buf * kDnK * kNR;
+    const int kmax = min(kDnK, n - it * kDnK);
+    for (int k = 0; k < kmax; ++k) {
+      const float a0 = as[(2 * ty) * kDnK + k], a1 = as[(2 * ty + 1) * kDnK + k];
+      const float4 rv = reinterpret_cast<const float4*>(rs + k * kNR)[tx];
+      acc0.x = fmaf(a0, rv.x, acc0.x);
+      acc0.y = fmaf(a0, rv.y, acc0.y);
+      acc0.z = fmaf(a0, rv.z, acc0.z);
+      acc0.w = fmaf(a0, rv.w, acc0.w);
+      acc1.x = fmaf(a1, rv.x, acc1.x);
+      acc1.y = fmaf(a1, rv.y, acc1.y);
+      acc1.z = fmaf(a1, rv.z, acc1.z);
+      acc1.w = fmaf(a1, rv.w, acc1.w);
+    }
+    __syncthreads();   // the buffer is refilled by the next stage call
+  }
+  const int r0 = row0 + 2 * ty, r1 = r0 + 1;
+  if (r0 < n) reinterpret_cast<float4*>(E + (int64_t)r0 * kNR)[tx] = acc0;
+  if (r1 < n) reinterpret_cast<float4*>(E + (int64_t)r1 * kNR)[tx] = acc1;
+}
+
 // ---------------------------------------------------------------------------
 // Gram-Schmidt per RHS on interleaved vectors.  A block is 256 threads =
 // 4 row lanes x kNR RHS; per-thread sums FP32, the 4 lanes and the blocks
@@ -1471,7 +1549,7 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
     brestrict_kernel<<<nblk((int64_t)nn * kNR, 256), 256, 0, st>>>(S.lrr[l], S.le[l], S.lr[l + 1], S.le[l + 1], n, nn);
     bump();
   }
-  bdense_kernel<<<nblk(M.lev[lc].n, 8), 128, 0, st>>>(M.dense_inv, S.lr[lc], S.le[lc], M.lev[lc].n);
+  bdense2_kernel<<<nblk(M.lev[lc].n, kDnRows), 128, kDnSmem, st>>>(M.dense_inv, S.lr[lc], S.le[lc], M.lev[lc].n);
   bump();
   for (int l = lc - 1; l >= 0; --l) {
     const int n = M.lev[l].n;
@@ -1646,6 +1724,7 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
   CK(c, cudaFuncSetAttribute(bres_tc05_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcDyn));
   CK(c, cudaFuncSetAttribute(bres_tcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTsDyn));
   CK(c, cudaFuncSetAttribute(bres_tcw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTwDyn));
+  CK(c, cudaFuncSetAttribute(bdense2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDnSmem));
   if ((rc = autotune_batched(c, M, batch_of(M), st))) return rc;
   CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));   // bulk-copy wait time-outs land here
   BatchState& S = batch_of(M);
@@ -1656,17 +1735,43 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
   std::vector<int32_t> its(kNR, 0);
   std::vector<char> active(kNR, 0);
   for (int q = 0; q < nrhs; ++q) tolv[q] = tol[q];
-  std::vector<double> Hh((size_t)kNR * (m + 1) * m), ybuf((size_t)32 * kNR), nrm(kNR);
+  std::vector<double> Hh((size_t)kNR * (m + 1) * m), ybuf((size_t)32 * kNR), nrm(kNR), rnew(kNR);
+  // FP64 residuals r_q = b_q - A x_q (one FP64 apply per RHS, bound by the
+  // FP64 pipe) for the RHS in `redo`; the others keep r_q and |r_q|: a zero
+  // start gives r_q = b_q exactly, and an RHS that no refinement step
+  // updated keeps its x_q
+  std::vector<char> redo(kNR, 0);
   auto outer_residuals = [&]() -> int {
     int r2;
     for (int q = 0; q < nrhs; ++q) {
-      if ((r2 = residual(c, x + (size_t)q * n, b + (size_t)q * n, S.r64 + (size_t)q * n, nullptr, 0, st))) return r2;
+      if (!redo[q]) continue;
+      if (redo[q] == 2) {
+        CK(c, cudaMemcpyAsync(S.r64 + (size_t)q * n, b + (size_t)q * n, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                              st));
+      } else if ((r2 = residual(c, x + (size_t)q * n, b + (size_t)q * n, S.r64 + (size_t)q * n, nullptr, 0, st))) {
+        return r2;
+      }
       if ((r2 = norm2(c, S.r64 + (size_t)q * n, c->d_scal + q, st))) return r2;
     }
-    CK(c, cudaMemcpyAsync(rn.data(), c->d_scal, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+    CK(c, cudaMemcpyAsync(rnew.data(), c->d_scal, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
     CK(c, cudaStreamSynchronize(st));
+    for (int q = 0; q < nrhs; ++q)
+      if (redo[q]) rn[q] = rnew[q];
     return DG_OK;
   };
+  {
+    // which starting x_q are zero (2: r_q = b_q) or not (1: FP64 residual)
+    int* flag = reinterpret_cast<int*>(S.h);   // scratch until the first inner step
+    CK(c, cudaMemsetAsync(flag, 0, sizeof(int) * kNR, st));
+    bnonzero_kernel<<<dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>(2 * c->nsm, (n + 255) / 256)), nrhs), 256,
+                      0, st>>>(x, n, flag);
+    bump();
+    CKL(c);
+    std::vector<int> nz(kNR, 0);
+    CK(c, cudaMemcpyAsync(nz.data(), flag, sizeof(int) * nrhs, cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    for (int q = 0; q < nrhs; ++q) redo[q] = nz[q] ? 1 : 2;
+  }
   if ((rc = outer_residuals())) return rc;
   int total = 0, status = DG_OK;
   while (total < max_its) {
@@ -1774,6 +1879,7 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
     bupdate_kernel<<<tgrid, tblock, 0, st>>>(x, n, nrhs, S.scl, S.t6);
     bump();
     CKL(c);
+    for (int q = 0; q < nrhs; ++q) redo[q] = active[q] ? 1 : 0;
     if ((rc = outer_residuals())) return rc;
   }
   {
@@ -1824,6 +1930,7 @@ int batched_prep(dg_ctx* c, const char* name, cudaStream_t st) {
   CK(c, cudaFuncSetAttribute(bres_tc05_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcDyn));
   CK(c, cudaFuncSetAttribute(bres_tcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTsDyn));
   CK(c, cudaFuncSetAttribute(bres_tcw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTwDyn));
+  CK(c, cudaFuncSetAttribute(bdense2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDnSmem));
   return DG_OK;
 }
 

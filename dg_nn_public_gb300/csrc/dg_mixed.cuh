@@ -87,6 +87,7 @@ struct Mixed {
   // launch reduces the partial sums and resets its counter): [0, 32) one per
   // grid row of the dots, [32] the update's norm
   unsigned* gs_cnt = nullptr;
+  int* nzflag = nullptr;   // bnonzero_kernel flag of the solve's starting x
   // batched (multi-RHS) solve state (dg_batched.cuh)
   void* batch = nullptr;
   // cluster V-cycle (dg_vcycle_cluster.cuh): CTAs per cluster (0 = the
@@ -1515,6 +1516,18 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   return DG_OK;
 }
 
+// flag[q] |= 1 if x_q (row q of the RHS-major (nrhs, n) array) has an entry
+// other than +-0 (NaN counts as nonzero); grid (blocks, nrhs).  A zero start
+// needs no FP64 apply: b - A 0 = b exactly.
+__global__ void bnonzero_kernel(const double* __restrict__ x, int64_t n, int* __restrict__ flag) {
+  const int q = blockIdx.y;
+  bool nz = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    nz |= !(x[(int64_t)q * n + i] == 0.0);
+  nz = __syncthreads_or(nz);
+  if (nz && threadIdx.x == 0) atomicOr(flag + q, 1);
+}
+
 __global__ void convert_f64_f32_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) b[k] = (float)a[k];
@@ -2440,7 +2453,21 @@ extern "C" int dg_solve_mixed(dg_ctx* c, double* x, const double* b, double tol,
   float* rhs32 = M.t2;
   float* d32 = M.t6;
   float* V0 = M.V;
-  if ((rc = residual(c, x, b, r64, nullptr, 0, st))) return rc;
+  // starting residual: r = b for a zero x (no FP64 apply), else b - A x
+  if (!M.nzflag && (rc = dalloc(c, &M.nzflag, 1))) return rc;
+  CK(c, cudaMemsetAsync(M.nzflag, 0, sizeof(int), st));
+  bnonzero_kernel<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(2 * c->nsm, (n + 255) / 256)), 256, 0, st>>>(
+      x, n, M.nzflag);
+  bump();
+  CKL(c);
+  int nzx = 1;
+  CK(c, cudaMemcpyAsync(&nzx, M.nzflag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(c, cudaStreamSynchronize(st));
+  if (nzx) {
+    if ((rc = residual(c, x, b, r64, nullptr, 0, st))) return rc;
+  } else {
+    CK(c, cudaMemcpyAsync(r64, b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  }
   if ((rc = norm2(c, r64, c->d_scal, st))) return rc;
   double rn;
   if ((rc = read_scalar(c, c->d_scal, &rn, st))) return rc;
