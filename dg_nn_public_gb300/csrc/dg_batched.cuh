@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(128) bres_kernel(const MT* __restrict__ blk, c
                                                    const int* __restrict__ nbe, const float* __restrict__ x,
                                                    const float* __restrict__ b, float* __restrict__ r,
                                                    float* __restrict__ x_out, int64_t B, int flags,
-                                                   const double* __restrict__ P, float* __restrict__ r1,
+                                                   const float* __restrict__ P, float* __restrict__ r1,
                                                    const float* __restrict__ wsp) {
   constexpr int N = 20, F = 4;
   const float ws = wsp ? *wsp : 1.0f;
@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(128) bres_kernel(const MT* __restrict__ blk, c
   __shared__ __align__(16) unsigned char Ws[W_BYTES];
   __shared__ __align__(16) float xs[F + 1][N][kNR];
   __shared__ __align__(16) float rs[N][kNR];
+  __shared__ float Ps[N * F];   // P converted once per CTA, not per use (FP64 conversions are slow here)
   __shared__ int nbs[F];
   const int64_t e = blockIdx.x;
   if (e >= B) return;
@@ -74,6 +75,7 @@ __global__ void __launch_bounds__(128) bres_kernel(const MT* __restrict__ blk, c
   const bool zerox = flags & RF_ZEROX;
   const bool smooth = flags & RF_SMOOTH;
   if (tid < F) nbs[tid] = nbe[e * F + tid];
+  if ((flags & RF_RESTRICT) && tid < N * F) Ps[tid] = (float)P[tid];
   if (!zerox) {
     const uint4* src = reinterpret_cast<const uint4*>(blk + e * (F + 1) * BLK);
     for (int i = tid; i < EL_BYTES / 16; i += 128) reinterpret_cast<uint4*>(As)[i] = src[i];
@@ -161,7 +163,7 @@ __global__ void __launch_bounds__(128) bres_kernel(const MT* __restrict__ blk, c
         const int cc = o / kNR, q = o % kNR;
         float t = 0.0f;
 #pragma unroll
-        for (int n = 0; n < N; ++n) t += (float)P[n * F + cc] * rs[n][q];
+        for (int n = 0; n < N; ++n) t += Ps[n * F + cc] * rs[n][q];
         r1[(e * F + cc) * kNR + q] = t;
       }
     }
@@ -307,7 +309,7 @@ __global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat1
                                                        const int* __restrict__ nbe, const float* __restrict__ x,
                                                        const float* __restrict__ b, float* __restrict__ r,
                                                        float* __restrict__ x_out, int64_t B, int flags,
-                                                       const double* __restrict__ P, float* __restrict__ r1,
+                                                       const float* __restrict__ P, float* __restrict__ r1,
                                                        const float* __restrict__ wsp) {
   constexpr int N = 20, F = 4;
   const float ws = wsp ? *wsp : 1.0f;
@@ -316,6 +318,7 @@ __global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat1
   __shared__ __align__(16) unsigned char Xhi[kXK * kXRow];
   __shared__ __align__(16) unsigned char Xlo[kXK * kXRow];
   __shared__ __align__(16) float rs[N][kNR];
+  __shared__ float Ps[N * F];   // P converted once per CTA, not per use (FP64 conversions are slow here)
   __shared__ int nbs[F];
   const int64_t e = blockIdx.x;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -323,6 +326,8 @@ __global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat1
   const bool zerox = flags & RF_ZEROX;
   const bool smooth = flags & RF_SMOOTH;
   if (tid < F) nbs[tid] = nbe[e * F + tid];
+  if (flags & RF_RESTRICT)
+    for (int i = tid; i < N * F; i += NWARP * 32) Ps[i] = (float)P[i];
   if (!zerox)
     for (int i = tid; i < (F + 1) * 800 / 16; i += NWARP * 32)
       reinterpret_cast<uint4*>(As)[i] = reinterpret_cast<const uint4*>(blk + e * 2000)[i];
@@ -419,7 +424,7 @@ __global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat1
       const int cc = o / kNR, q = o % kNR;
       float s = 0.0f;
 #pragma unroll
-      for (int n = 0; n < N; ++n) s += (float)P[n * F + cc] * rs[n][q];
+      for (int n = 0; n < N; ++n) s += Ps[n * F + cc] * rs[n][q];
       r1[(e * F + cc) * kNR + q] = s;
     }
   }
@@ -479,7 +484,7 @@ constexpr int kBT = 256;                                 // threads: 8 warps, wa
 __global__ void __launch_bounds__(kBT, kBS) bres_mma_tma_kernel(
     const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
     const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
-    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err,
+    int64_t B, int flags, const float* __restrict__ P, float* __restrict__ r1, int* __restrict__ err,
     const float* __restrict__ wsp) {
   constexpr int N = 20, F = 4;
   const float ws = wsp ? *wsp : 1.0f;
@@ -675,17 +680,29 @@ namespace {
 // ---------------------------------------------------------------------------
 // DG <-> CG P1 transfers and SFC levels on kNR columns (thread per (row, RHS))
 
-// out[pos(i)][q] = sum over DG copies (e, c) of vertex i of w_ec * r1[(e, c)][q]
+// out[pos(i)][q] = sum over DG copies (e, c) of vertex i of w_ec * r1[(e, c)][q];
+// the vertex's entries and weights are staged once per CTA (kNR at a time),
+// so each FP64 weight is converted once, not once per RHS
 __global__ void bgather_kernel(const float* __restrict__ r1, const int* __restrict__ gptr,
-                               const int* __restrict__ gent, const double* __restrict__ wdg,
+                               const int* __restrict__ gent, const float* __restrict__ wdg,
                                const int* __restrict__ pos, float* __restrict__ out, int ncg) {
+  __shared__ int es[kNR];
+  __shared__ float ws[kNR];
   const int i = blockIdx.x;
   const int q = threadIdx.x;
   if (i >= ncg) return;
+  const int k0 = gptr[i], k1 = gptr[i + 1];
   float acc = 0.0f;
-  for (int k = gptr[i]; k < gptr[i + 1]; ++k) {
-    const int ent = gent[k];
-    acc += (float)wdg[ent] * r1[(int64_t)ent * kNR + q];
+  for (int kb = k0; kb < k1; kb += kNR) {
+    const int cnt = min(kNR, k1 - kb);
+    __syncthreads();   // the previous chunk is consumed
+    if (q < cnt) {
+      const int ent = gent[kb + q];
+      es[q] = ent;
+      ws[q] = (float)wdg[ent];
+    }
+    __syncthreads();
+    for (int k = 0; k < cnt; ++k) acc += ws[k] * r1[(int64_t)es[k] * kNR + q];
   }
   out[(int64_t)pos[i] * kNR + q] = acc;
 }
@@ -694,7 +711,7 @@ __global__ void bgather_kernel(const float* __restrict__ r1, const int* __restri
 // 320 threads per element: thread (n, quad of 4 RHS)
 __global__ void __launch_bounds__(320) bprolong_kernel(float* __restrict__ x, const float* __restrict__ ecg,
                                                        const int* __restrict__ pos, const int* __restrict__ p1cg,
-                                                       const double* __restrict__ wdg, const double* __restrict__ P,
+                                                       const float* __restrict__ wdg, const float* __restrict__ P,
                                                        int64_t B) {
   __shared__ int vp[4];
   __shared__ float wc[4];
@@ -1343,7 +1360,7 @@ template <typename MT>
 int bres(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out, int flags,
          float* r1, cudaStream_t st, const float* ws = nullptr) {
   if (c->B > 0)
-    bres_kernel<MT><<<(unsigned)c->B, 128, 0, st>>>(blk, W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, r1, ws);
+    bres_kernel<MT><<<(unsigned)c->B, 128, 0, st>>>(blk, W, c->d_nbe, x, b, r, x_out, c->B, flags, c->d_P32, r1, ws);
   bump();
   CKL(c);
   return DG_OK;
@@ -1357,7 +1374,7 @@ int btcs(dg_ctx* c, BatchState& S, const unsigned char* xs, const float* b, void
   if (c->batched_kernel == 6) {   // warp-specialized, one CTA per SM
     const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm);
     if (g)
-      bres_tcw_kernel<<<g, kTwT, kTwDyn, st>>>(S.tc, c->d_nbe, xs, b, xo, c->B, flags | (xs ? 0 : RF_ZEROX), c->T.P,
+      bres_tcw_kernel<<<g, kTwT, kTwDyn, st>>>(S.tc, c->d_nbe, xs, b, xo, c->B, flags | (xs ? 0 : RF_ZEROX), c->d_P32,
                                                rr1, c->d_err, ws);
     bump();
     CKL(c);
@@ -1366,7 +1383,7 @@ int btcs(dg_ctx* c, BatchState& S, const unsigned char* xs, const float* b, void
   const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kTsCTA);
   if (g)
     bres_tcs_kernel<<<g, kTcT, kTsDyn, st>>>(S.tc, c->d_nbe, xs, b, nullptr, xo, c->B, flags | (xs ? 0 : RF_ZEROX),
-                                             c->T.P, rr1, c->d_err, ws);
+                                             c->d_P32, rr1, c->d_err, ws);
   bump();
   CKL(c);
   return DG_OK;
@@ -1388,10 +1405,10 @@ int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, co
       if (c->B > 0) {
         if (variant == 2)
           bres_mma_kernel<8><<<(unsigned)c->B, 256, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, b, nullptr, xo, c->B,
-                                                             flags, c->T.P, rr1, ws);
+                                                             flags, c->d_P32, rr1, ws);
         else
           bres_mma_kernel<4><<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, b, nullptr, xo, c->B,
-                                                             flags, c->T.P, rr1, ws);
+                                                             flags, c->d_P32, rr1, ws);
       }
       bump();
       CKL(c);
@@ -1399,7 +1416,7 @@ int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, co
     case 3: {
       const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kBS);
       if (g)
-        bres_mma_tma_kernel<<<g, kBT, kBDyn, st>>>(M.blk16, M.W16, c->d_nbe, xx, b, nullptr, xo, c->B, flags, c->T.P,
+        bres_mma_tma_kernel<<<g, kBT, kBDyn, st>>>(M.blk16, M.W16, c->d_nbe, xx, b, nullptr, xo, c->B, flags, c->d_P32,
                                                    rr1, c->d_err, ws);
       bump();
       CKL(c);
@@ -1410,7 +1427,7 @@ int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, co
       if ((rc = ensure_tc_layout(c, M, S, st))) return rc;
       const unsigned g = (unsigned)std::min<int64_t>(c->B, (int64_t)c->nsm * kTcCTA);
       if (g)
-        bres_tc05_kernel<<<g, kTcT, kTcDyn, st>>>(S.tc, c->d_nbe, xx, b, nullptr, xo, c->B, flags, c->T.P, rr1,
+        bres_tc05_kernel<<<g, kTcT, kTcDyn, st>>>(S.tc, c->d_nbe, xx, b, nullptr, xo, c->B, flags, c->d_P32, rr1,
                                                   c->d_err, ws);
       bump();
       CKL(c);
@@ -1530,7 +1547,7 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
     }
     if ((rc = pc(cur, nullptr, RF_RESTRICT, S.r1, nullptr))) return rc;
   }
-  bgather_kernel<<<(unsigned)c->ncg, kNR, 0, st>>>(S.r1, c->d_gptr, c->d_gent, c->d_wdg, c->d_pos, S.lr[0],
+  bgather_kernel<<<(unsigned)c->ncg, kNR, 0, st>>>(S.r1, c->d_gptr, c->d_gent, c->d_wdg32, c->d_pos, S.lr[0],
                                                    (int)c->ncg);
   bump();
   const int lc = M.dense_l;
@@ -1563,8 +1580,8 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
     }
   }
   if (split) {
-    bprolong_split_kernel<<<(unsigned)c->B, 20 * (kNR / 4), 0, st>>>(scur, S.le[0], c->d_pos, c->d_p1cg, c->d_wdg,
-                                                                   c->T.P, c->B);
+    bprolong_split_kernel<<<(unsigned)c->B, 20 * (kNR / 4), 0, st>>>(scur, S.le[0], c->d_pos, c->d_p1cg, c->d_wdg32,
+                                                                   c->d_P32, c->B);
     bump();
     for (int it = 0; it < nsm; ++it) {
       const bool last_step = it == nsm - 1;
@@ -1576,7 +1593,7 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
     CKL(c);
     return DG_OK;
   }
-  bprolong_kernel<<<(unsigned)c->B, 20 * (kNR / 4), 0, st>>>(cur, S.le[0], c->d_pos, c->d_p1cg, c->d_wdg, c->T.P,
+  bprolong_kernel<<<(unsigned)c->B, 20 * (kNR / 4), 0, st>>>(cur, S.le[0], c->d_pos, c->d_p1cg, c->d_wdg32, c->d_P32,
                                                              c->B);
   bump();
   for (int it = 0; it < nsm; ++it) {

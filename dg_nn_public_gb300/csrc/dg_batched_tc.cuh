@@ -143,7 +143,7 @@ __device__ __forceinline__ uint4 split_hilo4(float4 v) {
 __global__ void __launch_bounds__(kTcT, kTcCTA) bres_tc05_kernel(
     const __nv_bfloat16* __restrict__ tcblk, const int* __restrict__ nbe, const float* __restrict__ x,
     const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out, int64_t B, int flags,
-    const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const float* __restrict__ wsp) {
+    const float* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const float* __restrict__ wsp) {
   constexpr int N = 20, F = 4;
   extern __shared__ __align__(1024) unsigned char tsm[];
   unsigned char* stages = tsm;
@@ -440,8 +440,8 @@ __global__ void to_split_kernel(const float* __restrict__ x, unsigned char* __re
 __global__ void __launch_bounds__(320) bprolong_split_kernel(unsigned char* __restrict__ xs,
                                                              const float* __restrict__ ecg, const int* __restrict__ pos,
                                                              const int* __restrict__ p1cg,
-                                                             const double* __restrict__ wdg,
-                                                             const double* __restrict__ P, int64_t B) {
+                                                             const float* __restrict__ wdg,
+                                                             const float* __restrict__ P, int64_t B) {
   __shared__ int vp[4];
   __shared__ float wc[4];
   __shared__ float Ps[20][4];
@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(320) bprolong_split_kernel(unsigned char* __re
 __global__ void __launch_bounds__(kTcT, kTsCTA) bres_tcs_kernel(
     const __nv_bfloat16* __restrict__ tcblk, const int* __restrict__ nbe, const unsigned char* __restrict__ xs,
     const float* __restrict__ b, float* __restrict__ r, void* __restrict__ x_out, int64_t B, int flags,
-    const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const float* __restrict__ wsp) {
+    const float* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const float* __restrict__ wsp) {
   constexpr int N = 20, F = 4;
   extern __shared__ __align__(1024) unsigned char tsm[];
   unsigned char* stages = tsm;
@@ -740,7 +740,7 @@ __device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.
 
 __global__ void __launch_bounds__(kTwT, 1) bres_tcw_kernel(
     const __nv_bfloat16* __restrict__ tcblk, const int* __restrict__ nbe, const unsigned char* __restrict__ xs,
-    const float* __restrict__ b, void* __restrict__ x_out, int64_t B, int flags, const double* __restrict__ P,
+    const float* __restrict__ b, void* __restrict__ x_out, int64_t B, int flags, const float* __restrict__ P,
     float* __restrict__ r1, int* __restrict__ err, const float* __restrict__ wsp) {
   constexpr int N = 20, F = 4, S = kTwStages, NT = kTwNT;
   extern __shared__ __align__(1024) unsigned char tsm[];

@@ -357,11 +357,12 @@ template <int EPB>
 __global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
     const __nv_bfloat16* __restrict__ blk, const __nv_bfloat16* __restrict__ W, const int* __restrict__ nbe,
     const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out,
-    int64_t B, int flags, const double* __restrict__ P, float* __restrict__ r1, const float* __restrict__ wsp) {
+    int64_t B, int flags, const float* __restrict__ P, float* __restrict__ r1, const float* __restrict__ wsp) {
   const float wscale = wsp ? *wsp : 1.0f;
   constexpr int N = 20, F = 4;
   __shared__ float xs[EPB][F + 1][N];
   __shared__ float rs[EPB][N];
+  __shared__ float Ps[N * F];   // P converted once per CTA, not per use
   __shared__ int nbs[EPB][F];
   const int le = threadIdx.x / N, m = threadIdx.x % N;
   const int64_t e = (int64_t)blockIdx.x * EPB + le;
@@ -369,6 +370,8 @@ __global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
   const bool zerox = flags & RF_ZEROX;
   const bool smooth = flags & RF_SMOOTH;
   if (valid && m < F) nbs[le][m] = nbe[e * F + m];
+  if (flags & RF_RESTRICT)
+    for (int i = threadIdx.x; i < N * F; i += EPB * N) Ps[i] = (float)P[i];
   __syncthreads();
   Row20 q[F + 1];
   Row20 wq = zero_row20();
@@ -407,7 +410,7 @@ __global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
     if (valid && m < NC) {
       float s = 0.0f;
 #pragma unroll
-      for (int n = 0; n < N; ++n) s += (float)P[n * NC + m] * rs[le][n];
+      for (int n = 0; n < N; ++n) s += Ps[n * NC + m] * rs[le][n];
       r1[e * NC + m] = s;
     }
   }
@@ -614,7 +617,7 @@ template <typename MT, int EPB, int S, int MINB, bool WITH_W, bool SF>
 __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     const MT* __restrict__ blk, const MT* __restrict__ W, const int* __restrict__ nbe, const float* __restrict__ x,
     const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out, int64_t B, int flags,
-    const double* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const int* __restrict__ fref5,
+    const float* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const int* __restrict__ fref5,
     const float* __restrict__ wsp) {
   const float wscale = wsp ? *wsp : 1.0f;
   constexpr int N = 20, F = 4;
@@ -832,10 +835,10 @@ int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const floa
   const size_t smem = (size_t)S * TmaGroup<MT, EPB, WITH_W>::StageBytes;
   if (sf)
     return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W, true>, g, EPB * 20, smem, st, blk, W,
-                    (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const double*)c->T.P, r1,
+                    (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const float*)c->d_P32, r1,
                     (int*)c->d_err, (const int*)c->d_fref5, wscale);
   return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W, false>, g, EPB * 20, smem, st, blk, W,
-                  (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const double*)c->T.P, r1,
+                  (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const float*)c->d_P32, r1,
                   (int*)c->d_err, (const int*)nullptr, wscale);
 }
 
@@ -984,7 +987,7 @@ int residual_pc(dg_ctx* c, const float* x, const float* b, float* r, float* x_ou
       unsigned g = nblk(c->B, 8);
       if (g)
         residual_bf16c20_kernel<8><<<g, 8 * 20, 0, st>>>(M.blk16, M.W16, c->d_nbe, x, b, r, x_out, c->B, flags,
-                                                          c->T.P, M.r1, ws);
+                                                          c->d_P32, M.r1, ws);
       bump();
       CKL(c);
       return DG_OK;
@@ -1002,8 +1005,8 @@ int residual_pc(dg_ctx* c, const float* x, const float* b, float* r, float* x_ou
 // programmatic-launch wait.
 __global__ void __launch_bounds__(160) prolong_cg32_kernel(float* __restrict__ x, const float* __restrict__ ecg,
                                                            const int* __restrict__ pos, const int* __restrict__ p1cg,
-                                                           const double* __restrict__ wdg,
-                                                           const double* __restrict__ P, int64_t B) {
+                                                           const float* __restrict__ wdg,
+                                                           const float* __restrict__ P, int64_t B) {
   __shared__ float vc[8][4];
   const int le = threadIdx.x / 20, n = threadIdx.x % 20;
   const int64_t e = (int64_t)blockIdx.x * 8 + le;
@@ -1033,7 +1036,7 @@ __global__ void __launch_bounds__(160) prolong_cg32_kernel(float* __restrict__ x
 // (lev_jacobi_kernel with e_in = NULL: rr = r, e_out = fma(rr / diag, w, 0),
 // rr_out = rr if set), so that sweep needs no launch of its own.
 __global__ void gather_cg32_kernel(const float* __restrict__ r1, const int* __restrict__ gptr,
-                                   const int* __restrict__ gent, const double* __restrict__ wdg,
+                                   const int* __restrict__ gent, const float* __restrict__ wdg,
                                    const int* __restrict__ pos, float* __restrict__ out, int ncg,
                                    const float* __restrict__ diag0, float* __restrict__ e_out,
                                    float* __restrict__ rr_out, float w) {
@@ -1075,7 +1078,7 @@ int launch_transfer32(dg_ctx* c, const float* r, float* cg_out, float* x_add, co
     int rc;
     if (D == 3)
       rc = launch_k(c, prolong_cg32_kernel, nblk(c->B, 8), 160, 0, st, x_add, e_sfc, (const int*)c->d_pos,
-                    (const int*)c->d_p1cg, (const double*)c->d_wdg, (const double*)c->T.P, (int64_t)c->B);
+                    (const int*)c->d_p1cg, (const float*)c->d_wdg32, (const float*)c->d_P32, (int64_t)c->B);
     else
       rc = launch_k(c, prolong_cg_kernel<E::N, E::NC, float>, nblk(c->B * E::N, 256), 256, 0, st, x_add, e_sfc,
                     (const int*)c->d_pos, (const int*)c->d_p1cg, (const double*)c->d_wdg, (const double*)c->T.P,
@@ -1265,7 +1268,7 @@ int vcycle32_cluster(dg_ctx* c, cudaStream_t st) {
   p.r1 = M.r1;
   p.gptr = c->d_gptr;
   p.gent = c->d_gent;
-  p.wdg = c->d_wdg;
+  p.wdg = c->d_wdg32;
   p.pos = c->d_pos;
   p.ncg = (int)c->ncg;
   int rc;
@@ -1300,7 +1303,7 @@ int vcycle32_fused(dg_ctx* c, cudaStream_t st) {
   {
     Lev32& L = M.lev[0];
     if ((rc = launch_k(c, gather_cg32_kernel, nblk(c->ncg, 8), 256, 0, st, (const float*)M.r1,
-                       (const int*)c->d_gptr, (const int*)c->d_gent, (const double*)c->d_wdg, (const int*)c->d_pos,
+                       (const int*)c->d_gptr, (const int*)c->d_gent, (const float*)c->d_wdg32, (const int*)c->d_pos,
                        L.r, (int)c->ncg, (const float*)L.diag, L.e2, npre == 0 ? L.rr : (float*)nullptr, w)))
       return rc;
     std::swap(L.e, L.e2);
@@ -1500,7 +1503,7 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   } else {
     float* cg_dst = M.dense_l > 0 ? M.lev[0].r : M.cg1;
     if ((rc = launch_k(c, gather_cg32_kernel, nblk(c->ncg, 8), 256, 0, st, (const float*)M.r1,
-                       (const int*)c->d_gptr, (const int*)c->d_gent, (const double*)c->d_wdg, (const int*)c->d_pos,
+                       (const int*)c->d_gptr, (const int*)c->d_gent, (const float*)c->d_wdg32, (const int*)c->d_pos,
                        cg_dst, (int)c->ncg, (const float*)nullptr, (float*)nullptr, (float*)nullptr, 0.0f)))
       return rc;
     if ((rc = vcycle32(c, cg_dst, st))) return rc;

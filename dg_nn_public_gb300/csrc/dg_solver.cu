@@ -100,6 +100,10 @@ struct dg_ctx {
   std::vector<std::vector<int64_t>> spidx, colidx;
   int *d_p1cg = nullptr, *d_gptr = nullptr, *d_gent = nullptr, *d_pos = nullptr, *d_whichc = nullptr;
   double* d_wdg = nullptr;
+  // FP32 copies of wdg and of the P1 -> P3 table for the reduced-precision
+  // kernels: an FP64 -> FP32 conversion per use costs FP64-pipe throughput
+  float* d_wdg32 = nullptr;
+  float* d_P32 = nullptr;
   int *d_spidx = nullptr, *d_colidx = nullptr;
   std::vector<int64_t> sp_off;
   double* d_rar = nullptr;
@@ -1014,6 +1018,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     c->T.drst = p;
     if ((rc = upload(c.get(), &p, m->p1_to_p3, (size_t)N * (D + 1)))) return rc;
     c->T.P = p;
+    std::vector<float> p32(m->p1_to_p3, m->p1_to_p3 + (size_t)N * (D + 1));
+    if ((rc = upload_vec(c.get(), &c->d_P32, p32))) return rc;
     std::vector<int> al(D * SG);
     for (int k = 0; k < D * SG; ++k) {
       if (m->gi_align[k] < 0 || m->gi_align[k] >= SG) return fail(c.get(), DG_ERR_ARG, "gi_align out of range");
@@ -1120,6 +1126,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     for (int64_t v : c->p1cg) cnt[v] += 1.0;
     for (size_t k = 0; k < c->p1cg.size(); ++k) wdg[k] = 1.0 / cnt[c->p1cg[k]];
     if ((rc = upload_vec(c.get(), &c->d_wdg, wdg))) return rc;
+    std::vector<float> wdg32(wdg.begin(), wdg.end());
+    if ((rc = upload_vec(c.get(), &c->d_wdg32, wdg32))) return rc;
     std::vector<int> gptr(c->ncg + 1, 0), gent(c->p1cg.size());
     for (int64_t v : c->p1cg) gptr[v + 1]++;
     for (int64_t i = 0; i < c->ncg; ++i) gptr[i + 1] += gptr[i];

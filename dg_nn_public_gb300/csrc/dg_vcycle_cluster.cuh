@@ -70,7 +70,7 @@ struct VcParams {
   const float* r1;
   const int* gptr;
   const int* gent;
-  const double* wdg;
+  const float* wdg;
   const int* pos;
   int ncg;
 };
