@@ -1178,14 +1178,19 @@ __global__ void bscale_kernel(const float* __restrict__ z, const float* __restri
   reinterpret_cast<float4*>(v)[t] = a;
 }
 
-// d[row][q] += sum_j Z_j[row][q] y[j][q]
-__global__ void bcombine_kernel(const float* __restrict__ Z, int64_t ld, int k, const double* __restrict__ y,
-                                float* __restrict__ d, int64_t total) {
+// d[row][q] += sum_j Z_j[row][q] y[j][q]; y (k <= 32 rows of kNR) is
+// converted to FP32 once per CTA into shared memory, not once per entry
+__global__ void __launch_bounds__(256) bcombine_kernel(const float* __restrict__ Z, int64_t ld, int k,
+                                                       const double* __restrict__ y, float* __restrict__ d,
+                                                       int64_t total) {
+  __shared__ float ys[32 * kNR];
+  for (int o = threadIdx.x; o < k * kNR; o += blockDim.x) ys[o] = (float)y[o];
+  __syncthreads();
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total) return;
   const int q = (int)(t % kNR);
   float s = d[t];
-  for (int j = 0; j < k; ++j) s += Z[(size_t)j * ld + t] * (float)y[j * kNR + q];
+  for (int j = 0; j < k; ++j) s += Z[(size_t)j * ld + t] * ys[j * kNR + q];
   d[t] = s;
 }
 

@@ -449,6 +449,21 @@ __global__ void combine_kernel(const VT* __restrict__ V, int64_t ld, int nv,
   x[k] = (XT)((double)x[k] + alpha * s);
 }
 
+// the same for FP32 vectors in FP32 arithmetic (the inner solve's
+// correction): y converted once per CTA, one FMA chain per entry (FP64
+// arithmetic per entry would run at the FP64 pipe's rate)
+__global__ void combine32_kernel(const float* __restrict__ V, int64_t ld, int nv, const double* __restrict__ y,
+                                 float* __restrict__ x, int64_t n) {
+  __shared__ float ys[256];   // nv <= 256 (the restart length limit of the mixed solve)
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) ys[i] = (float)y[i];
+  __syncthreads();
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  float s = x[k];
+  for (int i = 0; i < nv; ++i) s = fmaf(V[i * ld + k], ys[i], s);
+  x[k] = s;
+}
+
 }  // namespace dg
 
 namespace dg {

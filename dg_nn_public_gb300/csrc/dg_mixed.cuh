@@ -2558,7 +2558,7 @@ extern "C" int dg_solve_mixed(dg_ctx* c, double* x, const double* b, double tol,
         break;
       }
       CK(c, cudaMemcpyAsync(c->d_y, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, st));
-      combine_kernel<float, float><<<nblk(n, 256), 256, 0, st>>>(M.Z, n, k, c->d_y, d32, n, 1.0);
+      combine32_kernel<<<nblk(n, 256), 256, 0, st>>>(M.Z, n, k, c->d_y, d32, n);
       bump();
       CKL(c);
       inner_done = conv;
