@@ -154,18 +154,14 @@ int launch_k2(dg_ctx* c, void (*kern)(KArgs...), dim3 grid, unsigned block, size
 // e = Ainv r for a small dense level matrix: one warp per row.  The row of
 // the fixed inverse is read into registers (float4, up to 20 per lane, i.e.
 // n <= 2560 without a second pass) before the programmatic-launch wait, so
-// the 21.5 MB read overlaps the previous kernel; r is read after the wait.
-// With rr_src, r is formed on the fly as the pair sums of the finer level's
-// residual (r[k] = rr_src[2k] + rr_src[2k+1], zero pad at n_src: the SFC
-// restriction, lev_restrict_kernel), so the restriction needs no launch.
-__device__ __forceinline__ float dense_r(const float* __restrict__ r, const float* __restrict__ rr, int n_src,
-                                         int k) {
-  if (!rr) return r[k];
-  return rr[2 * k] + (2 * k + 1 < n_src ? rr[2 * k + 1] : 0.0f);
-}
-
+// the 21.5 MB read overlaps the previous kernel; after the wait the CTA
+// stages r in shared memory (n floats of dynamic shared memory).  With
+// rr_src, r is formed there as the pair sums of the finer level's residual
+// (r[k] = rr_src[2k] + rr_src[2k+1], zero pad at n_src: the SFC restriction,
+// lev_restrict_kernel), so the restriction needs no launch of its own.
 __global__ void dense_matvec_kernel(const float* __restrict__ Ainv, const float* __restrict__ r,
                                     float* __restrict__ e, int n, const float* __restrict__ rr_src, int n_src) {
+  extern __shared__ __align__(16) float dense_rs[];
   constexpr int PRE = 20;
   const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
@@ -191,36 +187,44 @@ __global__ void dense_matvec_kernel(const float* __restrict__ Ainv, const float*
     }
   }
   pdl_wait_then_trigger();
+  for (int k = threadIdx.x; k < n; k += blockDim.x)
+    dense_rs[k] = rr_src ? rr_src[2 * k] + (2 * k + 1 < n_src ? rr_src[2 * k + 1] : 0.0f) : r[k];
+  __syncthreads();
   if (row >= n) return;
+  const float* rs = dense_rs;
   float s = 0.0f;
   if (vec) {
+    const float4* rs4 = reinterpret_cast<const float4*>(rs);
 #pragma unroll
     for (int q = 0; q < PRE; ++q) {
       const int k4 = lane + 32 * q;
       if (k4 < n4) {
-        s = __fmaf_rn(a[q].x, dense_r(r, rr_src, n_src, 4 * k4), s);
-        s = __fmaf_rn(a[q].y, dense_r(r, rr_src, n_src, 4 * k4 + 1), s);
-        s = __fmaf_rn(a[q].z, dense_r(r, rr_src, n_src, 4 * k4 + 2), s);
-        s = __fmaf_rn(a[q].w, dense_r(r, rr_src, n_src, 4 * k4 + 3), s);
+        const float4 rv = rs4[k4];
+        float t = a[q].x * rv.x;
+        t = __fmaf_rn(a[q].y, rv.y, t);
+        t = __fmaf_rn(a[q].z, rv.z, t);
+        t = __fmaf_rn(a[q].w, rv.w, t);
+        s += t;
       }
     }
     for (int k4 = lane + 32 * PRE; k4 < n4; k4 += 32) {
-      const float4 av = reinterpret_cast<const float4*>(ar)[k4];
-      s = __fmaf_rn(av.x, dense_r(r, rr_src, n_src, 4 * k4), s);
-      s = __fmaf_rn(av.y, dense_r(r, rr_src, n_src, 4 * k4 + 1), s);
-      s = __fmaf_rn(av.z, dense_r(r, rr_src, n_src, 4 * k4 + 2), s);
-      s = __fmaf_rn(av.w, dense_r(r, rr_src, n_src, 4 * k4 + 3), s);
+      const float4 av = reinterpret_cast<const float4*>(ar)[k4], rv = rs4[k4];
+      float t = av.x * rv.x;
+      t = __fmaf_rn(av.y, rv.y, t);
+      t = __fmaf_rn(av.z, rv.z, t);
+      t = __fmaf_rn(av.w, rv.w, t);
+      s += t;
     }
   } else {
 #pragma unroll
     for (int q = 0; q < PRE; ++q) {
       const int k = lane + 128 * q;
-      if (k < n) s = __fmaf_rn(a[q].x, dense_r(r, rr_src, n_src, k), s);
-      if (k + 32 < n) s = __fmaf_rn(a[q].y, dense_r(r, rr_src, n_src, k + 32), s);
-      if (k + 64 < n) s = __fmaf_rn(a[q].z, dense_r(r, rr_src, n_src, k + 64), s);
-      if (k + 96 < n) s = __fmaf_rn(a[q].w, dense_r(r, rr_src, n_src, k + 96), s);
+      if (k < n) s = __fmaf_rn(a[q].x, rs[k], s);
+      if (k + 32 < n) s = __fmaf_rn(a[q].y, rs[k + 32], s);
+      if (k + 64 < n) s = __fmaf_rn(a[q].z, rs[k + 64], s);
+      if (k + 96 < n) s = __fmaf_rn(a[q].w, rs[k + 96], s);
     }
-    for (int k = lane + 128 * PRE; k < n; k += 32) s = __fmaf_rn(ar[k], dense_r(r, rr_src, n_src, k), s);
+    for (int k = lane + 128 * PRE; k < n; k += 32) s = __fmaf_rn(ar[k], rs[k], s);
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -1275,7 +1279,7 @@ int vcycle32_cluster(dg_ctx* c, cudaStream_t st) {
   if ((rc = launch_vc(c, vcycle_down_kernel, p, st))) return rc;
   {
     Lev32& L = M.lev[lc];
-    if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, 0, st, (const float*)M.dense_inv,
+    if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, sizeof(float) * L.n, st, (const float*)M.dense_inv,
                        (const float*)L.r, L.e, L.n, (const float*)nullptr, 0)))
       return rc;
   }
@@ -1330,7 +1334,7 @@ int vcycle32_fused(dg_ctx* c, cudaStream_t st) {
   {
     Lev32& L = M.lev[lc];
     const Lev32& P = M.lev[lc - 1];
-    if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, 0, st, (const float*)M.dense_inv,
+    if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, sizeof(float) * L.n, st, (const float*)M.dense_inv,
                        (const float*)nullptr, L.e, L.n, (const float*)P.rr, P.n)))
       return rc;
   }
@@ -1403,7 +1407,7 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
     }
     {
       Lev32& L = M.lev[lc];
-      if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, 0, st, (const float*)M.dense_inv,
+      if ((rc = launch_k(c, dense_matvec_kernel, nblk(L.n, 8), 256, sizeof(float) * L.n, st, (const float*)M.dense_inv,
                          (const float*)L.r, L.e, L.n, (const float*)nullptr, 0)))
         return rc;
     }
