@@ -556,6 +556,60 @@ __global__ void __launch_bounds__(256) block_inverse_kernel(const double* __rest
   for (int n = 0; n < N; ++n) Wo[n * N + m] = w * inv[n];
 }
 
+// The same damped block inverse in FP32 (the mixed preconditioner stores
+// its smoother matrices in FP32 / BF16): the FP64 block is read and rounded
+// once, the elimination runs in FP32 FMAs.  W (FP32) in the same layout.
+template <int N, int F>
+__global__ void __launch_bounds__(256) block_inverse32_kernel(const double* __restrict__ blk, float* __restrict__ W,
+                                                              int64_t B, float w, int* err) {
+  static_assert(N <= 32, "one lane per row");
+  constexpr int WPB = 8;
+  const int lane = threadIdx.x & 31;
+  const int64_t e = (int64_t)blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (e >= B) return;   // whole warp
+  const int m = lane < N ? lane : N - 1;   // lanes >= N repeat the last row, write nothing
+  const double* A = blk + (size_t)e * (F + 1) * N * N;   // A(m, n) at [n * N + m]
+  float a[N], inv[N];
+#pragma unroll
+  for (int n = 0; n < N; ++n) {
+    a[n] = (float)A[n * N + m];
+    inv[n] = (n == m) ? 1.0f : 0.0f;
+  }
+  bool bad = false;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    const float piv = __shfl_sync(0xffffffffu, a[k], k);
+    if (!(piv > 0.0f)) {   // uniform: every lane holds the same pivot
+      bad = true;
+      break;
+    }
+    const float rp = 1.0f / piv;
+    const float fm = a[k];   // this row's entry in the pivot column
+#pragma unroll
+    for (int n = 0; n < N; ++n) {
+      const float pa = __shfl_sync(0xffffffffu, a[n], k) * rp;
+      const float pi = __shfl_sync(0xffffffffu, inv[n], k) * rp;
+      if (m == k) {
+        a[n] = pa;
+        inv[n] = pi;
+      } else {
+        a[n] = fmaf(-fm, pa, a[n]);
+        inv[n] = fmaf(-fm, pi, inv[n]);
+      }
+    }
+  }
+  if (lane >= N) return;
+  float* Wo = W + (size_t)e * N * N;
+  if (bad) {
+    if (lane == 0) atomicExch(err, 2);
+#pragma unroll
+    for (int n = 0; n < N; ++n) Wo[n * N + m] = (m == n) ? w / (float)A[m * N + m] : 0.0f;
+    return;
+  }
+#pragma unroll
+  for (int n = 0; n < N; ++n) Wo[n * N + m] = w * inv[n];
+}
+
 // ---------------------------------------------------------------------------
 // Residual / smoother: EPB elements per CTA, one thread per (element, row).
 //   res = b - A x            (b = 0 when null; x = 0 when ZEROX)

@@ -305,8 +305,9 @@ __host__ __device__ __forceinline__ int chunk20_index(int m, int n) {
   return n < 8 ? m * 8 + n : (n < 16 ? kC20Off1 + m * 8 + (n - 8) : kC20Off2 + m * 4 + (n - 16));
 }
 
-// a: nblock column-major FP64 blocks [blk][n][m] -> chunked BF16 blocks
-__global__ void convert_f64_bf16_chunk20_kernel(const double* __restrict__ a, __nv_bfloat16* __restrict__ b,
+// a: nblock column-major FP64 (or FP32) blocks [blk][n][m] -> chunked BF16 blocks
+template <typename ST>
+__global__ void convert_f64_bf16_chunk20_kernel(const ST* __restrict__ a, __nv_bfloat16* __restrict__ b,
                                                 int64_t nblock) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nblock * 400) return;
@@ -431,7 +432,8 @@ __global__ void __launch_bounds__(EPB * 20) residual_bf16c20_kernel(
 // block is five 16-byte loads (chunk c at byte 320 c + 16 m).
 __host__ __device__ __forceinline__ int chunk20f_index(int m, int n) { return (n >> 2) * 80 + m * 4 + (n & 3); }
 
-__global__ void convert_f64_f32_chunk20_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t nblock) {
+template <typename ST>
+__global__ void convert_f64_f32_chunk20_kernel(const ST* __restrict__ a, float* __restrict__ b, int64_t nblock) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nblock * 400) return;
   const int64_t blk = k / 400;
@@ -896,6 +898,134 @@ __global__ void gj_update_kernel(double* __restrict__ G, int n, int k, const dou
   if (j >= 2 * n) return;
   double* row = G + (size_t)i * 2 * n;
   row[j] = (i == k) ? prow[j] : row[j] - fcol[i] * prow[j];
+}
+
+// ---------------------------------------------------------------------------
+// Blocked Gauss-Jordan inverse of the dense coarse level in FP32 (the
+// inverse is applied in FP32; the level matrix is symmetric positive
+// definite, so no pivoting).  G = [A | I] is n x 2n row-major.  Block step
+// over the rows and columns P = [k0, k0 + b):
+//   C = G[:, P] (copy; D = C[P, :]), Dinv = D^-1 (one CTA),
+//   G[P, :] = Dinv G[P, :],  G[i, :] -= C[i, :] G[P, :] for i not in P.
+// Columns left of k0 are already unit columns and the right half is still
+// zero beyond n + k0 + b in the rows of P, so a step touches the columns
+// [k0, n + k0 + b) only: n^3 FMAs in all, in n / b steps of four launches
+// instead of 2 n launches of the one-pivot form.
+constexpr int kGjB = 32;
+
+__global__ void gjb_copy_kernel(const float* __restrict__ G, int n, int k0, int b, float* __restrict__ C) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * b) return;
+  const int i = t / b, q = t % b;
+  C[t] = G[(size_t)i * 2 * n + k0 + q];
+}
+
+// Dinv = D^-1 for D = C[k0 .. k0+b, :] (b <= kGjB), one CTA of 256 threads
+__global__ void __launch_bounds__(256) gjb_dinv_kernel(const float* __restrict__ C, int k0, int b,
+                                                       float* __restrict__ Dinv, int* __restrict__ err) {
+  __shared__ float S[kGjB][2 * kGjB + 1];
+  __shared__ float f[kGjB];
+  for (int t = threadIdx.x; t < b * 2 * b; t += blockDim.x) {
+    const int r = t / (2 * b), j = t % (2 * b);
+    S[r][j] = j < b ? C[(size_t)(k0 + r) * b + j] : (j - b == r ? 1.0f : 0.0f);
+  }
+  __syncthreads();
+  for (int p = 0; p < b; ++p) {
+    const float piv = S[p][p];
+    if (!(piv > 0.0f)) {   // uniform
+      if (threadIdx.x == 0) atomicExch(err, 4);
+      return;
+    }
+    if (threadIdx.x < b) f[threadIdx.x] = S[threadIdx.x][p];
+    __syncthreads();
+    const float rp = 1.0f / piv;
+    for (int j = threadIdx.x; j < 2 * b; j += blockDim.x) S[p][j] *= rp;
+    __syncthreads();
+    for (int t = threadIdx.x; t < b * 2 * b; t += blockDim.x) {
+      const int r = t / (2 * b), j = t % (2 * b);
+      if (r != p) S[r][j] = fmaf(-f[r], S[p][j], S[r][j]);
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < b * b; t += blockDim.x) Dinv[t] = S[t / b][b + t % b];
+}
+
+// G[P, j] = sum_q Dinv[r][q] G[k0 + q][j] for the columns j in [k0, n + k0 + b);
+// one thread per column (reads its b entries, then writes them)
+__global__ void __launch_bounds__(128) gjb_rows_kernel(float* __restrict__ G, int n, int k0, int b,
+                                                       const float* __restrict__ Dinv) {
+  __shared__ float Ds[kGjB * kGjB];
+  for (int t = threadIdx.x; t < b * b; t += blockDim.x) Ds[t] = Dinv[t];
+  __syncthreads();
+  const int j = k0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= min(2 * n, n + k0 + b)) return;
+  float g[kGjB];
+#pragma unroll
+  for (int q = 0; q < kGjB; ++q) g[q] = q < b ? G[(size_t)(k0 + q) * 2 * n + j] : 0.0f;
+  for (int r = 0; r < b; ++r) {
+    float s = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kGjB; ++q) s = fmaf(Ds[r * b + (q < b ? q : 0)], g[q], s);
+    G[(size_t)(k0 + r) * 2 * n + j] = s;
+  }
+}
+
+// G[i, j] -= sum_q C[i][q] G[k0 + q][j] for rows i not in P and columns j in
+// [k0 + b, n + k0 + b); G[i, P] = 0.  64 x 64 tiles, 256 threads of 4 x 4.
+__global__ void __launch_bounds__(256) gjb_update_kernel(float* __restrict__ G, int n, int k0, int b,
+                                                         const float* __restrict__ C) {
+  __shared__ float Cs[64][kGjB + 1];
+  __shared__ __align__(16) float Rs[kGjB][64];
+  const int i0 = blockIdx.y * 64, j0 = k0 + b + blockIdx.x * 64;
+  const int jend = min(2 * n, n + k0 + b);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  for (int t = threadIdx.x; t < 64 * kGjB; t += 256) {
+    const int r = t / kGjB, q = t % kGjB;
+    Cs[r][q] = (i0 + r < n && q < b) ? C[(size_t)(i0 + r) * b + q] : 0.0f;
+  }
+  for (int t = threadIdx.x; t < kGjB * 64; t += 256) {
+    const int q = t / 64, c = t % 64;
+    Rs[q][c] = (q < b && j0 + c < jend) ? G[(size_t)(k0 + q) * 2 * n + j0 + c] : 0.0f;
+  }
+  __syncthreads();
+  float acc[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.0f;
+#pragma unroll 8
+  for (int q = 0; q < kGjB; ++q) {
+    const float4 rv = *reinterpret_cast<const float4*>(&Rs[q][4 * tx]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float cv = Cs[4 * ty + u][q];
+      acc[u][0] = fmaf(cv, rv.x, acc[u][0]);
+      acc[u][1] = fmaf(cv, rv.y, acc[u][1]);
+      acc[u][2] = fmaf(cv, rv.z, acc[u][2]);
+      acc[u][3] = fmaf(cv, rv.w, acc[u][3]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int i = i0 + 4 * ty + u;
+    if (i >= n || (i >= k0 && i < k0 + b)) continue;
+    float* row = G + (size_t)i * 2 * n;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int j = j0 + 4 * tx + v;
+      if (j < jend) row[j] -= acc[u][v];
+    }
+    if (blockIdx.x == 0)   // the block's own columns become zero
+      for (int q = tx; q < b; q += 16) row[k0 + q] = 0.0f;
+  }
+}
+
+// inv (n x n FP32) = right half of the FP32 G
+__global__ void gjb_extract_kernel(const float* __restrict__ G, int n, float* __restrict__ inv) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n * n) return;
+  const int64_t i = t / n, j = t % n;
+  inv[t] = G[i * 2 * n + n + j];
 }
 
 // inv (n x n FP32) = right half of G
@@ -1535,12 +1665,14 @@ __global__ void bnonzero_kernel(const double* __restrict__ x, int64_t n, int* __
   if (nz && threadIdx.x == 0) atomicOr(flag + q, 1);
 }
 
-__global__ void convert_f64_f32_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+template <typename ST>
+__global__ void convert_f64_f32_kernel(const ST* __restrict__ a, float* __restrict__ b, int64_t n) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) b[k] = (float)a[k];
 }
 
-__global__ void convert_f64_bf16_kernel(const double* __restrict__ a, __nv_bfloat16* __restrict__ b, int64_t n) {
+template <typename ST>
+__global__ void convert_f64_bf16_kernel(const ST* __restrict__ a, __nv_bfloat16* __restrict__ b, int64_t n) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) b[k] = __float2bfloat16_rn((float)a[k]);
 }
@@ -1685,34 +1817,45 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
   vt("operator copies");
   // smoother matrices of the mixed preconditioner
   const double* Wsrc = c->d_W;
+  const float* Wsrc32 = nullptr;
   double* Winv = nullptr;
   if (c->mixed_smoother == 1) {
     // scratch kept with the context: a cudaFree here would wait for every
     // stream of the device (other contexts' solves on a serving GPU)
     if (!M.winv && (rc = dalloc(c, &M.winv, nw))) return rc;
     Winv = M.winv;
+    // inverted in FP32: the copies it feeds are FP32 / BF16, and the FP64
+    // inverse ran at the FP64 pipe's rate (21 ms at 280k tets against 1 ms)
+    float* W32 = reinterpret_cast<float*>(M.winv);
     CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
     if (c->D == 3)
-      block_inverse_kernel<20, 4><<<nblk(c->B, 8), 256, 0, st>>>(c->d_blk, Winv, c->B, c->mixed_smooth_w, c->d_err);
+      block_inverse32_kernel<20, 4><<<nblk(c->B, 8), 256, 0, st>>>(c->d_blk, W32, c->B, (float)c->mixed_smooth_w,
+                                                                   c->d_err);
     else
-      block_inverse_kernel<10, 3><<<nblk(c->B, 8), 256, 0, st>>>(c->d_blk, Winv, c->B, c->mixed_smooth_w, c->d_err);
+      block_inverse32_kernel<10, 3><<<nblk(c->B, 8), 256, 0, st>>>(c->d_blk, W32, c->B, (float)c->mixed_smooth_w,
+                                                                   c->d_err);
     bump();
-    Wsrc = Winv;
+    Wsrc32 = W32;
     vt("block inverses");
   }
-  if (c->D == 3 && c->f32_tma)
-    convert_f64_f32_chunk20_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W, (int64_t)c->B);
-  else
-    convert_f64_f32_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W, (int64_t)nw);
-  bump();
-  if (c->precond_bf16) {
-    if (!M.W16 && (rc = dalloc(c, &M.W16, nw))) return rc;
-    if (c->D == 3)
-      convert_f64_bf16_chunk20_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W16, (int64_t)c->B);
+  auto copies = [&](auto src) -> int {
+    if (c->D == 3 && c->f32_tma)
+      convert_f64_f32_chunk20_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(src, M.W, (int64_t)c->B);
     else
-      convert_f64_bf16_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(Wsrc, M.W16, (int64_t)nw);
+      convert_f64_f32_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(src, M.W, (int64_t)nw);
     bump();
-  }
+    if (c->precond_bf16) {
+      int r2;
+      if (!M.W16 && (r2 = dalloc(c, &M.W16, nw))) return r2;
+      if (c->D == 3)
+        convert_f64_bf16_chunk20_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(src, M.W16, (int64_t)c->B);
+      else
+        convert_f64_bf16_kernel<<<nblk((int64_t)nw, 256), 256, 0, st>>>(src, M.W16, (int64_t)nw);
+      bump();
+    }
+    return DG_OK;
+  };
+  if ((rc = Wsrc32 ? copies(Wsrc32) : copies(Wsrc))) return rc;
   if (Winv) {
     int herr = 0;
     CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1766,28 +1909,51 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
         for (int64_t k = h.row_ptr[r0 + i]; k < h.row_ptr[r0 + i + 1]; ++k) Gh[(size_t)i * 2 * n + h.col[k]] += h.val[k];
         Gh[(size_t)i * 2 * n + n + i] = 1.0;
       }
-      // augmented matrix and pivot row / column, kept with the context
-      const size_t gneed = Gh.size() + 3 * (size_t)n;
+      // augmented matrix and pivot row / column (FP64 form) or the FP32
+      // augmented matrix, panel copy and block inverse, kept with the context
+      const size_t gneed = std::max(Gh.size() + 3 * (size_t)n,
+                                    (Gh.size() + (size_t)kGjB * n + (size_t)kGjB * kGjB + 1) / 2);
       if (M.gj_cap < gneed) {
         if ((rc = dalloc(c, &M.gj, gneed))) return rc;
         M.gj_cap = gneed;
       }
-      double* G = M.gj;
-      double* fcol = G + Gh.size();
-      double* prow = fcol + n;
-      CK(c, cudaMemcpyAsync(G, Gh.data(), sizeof(double) * Gh.size(), cudaMemcpyHostToDevice, st));
-      CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
-      for (int k = 0; k < n; ++k) {
-        gj_prep_kernel<<<nblk(2 * n - k > n ? 2 * n - k : n, 256), 256, 0, st>>>(G, n, k, fcol, prow, c->d_err);
-        gj_update_kernel<<<dim3(nblk(2 * n - k, 256), n), 256, 0, st>>>(G, n, k, fcol, prow);
-      }
-      bump(2 * (long long)n);
       if (!M.dense_inv || c->dense_n != n) {
         if ((rc = dalloc(c, &M.dense_inv, (size_t)n * n))) return rc;
         c->dense_n = n;
       }
-      gj_extract_kernel<<<nblk((int64_t)n * n, 256), 256, 0, st>>>(G, n, M.dense_inv);
-      bump();
+      CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
+      if (c->dense_fp64) {
+        // one pivot per launch pair, FP64 (DG_DENSE_FP64=1)
+        double* G = M.gj;
+        double* fcol = G + Gh.size();
+        double* prow = fcol + n;
+        CK(c, cudaMemcpyAsync(G, Gh.data(), sizeof(double) * Gh.size(), cudaMemcpyHostToDevice, st));
+        for (int k = 0; k < n; ++k) {
+          gj_prep_kernel<<<nblk(2 * n - k > n ? 2 * n - k : n, 256), 256, 0, st>>>(G, n, k, fcol, prow, c->d_err);
+          gj_update_kernel<<<dim3(nblk(2 * n - k, 256), n), 256, 0, st>>>(G, n, k, fcol, prow);
+        }
+        bump(2 * (long long)n);
+        gj_extract_kernel<<<nblk((int64_t)n * n, 256), 256, 0, st>>>(G, n, M.dense_inv);
+        bump();
+      } else {
+        // blocked FP32 form in the same scratch: G (n x 2n), C (n x kGjB), Dinv
+        float* G = reinterpret_cast<float*>(M.gj);
+        float* C = G + Gh.size();
+        float* Dinv = C + (size_t)n * kGjB;
+        std::vector<float> Gf(Gh.begin(), Gh.end());
+        CK(c, cudaMemcpyAsync(G, Gf.data(), sizeof(float) * Gf.size(), cudaMemcpyHostToDevice, st));
+        for (int k0 = 0; k0 < n; k0 += kGjB) {
+          const int b = std::min(kGjB, n - k0);
+          gjb_copy_kernel<<<nblk((int64_t)n * b, 256), 256, 0, st>>>(G, n, k0, b, C);
+          gjb_dinv_kernel<<<1, 256, 0, st>>>(C, k0, b, Dinv, c->d_err);
+          gjb_rows_kernel<<<nblk(n + b, 128), 128, 0, st>>>(G, n, k0, b, Dinv);
+          gjb_update_kernel<<<dim3((unsigned)((n + 63) / 64), (unsigned)((n + 63) / 64)), 256, 0, st>>>(G, n, k0, b,
+                                                                                                     C);
+          bump(4);
+        }
+        gjb_extract_kernel<<<nblk((int64_t)n * n, 256), 256, 0, st>>>(G, n, M.dense_inv);
+        bump();
+      }
       int herr = 0;
       CK(c, cudaMemcpyAsync(&herr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
       CK(c, cudaStreamSynchronize(st));

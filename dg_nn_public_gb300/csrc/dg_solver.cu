@@ -152,6 +152,9 @@ struct dg_ctx {
   // schedules, 0 = the launch chain (default: measured faster at c2),
   // 8 / 16 = that cluster size (dg_set_vcycle_cluster, DG_MIXED_VC_CLUSTER)
   int vc32_cluster = 0;
+  // dense coarse inverse of the mixed preconditioner by the one-pivot FP64
+  // Gauss-Jordan (DG_DENSE_FP64=1) instead of the blocked FP32 form
+  bool dense_fp64 = false;
   // the launch chain of that V-cycle without launches of its own for the
   // transfers between levels (vcycle32_fused; DG_MIXED_VC_FUSED=0: off)
   bool vc32_fused = true;
@@ -904,6 +907,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (msw && msw[0]) c->mixed_sweeps = std::atoi(msw);
     const char* mlw = std::getenv("DG_MIXED_LEV_SWEEPS");
     if (mlw && mlw[0]) c->mixed_lev_sweeps = std::atoi(mlw);
+    const char* dfp = std::getenv("DG_DENSE_FP64");
+    if (dfp && dfp[0]) c->dense_fp64 = dfp[0] != '0';
     const char* vcc = std::getenv("DG_MIXED_VC_CLUSTER");
     if (vcc && vcc[0]) c->vc32_cluster = std::atoi(vcc);
     const char* vcf = std::getenv("DG_MIXED_VC_FUSED");
