@@ -1721,18 +1721,36 @@ int set_smoother_schedule(dg_ctx* c, cudaStream_t st) {
   if ((rc = norm32(c, v, c->d_scal, st))) return rc;
   scale_kernel<float><<<nblk(n, 256), 256, 0, st>>>(v, c->d_scal, v, n);
   bump();
+  // the estimates of a run of steps stay on the device (d_scal[1 + it]) and
+  // are read once per run, not once per step; the stop is the first step
+  // it >= 8 whose estimate moved by at most 1e-3 (later steps of the run
+  // change nothing that is used)
+  constexpr int kMaxIts = 40;
   double lam = 0.0, prev = -1.0;
-  for (int it = 0; it < 40; ++it) {
-    if ((rc = residual_pc(c, v, zb, nullptr, u, RF_SMOOTH, st))) return rc;   // u = v - W A v
-    sub_f32_kernel<<<nblk(n, 256), 256, 0, st>>>(v, u, v, n);                 // v <- W A v
-    bump();
-    if ((rc = norm32(c, v, c->d_scal, st))) return rc;
-    if ((rc = read_scalar(c, c->d_scal, &lam, st))) return rc;
-    if (!(lam > 0.0) || !std::isfinite(lam)) return DG_OK;
-    scale_kernel<float><<<nblk(n, 256), 256, 0, st>>>(v, c->d_scal, v, n);
-    bump();
-    if (it >= 8 && std::fabs(lam - prev) <= 1e-3 * lam) break;
-    prev = lam;
+  std::vector<double> lams(kMaxIts, 0.0);
+  bool stop = false;
+  for (int it0 = 0; it0 < kMaxIts && !stop;) {
+    const int run = it0 == 0 ? 9 : std::min(8, kMaxIts - it0);
+    for (int it = it0; it < it0 + run; ++it) {
+      if ((rc = residual_pc(c, v, zb, nullptr, u, RF_SMOOTH, st))) return rc;   // u = v - W A v
+      sub_f32_kernel<<<nblk(n, 256), 256, 0, st>>>(v, u, v, n);                 // v <- W A v
+      bump();
+      if ((rc = norm32(c, v, c->d_scal + 1 + it, st))) return rc;
+      scale_kernel<float><<<nblk(n, 256), 256, 0, st>>>(v, c->d_scal + 1 + it, v, n);
+      bump();
+    }
+    CK(c, cudaMemcpyAsync(lams.data() + it0, c->d_scal + 1 + it0, sizeof(double) * run, cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    for (int it = it0; it < it0 + run; ++it) {
+      lam = lams[it];
+      if (!(lam > 0.0) || !std::isfinite(lam)) return DG_OK;
+      if (it >= 8 && std::fabs(lam - prev) <= 1e-3 * lam) {
+        stop = true;
+        break;
+      }
+      prev = lam;
+    }
+    it0 += run;
   }
   CKL(c);
   const double lmax = lam / c->mixed_smooth_w;   // of A_ee^-1 A

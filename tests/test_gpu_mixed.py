@@ -225,3 +225,35 @@ def test_cluster_vcycle_matches_launch_chain(kind, n, fits):
     assert res[0][:2] == res[-1][:2]
     assert torch.equal(res[0][2], res[-1][2])
     s.close()
+
+
+@pytest.mark.parametrize("kind,n", [("tet", 14), ("tet", 20), ("tri", 64)])
+def test_blocked_fp32_dense_inverse(kind, n, monkeypatch):
+    """The dense coarse inverse of the mixed preconditioner by the blocked
+    FP32 Gauss-Jordan against the one-pivot FP64 form (DG_DENSE_FP64=1):
+    the FP32 preconditioner outputs agree to 1e-4 of their max entry and
+    the mixed solves take the same inner iterations to the same tolerance."""
+    outs, its = {}, {}
+    for fp64 in ("0", "1"):
+        monkeypatch.setenv("DG_DENSE_FP64", fp64)
+        m = mesh.build_mesh(kind, n, seed=1)
+        s = DGSolver(m, sfc.hilbert_sfc_order(m.cg_coords), SolverConfig(pre_smooth_its=2, post_smooth_its=2),
+                     element.p3_element(m.ndim))
+        s.set_kappa(np.exp(0.5 * np.random.default_rng(5).standard_normal(m.nele)))
+        s.build_operator()
+        g = torch.Generator(device="cuda:0").manual_seed(3)
+        b = torch.randn(s.nonods, dtype=torch.float32, device="cuda:0", generator=g)
+        outs[fp64] = s.precond_f32(b).clone()
+        X = m.x_ref_in
+        u = np.prod([np.sin(np.pi * X[:, k]) for k in range(m.ndim)], axis=0).ravel()
+        bb = s.rhs(torch.tensor(m.ndim * np.pi ** 2 * u, device="cuda:0"))
+        tol = 1e-10 * float(torch.linalg.norm(bb))
+        x = torch.zeros_like(bb)
+        it, r, outer = s.solve_mixed(x, bb, tol)
+        assert r <= tol
+        its[fp64] = it
+        s.close()
+    err = float(torch.abs(outs["0"] - outs["1"]).max() / torch.abs(outs["1"]).max())
+    print("%s n=%d: blocked FP32 vs FP64 dense inverse: preconditioner %.2e, its %s" % (kind, n, err, its))
+    assert err < 1e-4, err
+    assert its["0"] == its["1"]
