@@ -1834,6 +1834,7 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
   };
   vt("operator copies");
   // smoother matrices of the mixed preconditioner
+  if (c->mixed_smoother != 1 && (rc = ensure_w64(c, st))) return rc;   // the reference's smoother copied
   const double* Wsrc = c->d_W;
   const float* Wsrc32 = nullptr;
   double* Winv = nullptr;

@@ -241,6 +241,9 @@ struct dg_ctx {
   // mixed-precision state (dg_mixed.cuh) and operator versions
   void* mixed_state = nullptr;
   int build_version = 0;
+  // operator build whose FP64 smoother matrices d_W are current (built on
+  // first use: only the FP64 smoothing reads them)
+  int w_version = -1;
   int mixed_version = -1;
   long long arnoldi_kernels = 0;   // kernels in the captured Arnoldi cycle graph
 };
@@ -347,9 +350,6 @@ int launch_build(dg_ctx* c, cudaStream_t st) {
     if (c->B > 0) k<<<(unsigned)c->B, E::N * E::N, sizeof(Sm), st>>>(p);
   }
   bump();
-  if (c->B > 0) smoother_matrix_kernel<E::N, E::F><<<(unsigned)c->B, E::N * E::N, 0, st>>>(
-      c->d_blk, c->d_W, c->B, c->cfg.jac_wei);
-  bump();
   CKL(c);
   if (c->nbf > 0) {
     BFaceParams q;
@@ -369,10 +369,33 @@ int launch_build(dg_ctx* c, cudaStream_t st) {
   return DG_OK;
 }
 
+// The reference's three-sweep Jacobi smoother matrices W_e of the current
+// operator build (FP64): formed on first use, since only the FP64 smoothing
+// reads them (the mixed preconditioner's default smoother is its own block
+// inverse).
+template <int D>
+int ensure_w64_t(dg_ctx* c, cudaStream_t st) {
+  using E = Elem<D>;
+  if (c->w_version == c->build_version) return DG_OK;
+  if (c->B > 0)
+    smoother_matrix_kernel<E::N, E::F><<<(unsigned)c->B, E::N * E::N, 0, st>>>(c->d_blk, c->d_W, c->B,
+                                                                             c->cfg.jac_wei);
+  bump();
+  CKL(c);
+  c->w_version = c->build_version;
+  return DG_OK;
+}
+
+int ensure_w64(dg_ctx* c, cudaStream_t st) { return c->D == 3 ? ensure_w64_t<3>(c, st) : ensure_w64_t<2>(c, st); }
+
 template <int D>
 int launch_residual(dg_ctx* c, const double* x, const double* b, double* r, double* x_out, int flags,
                     cudaStream_t st, double* r1) {
   using E = Elem<D>;
+  if (flags & RF_SMOOTH) {
+    int rc;
+    if ((rc = ensure_w64_t<D>(c, st))) return rc;
+  }
   unsigned g = nblk(c->B, E::EPB);
   if (g) residual_kernel<E::N, E::F, E::EPB><<<g, E::EPB * E::N, 0, st>>>(
       c->d_blk, c->d_W, c->d_nbe, x, b, r, x_out, c->B, flags, c->T.P, r1);
