@@ -312,67 +312,99 @@ struct FastTab {
   static constexpr int Size = S + F * F * D * NN;
 };
 
+// Per-element geometry of the affine build, kappa-free and fixed for a
+// context (the coordinates do not change): det, C = Mi^T Mi, and per face
+// the area element sdet, the penalty gam = eta / h, cf = Mi^T n and the
+// neighbour's cn = Mn^T n.  One thread per element, so the FP64 work of the
+// Jacobians and inverses runs in full warps (on the GB300 a warp's FP64
+// instruction occupies its SM partition's FP64 pipe for the whole warp
+// whether one lane is active or 32); the record is GeomRec<D, F>::Size
+// doubles, and detw is written here too.
+template <int D, int F>
+struct GeomRec {
+  static constexpr int Det = 0, C = 1, Face = 1 + D * D, PerFace = 2 + 2 * D;
+  static constexpr int Size = Face + F * PerFace;
+};
+
 template <int D, int N, int F, int VG, int SG>
-__global__ void __launch_bounds__(N* N) build_blocks_affine_kernel(BuildParams p, const double* __restrict__ ftab) {
-  using TB = FastTab<D, N, F>;
-  constexpr int NN = N * N;
-  __shared__ double xe[D * N];
-  __shared__ double xnb[F][D * N];
-  __shared__ double Mi[D * D], C[D * D], det_s;
-  __shared__ double cf[F][D], cn[F][D], sdet[F], gam[F], kf[F];
-  __shared__ int nbi[F], nbfc[F], aln[F], bct[F];
-  const int64_t e = blockIdx.x;
-  const int tid = threadIdx.x;
+__global__ void __launch_bounds__(128) geom_affine_kernel(BuildParams p, double* __restrict__ geom) {
+  using G = GeomRec<D, F>;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= p.B) return;
   const Tables& T = p.T;
-  for (int k = tid; k < D * N; k += NN) xe[k] = p.x[e * D * N + k];
-  if (tid < F) {
-    const int64_t fi = e * F + tid;
-    nbi[tid] = p.nbe[fi];
-    nbfc[tid] = p.nbface[fi];
-    aln[tid] = p.aln[fi];
-    bct[tid] = p.bct[fi];
-  }
-  __syncthreads();
-  for (int k = tid; k < F * D * N; k += NN) {
-    const int f = k / (D * N), r = k % (D * N);
-    const int nb = nbi[f];
-    xnb[f][r] = nb >= 0 ? p.x[(int64_t)nb * D * N + r] : 0.0;
-  }
-  if (tid == 0) {
-    double j[D * D];
-    jacobian<D, N>(T.nlx, VG, 0, xe, j);
-    const double det = inv_det<D>(j, Mi);
-    det_s = det;
-    if (!(det > 0.0)) atomicExch(p.err, 1);
+  double* rec = geom + e * G::Size;
+  double j[D * D], Mi[D * D];
+  jacobian<D, N>(T.nlx, VG, 0, p.x + e * D * N, j);
+  const double det = inv_det<D>(j, Mi);
+  if (!(det > 0.0)) atomicExch(p.err, 1);
+  rec[G::Det] = det;
 #pragma unroll
-    for (int a = 0; a < D; ++a)
+  for (int a = 0; a < D; ++a)
 #pragma unroll
-      for (int b = 0; b < D; ++b) {
-        double t = 0.0;
+    for (int b = 0; b < D; ++b) {
+      double t = 0.0;
 #pragma unroll
-        for (int i = 0; i < D; ++i) t += Mi[i * D + a] * Mi[i * D + b];
-        C[a * D + b] = t;
-      }
-  }
-  __syncthreads();
-  for (int g = tid; g < VG; g += NN) p.detw[e * VG + g] = det_s * T.weight[g];
-  if (tid < F) {
-    const int f = tid;
-    double j[D * D], nrm[D];
-    jacobian<D, N>(T.nlx, VG, 0, xe, j);
+      for (int i = 0; i < D; ++i) t += Mi[i * D + a] * Mi[i * D + b];
+      rec[G::C + a * D + b] = t;
+    }
+  for (int g = 0; g < VG; ++g) p.detw[e * VG + g] = det * T.weight[g];
+  for (int f = 0; f < F; ++f) {
+    double* fr = rec + G::Face + f * G::PerFace;
+    double nrm[D];
     const double sd = face_normal<D>(j, T.drst + f * D * (D - 1), nrm);
-    sdet[f] = sd;
+    fr[0] = sd;
+    double h = 0.0;
+    for (int g = 0; g < SG; ++g) h += sd * T.sweight[g];
+    if (D == 3) h = sqrt(h);
+    fr[1] = p.eta / h;
 #pragma unroll
     for (int jj = 0; jj < D; ++jj) {
       double t = 0.0;
 #pragma unroll
       for (int i = 0; i < D; ++i) t += Mi[i * D + jj] * nrm[i];
-      cf[f][jj] = t;
+      fr[2 + jj] = t;
     }
-    double h = 0.0;
-    for (int g = 0; g < SG; ++g) h += sd * T.sweight[g];
-    if (D == 3) h = sqrt(h);
-    gam[f] = p.eta / h;
+    const int nb = p.nbe[e * F + f];
+    if (nb >= 0) {
+      double jn[D * D], mn[D * D];
+      jacobian<D, N>(T.nlx, VG, 0, p.x + (int64_t)nb * D * N, jn);
+      inv_det<D>(jn, mn);
+#pragma unroll
+      for (int jj = 0; jj < D; ++jj) {
+        double t = 0.0;
+#pragma unroll
+        for (int i = 0; i < D; ++i) t += mn[i * D + jj] * nrm[i];
+        fr[2 + D + jj] = t;
+      }
+    } else {
+#pragma unroll
+      for (int jj = 0; jj < D; ++jj) fr[2 + D + jj] = 0.0;
+    }
+  }
+}
+
+// Blocks of straight-sided elements from the geometry record and the
+// kappa-dependent face coefficients: one CTA per element, one thread per
+// block entry, no serial phase (the record is read into shared memory).
+template <int D, int N, int F, int VG, int SG>
+__global__ void __launch_bounds__(N* N) build_blocks_affine_kernel(BuildParams p, const double* __restrict__ ftab,
+                                                                   const double* __restrict__ geom) {
+  using TB = FastTab<D, N, F>;
+  using G = GeomRec<D, F>;
+  constexpr int NN = N * N;
+  __shared__ double rec[G::Size];
+  __shared__ double kf[F];
+  __shared__ int nbi[F], nbfc[F], aln[F], bct[F];
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x;
+  for (int k = tid; k < G::Size; k += NN) rec[k] = geom[e * G::Size + k];
+  if (tid < F) {
+    const int64_t fi = e * F + tid;
+    const int f = tid;
+    nbi[f] = p.nbe[fi];
+    nbfc[f] = p.nbface[fi];
+    aln[f] = p.aln[fi];
+    bct[f] = p.bct[fi];
     const double ke = p.kappa[e];
     if (bct[f] < 0) {
       const int nb = nbi[f];
@@ -383,23 +415,10 @@ __global__ void __launch_bounds__(N* N) build_blocks_affine_kernel(BuildParams p
     } else {
       kf[f] = 0.0;
     }
-    if (nbi[f] >= 0) {
-      double jn[D * D], mn[D * D];
-      jacobian<D, N>(T.nlx, VG, 0, xnb[f], jn);
-      inv_det<D>(jn, mn);
-#pragma unroll
-      for (int jj = 0; jj < D; ++jj) {
-        double t = 0.0;
-#pragma unroll
-        for (int i = 0; i < D; ++i) t += mn[i * D + jj] * nrm[i];
-        cn[f][jj] = t;
-      }
-    } else {
-#pragma unroll
-      for (int jj = 0; jj < D; ++jj) cn[f][jj] = 0.0;
-    }
   }
   __syncthreads();
+  const double* C = rec + G::C;
+  const double det_s = rec[G::Det];
   const int m = tid % N, n = tid / N;
   const int mn_ = m * N + n, nm_ = n * N + m;
   double vol = 0.0;
@@ -409,6 +428,10 @@ __global__ void __launch_bounds__(N* N) build_blocks_affine_kernel(BuildParams p
   double* out = p.blk + (size_t)e * (F + 1) * N * N;
 #pragma unroll
   for (int f = 0; f < F; ++f) {
+    const double* fr = rec + G::Face + f * G::PerFace;
+    const double sdet = fr[0], gam = fr[1];
+    const double* cf = fr + 2;
+    const double* cn = fr + 2 + D;
     double off = 0.0;
     if (kf[f] != 0.0) {
       const bool interior = bct[f] < 0;
@@ -417,21 +440,21 @@ __global__ void __launch_bounds__(N* N) build_blocks_affine_kernel(BuildParams p
 #pragma unroll
       for (int jj = 0; jj < D; ++jj) {
         const double* R = ftab + TB::R + (f * D + jj) * NN;
-        cs += cf[f][jj] * __ldg(R + mn_);
-        sc += cf[f][jj] * __ldg(R + nm_);
+        cs += cf[jj] * __ldg(R + mn_);
+        sc += cf[jj] * __ldg(R + nm_);
       }
       const double ss = __ldg(ftab + TB::Mf + f * NN + mn_);
-      diag += kf[f] * sdet[f] * (-a * cs - a * sc + gam[f] * ss);
+      diag += kf[f] * sdet * (-a * cs - a * sc + gam * ss);
       if (interior) {
         const int cmb = (f * F + nbfc[f]) * D + aln[f];
         double cnb = 0.0, snbv = 0.0;
 #pragma unroll
         for (int jj = 0; jj < D; ++jj) {
-          cnb += cn[f][jj] * __ldg(ftab + TB::Q + (cmb * D + jj) * NN + mn_);
-          snbv += cf[f][jj] * __ldg(ftab + TB::P + (cmb * D + jj) * NN + mn_);
+          cnb += cn[jj] * __ldg(ftab + TB::Q + (cmb * D + jj) * NN + mn_);
+          snbv += cf[jj] * __ldg(ftab + TB::P + (cmb * D + jj) * NN + mn_);
         }
         const double ssnb = __ldg(ftab + TB::S + cmb * NN + mn_);
-        off = kf[f] * sdet[f] * (-0.5 * cnb + 0.5 * snbv - gam[f] * ssnb);
+        off = kf[f] * sdet * (-0.5 * cnb + 0.5 * snbv - gam * ssnb);
       }
     }
     out[(size_t)(1 + f) * N * N + n * N + m] = off;

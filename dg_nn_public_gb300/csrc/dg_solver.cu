@@ -244,6 +244,10 @@ struct dg_ctx {
   // operator build whose FP64 smoother matrices d_W are current (built on
   // first use: only the FP64 smoothing reads them)
   int w_version = -1;
+  // geometry record of the affine build (GeomRec), formed once per context;
+  // geom_ok once a build that formed it passed the Jacobian check
+  double* d_geom = nullptr;
+  bool geom_ok = false;
   int mixed_version = -1;
   long long arnoldi_kernels = 0;   // kernels in the captured Arnoldi cycle graph
 };
@@ -342,8 +346,17 @@ int launch_build(dg_ctx* c, cudaStream_t st) {
                                  c->fast_build ? "affine" : "quadrature");
   }
   if (c->fast_build == 1 && !c->general_build && c->d_ftab) {
+    using GR = GeomRec<D, E::F>;
+    if (!c->geom_ok) {   // kappa-free geometry, once per context (again after a failed build)
+      int rc;
+      if (!c->d_geom && (rc = dalloc(c, &c->d_geom, (size_t)std::max<int64_t>(c->B, 1) * GR::Size))) return rc;
+      if (c->B > 0) geom_affine_kernel<D, E::N, E::F, E::VG, E::SG><<<nblk(c->B, 128), 128, 0, st>>>(p, c->d_geom);
+      bump();
+      CKL(c);
+    }
     if (c->B > 0)
-      build_blocks_affine_kernel<D, E::N, E::F, E::VG, E::SG><<<(unsigned)c->B, E::N * E::N, 0, st>>>(p, c->d_ftab);
+      build_blocks_affine_kernel<D, E::N, E::F, E::VG, E::SG><<<(unsigned)c->B, E::N * E::N, 0, st>>>(p, c->d_ftab,
+                                                                                                   c->d_geom);
   } else {
     auto k = build_blocks_kernel<D, E::N, E::F, E::VG, E::SG>;
     CK(c, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm)));
@@ -1239,6 +1252,7 @@ int dg_build_operator(dg_ctx* c, void* stream) {
   CK(c, cudaStreamSynchronize(st));
   const double t_blocks = ms_since(t0);
   if (herr) return fail(c, DG_ERR_MESH, "non-positive element Jacobian (element not positively oriented)");
+  if (c->d_geom) c->geom_ok = true;
   c->built = true;   // blocks are usable from here on (the probes below apply them)
   ++c->build_version;
   // colour-probe Galerkin operator on P1CG (volume_mf_diff.py:1696-1754), or
