@@ -119,7 +119,7 @@ int32_t nlevel_sfc(int64_t nonods) {
 // order they first appear while the fine rows are visited in curve order
 // (each in CSR order), and its values are accumulated in that same order.
 int sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double* a,
-               const int64_t* sfc_order, SfcHierarchy& h) {
+               const int64_t* sfc_order, SfcHierarchy& h, std::vector<std::vector<int64_t>>* visit_tgt) {
   h.nlevel = nlevel_sfc(n);
   std::vector<int64_t> pos(n), inv(n, -1);
   for (int64_t i = 0; i < n; ++i) {
@@ -144,8 +144,11 @@ int sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double
     std::vector<double> val;
   };
   std::vector<Lv> lv(h.nlevel);
+  if (visit_tgt) visit_tgt->assign(h.nlevel, std::vector<int64_t>());
   auto build_level = [&](int l) {
     Lv& L = lv[l];
+    std::vector<int64_t>* tg = visit_tgt ? &(*visit_tgt)[l] : nullptr;
+    if (tg) tg->reserve((size_t)fina[n]);
     const int64_t nc = h.sizes[l];
     L.rp.assign(nc + 1, 0);
     std::vector<int64_t> slot(nc, -1);   // coarse column -> entry of the current row
@@ -173,6 +176,7 @@ int sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double
           L.col.push_back(jc);
           L.val.push_back(a[k]);
         }
+        if (tg) tg->push_back(sl);
       }
     }
     if (cur_row >= 0) L.rp[cur_row + 1] = (int64_t)L.col.size();

@@ -55,8 +55,12 @@ void sparse_idx_for_color(int64_t n, const int64_t* fina, const int64_t* cola,
                           std::vector<std::vector<int64_t>>& spidx,
                           std::vector<std::vector<int64_t>>& colidx);
 int32_t nlevel_sfc(int64_t nonods);
+// visit_tgt (optional): per level, for each fine entry in the order the
+// level sums visit them (rows in curve order, entries in row order), the
+// index of the level entry it is added to
 int sfc_levels(int64_t n, const int64_t* fina, const int64_t* cola, const double* a,
-               const int64_t* sfc_order, SfcHierarchy& h);
+               const int64_t* sfc_order, SfcHierarchy& h,
+               std::vector<std::vector<int64_t>>* visit_tgt = nullptr);
 int face_connectivity(int ndim, int64_t nele, const int64_t* corners, int64_t* nbf, int64_t* alnmt);
 
 }  // namespace dg

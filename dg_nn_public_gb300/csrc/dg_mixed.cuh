@@ -1921,11 +1921,21 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
       if (h.sizes[l] <= c->dense_max32) { lc = l; break; }
     if (lc >= 0) {
       const int n = (int)h.sizes[lc];
-      // augmented [A | I] assembled on the host from the level's CSR, inverted on the GPU
+      // augmented [A | I] assembled on the host from the level's device CSR
+      // (its values are formed on the device after the first build),
+      // inverted on the GPU
+      const DevLevel& DL = c->lev[lc];
+      std::vector<int> drp(n + 1);
+      CK(c, cudaMemcpyAsync(drp.data(), DL.rowptr, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st));
+      CK(c, cudaStreamSynchronize(st));
+      std::vector<int> dcl(drp[n]);
+      std::vector<double> dvl(drp[n]);
+      CK(c, cudaMemcpyAsync(dcl.data(), DL.col, sizeof(int) * drp[n], cudaMemcpyDeviceToHost, st));
+      CK(c, cudaMemcpyAsync(dvl.data(), DL.val, sizeof(double) * drp[n], cudaMemcpyDeviceToHost, st));
+      CK(c, cudaStreamSynchronize(st));
       std::vector<double> Gh((size_t)n * 2 * n, 0.0);
-      const int64_t r0 = h.start[lc];
       for (int i = 0; i < n; ++i) {
-        for (int64_t k = h.row_ptr[r0 + i]; k < h.row_ptr[r0 + i + 1]; ++k) Gh[(size_t)i * 2 * n + h.col[k]] += h.val[k];
+        for (int k = drp[i]; k < drp[i + 1]; ++k) Gh[(size_t)i * 2 * n + dcl[k]] += dvl[k];
         Gh[(size_t)i * 2 * n + n + i] = 1.0;
       }
       // augmented matrix and pivot row / column (FP64 form) or the FP32

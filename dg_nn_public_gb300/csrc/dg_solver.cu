@@ -30,6 +30,17 @@ inline void bump(long long k = 1) { g_launches.fetch_add(k, std::memory_order_re
 
 struct DevLevel {
   int n = 0;
+  // fixed summation lists of the level values (after the first build): entry
+  // d = sum of rar[vk[j]] over j in [vptr[d], vptr[d+1]) in that order;
+  // didx[i] = entry of row i's diagonal or -1
+  int nnz = 0;
+  int* vptr = nullptr;
+  int* vk = nullptr;
+  int* didx = nullptr;
+  // coarse levels (long lists: one device thread would sum thousands of
+  // values in sequence) keep their lists on the host and are summed there
+  bool host_sum = false;
+  std::vector<int> h_vptr, h_vk, h_didx;
   int* rowptr = nullptr;
   int* col = nullptr;
   double* val = nullptr;
@@ -244,6 +255,10 @@ struct dg_ctx {
   // operator build whose FP64 smoother matrices d_W are current (built on
   // first use: only the FP64 smoothing reads them)
   int w_version = -1;
+  // the SFC level structure and summation lists are on the device: later
+  // builds form the level values there (no RAR download, host sums, upload)
+  bool lev_maps_ready = false;
+  double* rar_pinned = nullptr;   // pinned host copy of the Galerkin values (host-summed levels)
   // geometry record of the affine build (GeomRec), formed once per context;
   // geom_ok once a build that formed it passed the Jacobian check
   double* d_geom = nullptr;
@@ -307,6 +322,25 @@ template <>
 struct Elem<2> {
   static constexpr int N = 10, F = 3, VG = 12, SG = 4, NC = 3, EPB = 16;
 };
+
+// SFC level values from the Galerkin values: entry d is the sum of
+// rar[vk[j]] for j in [vptr[d], vptr[d+1]), left to right (the host
+// builder's order); diag[i] = the value of row i's diagonal entry (0 if none)
+__global__ void sfc_level_values_kernel(const double* __restrict__ rar, const int* __restrict__ vptr,
+                                        const int* __restrict__ vk, int nnz, double* __restrict__ val) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= nnz) return;
+  const int j0 = vptr[d], j1 = vptr[d + 1];
+  double s = rar[vk[j0]];
+  for (int j = j0 + 1; j < j1; ++j) s += rar[vk[j]];
+  val[d] = s;
+}
+
+__global__ void sfc_level_diag_kernel(const double* __restrict__ val, const int* __restrict__ didx, int n,
+                                      double* __restrict__ diag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) diag[i] = didx[i] >= 0 ? val[didx[i]] : 0.0;
+}
 
 template <int D>
 int launch_build(dg_ctx* c, cudaStream_t st) {
@@ -833,6 +867,7 @@ void dg_destroy(dg_ctx* ctx) {
   if (ctx->arnoldi_exec) cudaGraphExecDestroy(ctx->arnoldi_exec);
   destroy_mixed(ctx);
   if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
+  if (ctx->rar_pinned) cudaFreeHost(ctx->rar_pinned);
   for (void* p : ctx->allocs) cudaFree(p);
   cudaSetDevice(cur);
   delete ctx;
@@ -1281,14 +1316,67 @@ int dg_build_operator(dg_ctx* c, void* stream) {
                                                             (int)(b - a)); bump();
     CKL(c);
   }
+  SfcHierarchy& h = c->sfc_h;
+  if (c->lev_maps_ready) {
+    // SFC level values and diagonals from the Galerkin values, on the device,
+    // in the host builder's summation order (same bits)
+    const double t_probes = ms_since(t0);
+    bool any_host = false;
+    for (int l = 0; l < h.nlevel; ++l) {
+      DevLevel& L = c->lev[l];
+      if (L.host_sum) {
+        any_host = true;
+        continue;
+      }
+      if (L.nnz > 0)
+        sfc_level_values_kernel<<<nblk(L.nnz, 256), 256, 0, st>>>(c->d_rar, L.vptr, L.vk, L.nnz, L.val);
+      sfc_level_diag_kernel<<<nblk(L.n, 256), 256, 0, st>>>(L.val, L.didx, L.n, L.diag);
+      bump(2);
+    }
+    CKL(c);
+    if (any_host) {
+      if (!c->rar_pinned) CK(c, cudaMallocHost((void**)&c->rar_pinned, sizeof(double) * c->cola.size()));
+      CK(c, cudaMemcpyAsync(c->rar_pinned, c->d_rar, sizeof(double) * c->cola.size(), cudaMemcpyDeviceToHost, st));
+      CK(c, cudaStreamSynchronize(st));
+      struct HV {
+        std::vector<double> val, diag;
+      };
+      std::vector<HV> hv(h.nlevel);
+      parallel_for(h.nlevel, [&](int l) {
+        const DevLevel& L = c->lev[l];
+        if (!L.host_sum) return;
+        HV& o = hv[l];
+        o.val.resize(L.nnz);
+        for (int d = 0; d < L.nnz; ++d) {
+          int j = L.h_vptr[d];
+          double sum = c->rar_pinned[L.h_vk[j]];
+          for (++j; j < L.h_vptr[d + 1]; ++j) sum += c->rar_pinned[L.h_vk[j]];
+          o.val[d] = sum;
+        }
+        o.diag.resize(L.n);
+        for (int i = 0; i < L.n; ++i) o.diag[i] = L.h_didx[i] >= 0 ? o.val[L.h_didx[i]] : 0.0;
+      });
+      for (int l = 0; l < h.nlevel; ++l) {
+        const DevLevel& L = c->lev[l];
+        if (!L.host_sum) continue;
+        CK(c, cudaMemcpyAsync(L.val, hv[l].val.data(), sizeof(double) * L.nnz, cudaMemcpyHostToDevice, st));
+        CK(c, cudaMemcpyAsync(L.diag, hv[l].diag.data(), sizeof(double) * L.n, cudaMemcpyHostToDevice, st));
+      }
+    }
+    CK(c, cudaStreamSynchronize(st));
+    if (c->verbose)
+      std::fprintf(stderr, "[dg_build_operator] ms: blocks %.2f, colour probes %.2f, SFC level values (device) %.2f\n",
+                   t_blocks, t_probes - t_blocks, ms_since(t0) - t_probes);
+    return DG_OK;
+  }
   c->rar_host.assign(c->cola.size(), 0.0);
   CK(c, cudaMemcpyAsync(c->rar_host.data(), c->d_rar, sizeof(double) * c->cola.size(), cudaMemcpyDeviceToHost, st));
   CK(c, cudaStreamSynchronize(st));
   const double t_probes = ms_since(t0);
   // SFC levels (compact_fcode.f90 + get_a_diaga)
-  SfcHierarchy& h = c->sfc_h;
   h = SfcHierarchy();
-  if ((rc = sfc_levels(c->ncg, c->fina.data(), c->cola.data(), c->rar_host.data(), c->sfc.data(), h)))
+  std::vector<std::vector<int64_t>> visit_tgt;
+  if ((rc = sfc_levels(c->ncg, c->fina.data(), c->cola.data(), c->rar_host.data(), c->sfc.data(), h, &visit_tgt)))
     return fail(c, rc, g_thread_error);
   const double t_sfc = ms_since(t0);
   // (re)allocate the device levels
@@ -1328,9 +1416,21 @@ int dg_build_operator(dg_ctx* c, void* stream) {
   choose_vcycle_cluster(c);
   // rows sorted by column (torch CSR from COO) and the diagonal taken, level
   // by level on parallel host threads; then the uploads in level order
+  // the fine entries in the order the level sums visit them
+  std::vector<int> vk;
+  {
+    std::vector<int64_t> inv(c->ncg);
+    for (int64_t i = 0; i < c->ncg; ++i) inv[c->sfc[i] - 1] = i;
+    vk.reserve(c->cola.size());
+    for (int64_t sidx = 0; sidx < c->ncg; ++sidx) {
+      const int64_t node = inv[sidx];
+      for (int64_t k = c->fina[node]; k < c->fina[node + 1]; ++k) vk.push_back((int)k);
+    }
+  }
   struct Up {
     std::vector<int> rp, cl;
     std::vector<double> vl, dg;
+    std::vector<int> vptr, vkl, didx;   // summation lists in device entry order
   };
   std::vector<Up> ups(h.nlevel);
   parallel_for(h.nlevel, [&](int l) {
@@ -1343,20 +1443,35 @@ int dg_build_operator(dg_ctx* c, void* stream) {
     U.cl.resize(nnz);
     U.vl.resize(nnz);
     U.dg.assign(n, 0.0);
-    std::vector<std::pair<int64_t, double>> row;
+    U.didx.assign(n, -1);
+    std::vector<int64_t> dev_of(nnz);   // host (level-local) entry -> device entry
+    std::vector<std::pair<int64_t, int64_t>> row;   // (column, host entry)
     for (int i = 0; i < n; ++i) {
       const int64_t a = h.row_ptr[r0 + i], b = h.row_ptr[r0 + i + 1];
       row.clear();
-      for (int64_t k = a; k < b; ++k) row.emplace_back(h.col[k], h.val[k]);
+      for (int64_t k = a; k < b; ++k) row.emplace_back(h.col[k], k - base);
       std::sort(row.begin(), row.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
       U.rp[i] = (int)(a - base);
       for (size_t k = 0; k < row.size(); ++k) {
-        U.cl[a - base + k] = (int)row[k].first;
-        U.vl[a - base + k] = row[k].second;
-        if (row[k].first == i) U.dg[i] = row[k].second;
+        const int64_t d = a - base + (int64_t)k;
+        U.cl[d] = (int)row[k].first;
+        U.vl[d] = h.val[base + row[k].second];
+        dev_of[row[k].second] = d;
+        if (row[k].first == i) {
+          U.dg[i] = U.vl[d];
+          U.didx[i] = (int)d;
+        }
       }
     }
     U.rp[n] = (int)nnz;
+    // counting sort of the visits by device entry, visit order kept
+    const std::vector<int64_t>& tg = visit_tgt[l];
+    U.vptr.assign(nnz + 1, 0);
+    for (int64_t t : tg) U.vptr[dev_of[t] + 1]++;
+    for (int64_t d = 0; d < nnz; ++d) U.vptr[d + 1] += U.vptr[d];
+    std::vector<int> fill(U.vptr.begin(), U.vptr.end() - 1);
+    U.vkl.resize(tg.size());
+    for (size_t v = 0; v < tg.size(); ++v) U.vkl[fill[dev_of[tg[v]]]++] = vk[v];
   });
   for (int l = 0; l < h.nlevel; ++l) {
     DevLevel& L = c->lev[l];
@@ -1368,8 +1483,27 @@ int dg_build_operator(dg_ctx* c, void* stream) {
     CK(c, cudaMemcpyAsync(L.col, U.cl.data(), sizeof(int) * U.cl.size(), cudaMemcpyHostToDevice, st));
     CK(c, cudaMemcpyAsync(L.val, U.vl.data(), sizeof(double) * U.vl.size(), cudaMemcpyHostToDevice, st));
     CK(c, cudaMemcpyAsync(L.diag, U.dg.data(), sizeof(double) * U.dg.size(), cudaMemcpyHostToDevice, st));
+    L.nnz = (int)U.cl.size();
+    int maxlen = 0;
+    for (int d = 0; d < L.nnz; ++d) maxlen = std::max(maxlen, U.vptr[d + 1] - U.vptr[d]);
+    L.host_sum = maxlen > 64;
+    if (L.host_sum) {
+      L.h_vptr = U.vptr;
+      L.h_vk = U.vkl;
+      L.h_didx = U.didx;
+    } else {
+      if (!L.vptr) {
+        if ((rc = dalloc(c, &L.vptr, U.vptr.size()))) return rc;
+        if ((rc = dalloc(c, &L.vk, std::max<size_t>(U.vkl.size(), 1)))) return rc;
+        if ((rc = dalloc(c, &L.didx, std::max<size_t>(U.didx.size(), 1)))) return rc;
+      }
+      CK(c, cudaMemcpyAsync(L.vptr, U.vptr.data(), sizeof(int) * U.vptr.size(), cudaMemcpyHostToDevice, st));
+      CK(c, cudaMemcpyAsync(L.vk, U.vkl.data(), sizeof(int) * U.vkl.size(), cudaMemcpyHostToDevice, st));
+      CK(c, cudaMemcpyAsync(L.didx, U.didx.data(), sizeof(int) * U.didx.size(), cudaMemcpyHostToDevice, st));
+    }
   }
   CK(c, cudaStreamSynchronize(st));
+  c->lev_maps_ready = true;
   if (c->verbose)
     std::fprintf(stderr, "[dg_build_operator] ms: blocks %.2f, colour probes %.2f, SFC levels (host) %.2f, "
                  "level upload %.2f\n", t_blocks, t_probes - t_blocks, t_sfc - t_probes, ms_since(t0) - t_sfc);

@@ -238,3 +238,39 @@ def test_kappa_operator_against_reference_varprop():
         print("kappa residual vs reference varprop, component %d: %.3e" % (k, err))
         assert err < STAGE_TOL, (k, err)
     s.close()
+
+
+@pytest.mark.parametrize("kind,n", [("tet", 6), ("tri", 12)])
+def test_rebuild_forms_level_values_on_device(kind, n):
+    """After the first operator build a context forms the SFC level values
+    on the device from fixed summation lists; a rebuild with new kappa must
+    give the bits of a fresh context's host-formed levels: the FP64
+    preconditioner, the mixed preconditioner and the mixed solve agree
+    exactly."""
+    m = mesh.build_mesh(kind, n, seed=2)
+    order = sfc.hilbert_sfc_order(m.cg_coords)
+    cfg = SolverConfig(pre_smooth_its=2, post_smooth_its=2)
+    rng = np.random.default_rng(7)
+    k1 = np.exp(0.7 * rng.standard_normal(m.nele))
+    k2 = np.exp(0.7 * rng.standard_normal(m.nele))
+    a = DGSolver(m, order, cfg, element.p3_element(m.ndim))
+    a.set_kappa(k1)
+    a.build_operator()
+    a.set_kappa(k2)
+    a.build_operator()            # level values on the device
+    b = DGSolver(m, order, cfg, element.p3_element(m.ndim))
+    b.set_kappa(k2)
+    b.build_operator()            # level values on the host
+    g = torch.Generator(device="cuda:0").manual_seed(4)
+    r = torch.randn(a.nonods, dtype=torch.float64, device="cuda:0", generator=g)
+    assert torch.equal(a.precond(r), b.precond(r))
+    r32 = r.float()
+    assert torch.equal(a.precond_f32(r32), b.precond_f32(r32))
+    assert torch.equal(a.rar_values(), b.rar_values())
+    xa, xb = torch.zeros_like(r), torch.zeros_like(r)
+    tol = 1e-10 * float(torch.linalg.norm(r))
+    ia = a.solve_mixed(xa, r, tol)
+    ib = b.solve_mixed(xb, r, tol)
+    assert ia[0] == ib[0] and torch.equal(xa, xb)
+    a.close()
+    b.close()
