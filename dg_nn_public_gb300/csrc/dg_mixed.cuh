@@ -46,6 +46,11 @@ struct Mixed {
   float* sblk32 = nullptr;
   __nv_bfloat16* sblk16 = nullptr;
   bool sf = false, has5 = false;
+  // scaled face blocks S_ef = W_e A_ef (BF16, chunked, four per element) and
+  // c = W b of the current preconditioner application; sc = in use
+  __nv_bfloat16* scblk16 = nullptr;
+  float* chat = nullptr;
+  bool sc = false;
   std::vector<Lev32> lev;
   float *t1 = nullptr, *t2 = nullptr, *t3 = nullptr, *t4 = nullptr, *t5 = nullptr, *t6 = nullptr;
   float *cg1 = nullptr;
@@ -624,7 +629,7 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
     const MT* __restrict__ blk, const MT* __restrict__ W, const int* __restrict__ nbe, const float* __restrict__ x,
     const float* __restrict__ b, float* __restrict__ r, float* __restrict__ x_out, int64_t B, int flags,
     const float* __restrict__ P, float* __restrict__ r1, int* __restrict__ err, const int* __restrict__ fref5,
-    const float* __restrict__ wsp) {
+    const float* __restrict__ wsp, float* __restrict__ c_out) {
   const float wscale = wsp ? *wsp : 1.0f;
   constexpr int N = 20, F = 4;
   using G = TmaGroup<MT, EPB, WITH_W>;
@@ -810,9 +815,11 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
         for (int n = 0; n < N; ++n) t += Ps[n][m] * rs[le][n];
         r1[e * F + m] = t;
       }
-      if (smooth && valid)
-        x_out[e * N + m] = (zerox ? 0.0f : xs[le][0][m]) +
-                           wscale * C::dot(C::lds(sp + G::ABytes + (size_t)le * G::BlockBytes, m), rs[le], 0.0f);
+      if (smooth && valid) {
+        const float wr = C::dot(C::lds(sp + G::ABytes + (size_t)le * G::BlockBytes, m), rs[le], 0.0f);
+        x_out[e * N + m] = (zerox ? 0.0f : xs[le][0][m]) + wscale * wr;
+        if (c_out) c_out[e * N + m] = wr;   // W_e res, kept for the scaled-face steps
+      }
     }
     __syncthreads();   // stage s and xs / rs free again
     if (tid < 32) {
@@ -834,7 +841,8 @@ __global__ void __launch_bounds__(EPB * 20, MINB) residual_tma_kernel(
 // face, addressed through c->d_fref5); otherwise five blocks per element
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
 int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const float* b, float* r, float* x_out,
-               int flags, float* r1, cudaStream_t st, bool sf, const float* wscale = nullptr) {
+               int flags, float* r1, cudaStream_t st, bool sf, const float* wscale = nullptr,
+               float* c_out = nullptr) {
   if (c->l2_hint) flags |= RF_STREAM_HINT;
   const int64_t ngroups = (c->B + EPB - 1) / EPB;
   const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
@@ -842,10 +850,10 @@ int launch_tma(dg_ctx* c, const MT* blk, const MT* W, const float* x, const floa
   if (sf)
     return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W, true>, g, EPB * 20, smem, st, blk, W,
                     (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const float*)c->d_P32, r1,
-                    (int*)c->d_err, (const int*)c->d_fref5, wscale);
+                    (int*)c->d_err, (const int*)c->d_fref5, wscale, c_out);
   return launch_k(c, residual_tma_kernel<MT, EPB, S, MINB, WITH_W, false>, g, EPB * 20, smem, st, blk, W,
                   (const int*)c->d_nbe, x, b, r, x_out, (int64_t)c->B, flags, (const float*)c->d_P32, r1,
-                  (int*)c->d_err, (const int*)nullptr, wscale);
+                  (int*)c->d_err, (const int*)nullptr, wscale, c_out);
 }
 
 template <typename MT, int EPB, int S, int MINB, bool WITH_W>
@@ -866,13 +874,192 @@ int set_tma_smem(dg_ctx* c) {
 constexpr int kTmaVariants = 3;
 
 int launch_bf16_tma(dg_ctx* c, Mixed& M, const float* x, const float* b, float* r, float* x_out, int flags,
-                    cudaStream_t st, const float* ws = nullptr) {
+                    cudaStream_t st, const float* ws = nullptr, float* c_out = nullptr) {
   const __nv_bfloat16* A = M.sf ? M.sblk16 : M.blk16;
   switch (c->tma_variant) {
-    case 1: return launch_tma<__nv_bfloat16, 8, 2, 2, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws);
-    case 2: return launch_tma<__nv_bfloat16, 4, 2, 4, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws);
-    default: return launch_tma<__nv_bfloat16, 6, 2, 3, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws);
+    case 1:
+      return launch_tma<__nv_bfloat16, 8, 2, 2, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws, c_out);
+    case 2:
+      return launch_tma<__nv_bfloat16, 4, 2, 4, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws, c_out);
+    default:
+      return launch_tma<__nv_bfloat16, 6, 2, 3, true>(c, A, M.W16, x, b, r, x_out, flags, M.r1, st, M.sf, ws, c_out);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Smoothing on scaled face blocks.  With W_e = w A_ee^-1 the damped block
+// Jacobi step x' = x + s W_e (b - A x) is, element by element,
+//   x'_e = x_e + s (c_e - w x_e - sum_f S_ef x_nb(f)),
+// c_e = W_e b_e and S_ef = W_e A_ef: the self block becomes w I.  A step then
+// streams the four face blocks of an element (BF16, chunked layout, 3,200
+// bytes) instead of its five blocks and its smoother matrix (4,800 bytes).
+// c is formed by the zero-start step of each preconditioner application
+// (c_out of residual_tma_kernel) and serves every later step on the same
+// right-hand side.  The same persistent bulk-copy ring as
+// residual_tma_kernel: MINB CTAs per SM, groups of EPB consecutive elements,
+// S stages; blocks are copied before the programmatic-launch wait (they are
+// fixed during a solve), x and c gathered after it.
+constexpr int kScVariants = 4;
+
+// S_ef = W_e A_ef for the four faces of every element, in FP32 from the FP32
+// smoother matrices (column-major, W(m, n) at [n * 20 + m]) and the FP64
+// blocks, rounded once to BF16 in the chunked layout: one CTA of 400 threads
+// per element, thread (m, n) forms entry (m, n) of each face block as one
+// FMA chain over k.
+__global__ void __launch_bounds__(400) scaled_faces_kernel(const float* __restrict__ W,
+                                                           const double* __restrict__ blk,
+                                                           __nv_bfloat16* __restrict__ out, int64_t B) {
+  constexpr int N = 20, F = 4;
+  __shared__ float Ws[N * N];
+  __shared__ float As[F][N * N];
+  const int64_t e = blockIdx.x;
+  const int t = threadIdx.x;
+  Ws[t] = W[e * N * N + t];
+#pragma unroll
+  for (int f = 0; f < F; ++f) As[f][t] = (float)blk[(e * (F + 1) + 1 + f) * N * N + t];
+  __syncthreads();
+  const int m = t % N, n = t / N;
+#pragma unroll
+  for (int f = 0; f < F; ++f) {
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < N; ++k) acc = fmaf(Ws[k * N + m], As[f][n * N + k], acc);
+    out[(e * F + f) * N * N + chunk20_index(m, n)] = __float2bfloat16_rn(acc);
+  }
+}
+
+template <int EPB, int S, int MINB>
+__global__ void __launch_bounds__(EPB * 20, MINB) smooth_scaled_tma_kernel(
+    const __nv_bfloat16* __restrict__ sblk, const int* __restrict__ nbe, const float* __restrict__ x,
+    const float* __restrict__ cv, float* __restrict__ x_out, int64_t B, float w, const float* __restrict__ wsp,
+    int* __restrict__ err, int flags) {
+  constexpr int N = 20, F = 4, BB = Chunk20<__nv_bfloat16>::BlockBytes;
+  constexpr uint32_t GroupBytes = EPB * F * BB;
+  using C = Chunk20<__nv_bfloat16>;
+  const float wscale = wsp ? *wsp : 1.0f;
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  __shared__ __align__(8) uint64_t bar[S];
+  __shared__ float xs[EPB][F][N];
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x;
+  const int le = tid / N, m = tid % N;
+  const int64_t ngroups = (B + EPB - 1) / EPB;
+  const int64_t stride = gridDim.x;
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const uint64_t pol = l2_evict_first_policy();
+  const bool hint = flags & RF_STREAM_HINT;
+  auto issue = [&](int64_t k) {   // thread 0: group k of this CTA -> stage k % S
+    const int64_t g = blockIdx.x + k * stride;
+    if (g >= ngroups) return;
+    const int64_t e0 = g * EPB;
+    const uint32_t ne = (uint32_t)((B - e0) < EPB ? (B - e0) : EPB);
+    unsigned char* sp = tma_smem + (size_t)(k % S) * GroupBytes;
+    uint64_t* br = &bar[k % S];
+    mbar_expect_tx(br, ne * F * BB);
+    if (hint) bulk_copy_g2s_hint(sp, sblk + e0 * F * 400, ne * F * BB, br, pol);
+    else bulk_copy_g2s(sp, sblk + e0 * F * 400, ne * F * BB, br);
+  };
+  if (tid == 0)
+    for (int k = 0; k < S; ++k) issue(k);
+  auto load_nb = [&](int64_t g) {
+    const int64_t e = g * EPB + le;
+    return (g < ngroups && e < B) ? reinterpret_cast<const int4*>(nbe)[e] : make_int4(-1, -1, -1, -1);
+  };
+  int4 nb_cur = load_nb(blockIdx.x);
+  pdl_wait_then_trigger();
+  float x_own = 0.0f, c_own = 0.0f, x_nb[F] = {0.0f, 0.0f, 0.0f, 0.0f};
+  auto load_x = [&](int64_t g, const int4& nb) {
+    const int64_t e = g * EPB + le;
+    const bool ok = g < ngroups && e < B;
+    x_own = ok ? x[e * N + m] : 0.0f;
+    c_own = ok ? cv[e * N + m] : 0.0f;
+    const int nbv[F] = {nb.x, nb.y, nb.z, nb.w};
+#pragma unroll
+    for (int f = 0; f < F; ++f) x_nb[f] = (ok && nbv[f] >= 0) ? x[(int64_t)nbv[f] * N + m] : 0.0f;
+  };
+  load_x(blockIdx.x, nb_cur);
+  int4 nb_next = load_nb(blockIdx.x + stride);
+  int64_t k = 0;
+  for (int64_t g = blockIdx.x; g < ngroups; g += stride, ++k) {
+    const int64_t e = g * EPB + le;
+    const bool valid = e < B;
+    const int nbv[F] = {nb_cur.x, nb_cur.y, nb_cur.z, nb_cur.w};
+#pragma unroll
+    for (int f = 0; f < F; ++f) xs[le][f][m] = x_nb[f];
+    const float xo = x_own, co = c_own;
+    nb_cur = nb_next;
+    load_x(g + stride, nb_cur);
+    nb_next = load_nb(g + 2 * stride);
+    const int s = (int)(k % S);
+    if (!mbar_wait_bounded(&bar[s], (uint32_t)((k / S) & 1))) {
+      atomicExch(err, 3);
+      abort_flag = 1;
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    if (valid) {
+      const unsigned char* Se = tma_smem + (size_t)s * GroupBytes + (size_t)le * F * BB;
+      float acc = 0.0f;
+#pragma unroll
+      for (int f = 0; f < F; ++f)
+        if (nbv[f] >= 0) acc = C::dot(C::lds(Se + f * BB, m), xs[le][f], acc);
+      x_out[e * N + m] = xo + wscale * (co - fmaf(w, xo, acc));
+    }
+    __syncthreads();   // stage s and xs free again
+    if (tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(k + S);
+    }
+  }
+  if (abort_flag && tid == 0) {
+    for (int64_t j = k; j < k + S; ++j) {
+      if (blockIdx.x + j * stride >= ngroups) break;
+      (void)mbar_wait_bounded(&bar[j % S], (uint32_t)((j / S) & 1));
+    }
+  }
+}
+
+template <int EPB, int S, int MINB>
+int launch_scaled_shape(dg_ctx* c, const __nv_bfloat16* sblk, const float* x, const float* cv, float* x_out,
+                        cudaStream_t st, const float* ws) {
+  const int64_t ngroups = (c->B + EPB - 1) / EPB;
+  const unsigned g = (unsigned)std::min<int64_t>(ngroups, (int64_t)c->nsm * MINB);
+  const size_t smem = (size_t)S * EPB * 4 * Chunk20<__nv_bfloat16>::BlockBytes;
+  return launch_k(c, smooth_scaled_tma_kernel<EPB, S, MINB>, g, EPB * 20, smem, st, sblk, (const int*)c->d_nbe, x,
+                  cv, x_out, (int64_t)c->B, (float)c->mixed_smooth_w, ws, (int*)c->d_err,
+                  c->l2_hint ? (int)RF_STREAM_HINT : 0);
+}
+
+template <int EPB, int S, int MINB>
+int set_scaled_smem(dg_ctx* c) {
+  CK(c, cudaFuncSetAttribute(smooth_scaled_tma_kernel<EPB, S, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             S * EPB * 4 * Chunk20<__nv_bfloat16>::BlockBytes));
+  return DG_OK;
+}
+
+// launch shapes (elements per group, stages, CTAs per SM) of the scaled-face
+// smoothing kernel, picked by autotune_mixed
+int launch_scaled(dg_ctx* c, const __nv_bfloat16* sblk, const float* x, const float* cv, float* x_out,
+                  cudaStream_t st, const float* ws) {
+  switch (c->sc_variant) {
+    case 1: return launch_scaled_shape<8, 2, 3>(c, sblk, x, cv, x_out, st, ws);
+    case 2: return launch_scaled_shape<4, 2, 6>(c, sblk, x, cv, x_out, st, ws);
+    case 3: return launch_scaled_shape<6, 3, 3>(c, sblk, x, cv, x_out, st, ws);
+    default: return launch_scaled_shape<6, 2, 4>(c, sblk, x, cv, x_out, st, ws);
+  }
+}
+
+int set_scaled_smem_all(dg_ctx* c) {
+  int rc;
+  if ((rc = set_scaled_smem<6, 2, 4>(c)) || (rc = set_scaled_smem<8, 2, 3>(c)) || (rc = set_scaled_smem<4, 2, 6>(c)) ||
+      (rc = set_scaled_smem<6, 3, 3>(c)))
+    return rc;
+  return DG_OK;
 }
 
 // Gauss-Jordan inversion on the GPU (FP64, no pivoting: the coarse SFC level
@@ -1610,6 +1797,15 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
   return DG_OK;
 }
 
+// one smoothing step of the preconditioner with x != 0: x_out = x + s W (b -
+// A x), s = *ws.  On the scaled face blocks, rhs is c = W b (formed by the
+// zero-start step); otherwise it is b.
+int smooth_step(dg_ctx* c, const float* x, const float* rhs, float* x_out, cudaStream_t st, const float* ws) {
+  Mixed& M = mixed_of(c);
+  if (M.sc) return launch_scaled(c, M.scblk16, x, rhs, x_out, st, ws);
+  return residual_pc(c, x, rhs, nullptr, x_out, RF_SMOOTH, st, ws);
+}
+
 // z = M32^{-1} r (FP32, same schedule as precond()); scratch t3, t4, t5
 int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   Mixed& M = mixed_of(c);
@@ -1620,10 +1816,17 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   // per-step damping: pre-smoothing steps k = 0, 1, ... use ws[k], the
   // post-smoothing steps the same factors in reverse order
   auto ws = [&](int k) -> const float* { return (nsm == 2 || c->omegas_set) && k < 4 ? M.d_ws + k : nullptr; };
+  // scaled-face steps: the zero-start step also keeps c = W r, which every
+  // later step reads in place of r
+  const float* rs = M.sc ? M.chat : r;
   if (nsm > 0) {
-    if ((rc = residual_pc(c, nullptr, r, nullptr, cur, RF_ZEROX | RF_SMOOTH, st, ws(0)))) return rc;
+    if (M.sc) {
+      if ((rc = launch_bf16_tma(c, M, nullptr, r, nullptr, cur, RF_ZEROX | RF_SMOOTH, st, ws(0), M.chat))) return rc;
+    } else if ((rc = residual_pc(c, nullptr, r, nullptr, cur, RF_ZEROX | RF_SMOOTH, st, ws(0)))) {
+      return rc;
+    }
     for (int it = 1; it < nsm; ++it) {
-      if ((rc = residual_pc(c, cur, r, nullptr, other, RF_SMOOTH, st, ws(it)))) return rc;
+      if ((rc = smooth_step(c, cur, rs, other, st, ws(it)))) return rc;
       std::swap(cur, other);
     }
   } else {
@@ -1645,7 +1848,7 @@ int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   if ((rc = transfer32(c, nullptr, nullptr, cur, M.lev[0].e, st))) return rc;
   for (int it = 0; it < nsm; ++it) {
     float* out = (it == nsm - 1) ? z : other;
-    if ((rc = residual_pc(c, cur, r, nullptr, out, RF_SMOOTH, st, ws(nsm - 1 - it)))) return rc;
+    if ((rc = smooth_step(c, cur, rs, out, st, ws(nsm - 1 - it)))) return rc;
     other = cur;
     cur = out;
   }
@@ -1732,7 +1935,7 @@ int set_smoother_schedule(dg_ctx* c, cudaStream_t st) {
   for (int it0 = 0; it0 < kMaxIts && !stop;) {
     const int run = it0 == 0 ? 9 : std::min(8, kMaxIts - it0);
     for (int it = it0; it < it0 + run; ++it) {
-      if ((rc = residual_pc(c, v, zb, nullptr, u, RF_SMOOTH, st))) return rc;   // u = v - W A v
+      if ((rc = smooth_step(c, v, zb, u, st, nullptr))) return rc;   // u = v - W A v (c = W zb = 0)
       sub_f32_kernel<<<nblk(n, 256), 256, 0, st>>>(v, u, v, n);                 // v <- W A v
       bump();
       if ((rc = norm32(c, v, c->d_scal + 1 + it, st))) return rc;
@@ -1799,7 +2002,7 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
   const auto t0 = std::chrono::steady_clock::now();
   if ((rc = set_tma_smem<__nv_bfloat16, 6, 2, 3, true>(c)) || (rc = set_tma_smem<__nv_bfloat16, 8, 2, 2, true>(c)) ||
       (rc = set_tma_smem<__nv_bfloat16, 4, 2, 4, true>(c)) || (rc = set_tma_smem<float, 4, 2, 3, false>(c)) ||
-      (rc = set_tma_smem<float, 4, 2, 2, true>(c)))
+      (rc = set_tma_smem<float, 4, 2, 2, true>(c)) || (rc = set_scaled_smem_all(c)))
     return rc;
   const size_t nw = (size_t)c->B * c->N * c->N;
   if (!M.t1) {
@@ -1882,6 +2085,17 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
     if (herr) return fail(c, DG_ERR_NUMERIC, "element block with a non-positive pivot (not positive definite)");
   }
   vt("smoother copies");
+  // scaled face blocks of the BF16 bulk-copy smoothing steps (the smoother
+  // must be the damped block inverse: its self block is then w I)
+  M.sc = c->scaled_faces && c->D == 3 && c->precond_bf16 && c->bf16_tma && !M.sf && Wsrc32 != nullptr;
+  if (M.sc) {
+    if (!M.scblk16 && (rc = dalloc(c, &M.scblk16, (size_t)c->B * 4 * 400))) return rc;
+    if (!M.chat && (rc = dalloc(c, &M.chat, (size_t)c->nonods))) return rc;
+    scaled_faces_kernel<<<(unsigned)c->B, 400, 0, st>>>(Wsrc32, c->d_blk, M.scblk16, (int64_t)c->B);
+    bump();
+    CKL(c);
+    vt("scaled face blocks");
+  }
   if (M.lev.size() != c->lev.size()) {
     M.lev.assign(c->lev.size(), Lev32());
     for (size_t l = 0; l < c->lev.size(); ++l) {
@@ -2614,17 +2828,49 @@ int autotune_mixed(dg_ctx* c, cudaStream_t st) {
       bestv = v;
     }
   }
+  c->tma_variant = bestv;
+  bool changed = bestv != before;
+  float best_sc = 0.0f;
+  if (M.sc && !c->sc_pinned) {   // the scaled-face step's shape, timed the same way
+    const int before_sc = c->sc_variant;
+    best_sc = 1e30f;
+    int bv = 0;
+    for (int v = 0; v < kScVariants; ++v) {
+      c->sc_variant = v;
+      int rc = launch_scaled(c, M.scblk16, M.t3, M.t2, M.t4, st, nullptr);
+      if (!rc) CK(c, cudaEventRecord(e0, st));
+      for (int it = 0; it < 5 && !rc; ++it) rc = launch_scaled(c, M.scblk16, M.t3, M.t2, M.t4, st, nullptr);
+      if (rc) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rc;
+      }
+      CK(c, cudaEventRecord(e1, st));
+      CK(c, cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      CK(c, cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best_sc) {
+        best_sc = ms;
+        bv = v;
+      }
+    }
+    c->sc_variant = bv;
+    changed = changed || bv != before_sc;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  c->tma_variant = bestv;
-  if (bestv != before) {
+  if (changed) {
     for (auto& g : M.graphs)
       if (g) cudaGraphExecDestroy(g);
     M.graphs.clear();
     M.g_m = 0;
   }
-  if (c->verbose)
+  if (c->verbose) {
     std::fprintf(stderr, "[autotune] bulk-copy smoothing shape %d (%.1f us per launch)\n", bestv, best * 1e3f / 5.0f);
+    if (M.sc && !c->sc_pinned)
+      std::fprintf(stderr, "[autotune] scaled-face smoothing shape %d (%.1f us per launch)\n", c->sc_variant,
+                   best_sc * 1e3f / 5.0f);
+  }
   return DG_OK;
 }
 
@@ -2866,6 +3112,11 @@ extern "C" int dg_smooth_pc(dg_ctx* c, const float* x, const float* b, float* x_
   if (!M.built || c->mixed_version != c->build_version) {
     if ((rc = build_mixed(c, st))) return rc;
     c->mixed_version = c->build_version;
+  }
+  if (M.sc) {   // as the preconditioner runs it: c = W b first, then the scaled-face step
+    if ((rc = launch_bf16_tma(c, M, nullptr, b, nullptr, x_out, RF_ZEROX | RF_SMOOTH, st, nullptr, M.chat)))
+      return rc;
+    return launch_scaled(c, M.scblk16, x, M.chat, x_out, st, nullptr);
   }
   return residual_pc(c, x, b, nullptr, x_out, RF_SMOOTH, st);
 }

@@ -223,6 +223,12 @@ struct dg_ctx {
   bool batched_pinned = false;
   int tma_variant = 0;   // elements per group / stages / CTAs per SM of that kernel
   bool autotune = true;  // pick tma_variant by timing at the first mixed solve after a build
+  // mixed preconditioner (3D, BF16 bulk-copy path): smoothing steps after
+  // the zero-start one read the face blocks scaled by the smoother,
+  // S_ef = W_e A_ef, and c = W b (no self block, no smoother matrix)
+  bool scaled_faces = true;
+  int sc_variant = 0;    // launch shape of that kernel (autotuned with tma_variant)
+  bool sc_pinned = false;   // sc_variant set by DG_SCALED_VARIANT: not autotuned
   bool verbose = false;
   // mixed preconditioner smoother: 0 = the reference's three point-Jacobi
   // sweeps, 1 = damped exact block inverse w_b * A_ee^{-1}
@@ -988,6 +994,13 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (tv && tv[0]) {
       c->tma_variant = std::atoi(tv);
       c->autotune = false;
+    }
+    const char* scf = std::getenv("DG_SCALED_FACES");
+    if (scf && scf[0]) c->scaled_faces = scf[0] != '0';
+    const char* scv = std::getenv("DG_SCALED_VARIANT");
+    if (scv && scv[0]) {
+      c->sc_variant = std::atoi(scv);
+      c->sc_pinned = true;
     }
     const char* at = std::getenv("DG_AUTOTUNE");
     if (at && at[0]) c->autotune = at[0] != '0';

@@ -75,13 +75,17 @@ def test_mixed_iteration_limit_reports_noconv():
     assert torch.isfinite(x).all()
 
 
-@pytest.mark.parametrize("smoother,bf16,tol", [("jacobi3", False, 1e-5), ("blockinv", False, 1e-5),
-                                               ("blockinv", True, 3e-2)])
-def test_smooth_pc_matches_fp64_smoothing(smoother, bf16, tol):
+@pytest.mark.parametrize("smoother,bf16,scaled,tol", [("jacobi3", False, "1", 1e-5), ("blockinv", False, "1", 1e-5),
+                                                      ("blockinv", True, "0", 3e-2), ("blockinv", True, "1", 3e-2)])
+def test_smooth_pc_matches_fp64_smoothing(smoother, bf16, scaled, tol, monkeypatch):
     """One preconditioner smoothing step (FP32 vectors; FP32 or BF16 blocks)
     against the same step in FP64: the three-sweep Jacobi map through
     dg_residual(do_smooth=1), or x + w A_ee^-1 (b - A x) with the FP64
-    diagonal blocks from dg_get_bdiag.  Tolerance relative to max|x_out|."""
+    diagonal blocks from dg_get_bdiag.  With BF16 blocks the step runs on
+    the unscaled blocks and smoother matrices, or (scaled = "1") as
+    x + c - w x - sum_f S_f x_f with the scaled face blocks S_f = W A_f and
+    c = W b.  Tolerance relative to max|x_out|."""
+    monkeypatch.setenv("DG_SCALED_FACES", scaled)
     m, s, f, u = _setup("tet", 6, 2)
     w = 0.8
     s.set_mixed_options(smoother=smoother, smooth_w=w, precond_bf16=bf16)
@@ -111,6 +115,7 @@ def test_bulk_copy_kernels_match_plain_loads(n, monkeypatch):
     groups of elements)."""
     outs = {}
     monkeypatch.setenv("DG_SHARED_FACES", "0")
+    monkeypatch.setenv("DG_SCALED_FACES", "0")   # the plain-load kernels have no scaled form
     for tma in ("1", "0"):
         monkeypatch.setenv("DG_BF16_TMA", tma)
         monkeypatch.setenv("DG_F32_TMA", tma)
@@ -257,3 +262,25 @@ def test_blocked_fp32_dense_inverse(kind, n, monkeypatch):
     print("%s n=%d: blocked FP32 vs FP64 dense inverse: preconditioner %.2e, its %s" % (kind, n, err, its))
     assert err < 1e-4, err
     assert its["0"] == its["1"]
+
+
+@pytest.mark.parametrize("kind,n", [("tet", 6), ("tet", 8)])
+def test_scaled_face_smoothing_solve(kind, n, monkeypatch):
+    """The mixed solve with the preconditioner's smoothing steps on the
+    scaled face blocks (S_ef = W_e A_ef, c = W b: the self block is w I)
+    against the same solve on the unscaled blocks: both meet the FP64
+    residual tolerance, the solutions agree within 1e-7 and the inner
+    iteration counts stay within 10% of each other."""
+    res = {}
+    for scaled in ("0", "1"):
+        monkeypatch.setenv("DG_SCALED_FACES", scaled)
+        m, s, f, u = _setup(kind, n, 2)
+        b = s.rhs(torch.tensor(f, device="cuda:0"))
+        tol = 1e-10 * float(torch.linalg.norm(b))
+        x = torch.zeros_like(b)
+        its, r, outer = s.solve_mixed(x, b, tol)
+        assert r <= tol
+        res[scaled] = (its, x.clone())
+    (i0, x0), (i1, x1) = res["0"], res["1"]
+    assert float(torch.abs(x1 - x0).max() / torch.abs(x0).max()) < 1e-7
+    assert abs(i1 - i0) <= max(2, 0.1 * i0), (i0, i1)
