@@ -278,6 +278,7 @@ def config_block(args, m, extra=None):
 # by the element count (BF16 step, FP32 apply, FP64 residual;
 # profiles/residual_tma_kernel_c2.md); other workloads report null.
 TRAFFIC_C2 = {
+    "smooth_scaled": {"bytes_per_launch": None},
     "smooth_pc": {"bytes_per_launch": 240.2e6},
     "apply_f32": {"bytes_per_launch": 393.4e6},
     "apply_f64": {"bytes_per_launch": 773.9e6},
@@ -584,19 +585,32 @@ def run_ours(args):
         # stored blocks: own + one per interior face when faces are shared
         # (s_int counts interior face sides), else own + one per face side;
         # plus the face table read per element
-        nsh = int(s.info().get("shared_faces", 0))
+        info = s.info()
+        nsh = int(info.get("shared_faces", 0))
+        scaled = bool(info.get("scaled_faces", 0))
         nblk_a = m.nele + (nsh if nsh else s_int)
         ftab = m.nele * (F + 1) * 4 if nsh else 0
-        nb = nblk_a * N * N * mb + m.nele * N * N * mb + 3 * dofs * 4 + m.nele * F * 4 + ftab
-        # back-to-back launches stream the blocks from HBM (evict-first; ncu
-        # DRAM bytes = algorithmic bytes); the shared-face form keeps face
-        # blocks in L2 between reads, so it is timed with the L2 flushed
-        t = time_launch(lambda: s.smooth_pc(xs, bs, xo), cold=bool(nsh))
         form = "interior faces stored once" if nsh else "five blocks per element"
         sfx = "_sf" if nsh else ""
-        rooflines.append(("smooth_pc" + sfx, "residual_tma_kernel<bf16> (bulk-copy streamed preconditioner "
-                          "smoothing step, BF16 blocks (%s) + smoother matrices, FP32 vectors)" % form,
-                          nb, t, 2.0 * N * N * (2 * m.nele + s_int)))
+        if scaled:
+            # the preconditioner's smoothing steps after the zero-start one
+            # (3 of its 5 block-streaming launches): four scaled BF16 face
+            # blocks per element, x, c = W b and x_out (the neighbour x
+            # gathers hit L2), the neighbour table
+            nb = m.nele * F * N * N * 2 + 3 * dofs * 4 + m.nele * F * 4
+            t = time_launch(lambda: s.smooth_scaled(xs, bs, xo))
+            rooflines.append(("smooth_scaled", "smooth_scaled_tma_kernel (bulk-copy streamed preconditioner "
+                              "smoothing step on scaled face blocks W_e A_ef: four BF16 blocks per element, "
+                              "FP32 vectors)", nb, t, 2.0 * N * N * F * m.nele))
+        else:
+            nb = nblk_a * N * N * mb + m.nele * N * N * mb + 3 * dofs * 4 + m.nele * F * 4 + ftab
+            # back-to-back launches stream the blocks from HBM (evict-first; ncu
+            # DRAM bytes = algorithmic bytes); the shared-face form keeps face
+            # blocks in L2 between reads, so it is timed with the L2 flushed
+            t = time_launch(lambda: s.smooth_pc(xs, bs, xo), cold=bool(nsh))
+            rooflines.append(("smooth_pc" + sfx, "residual_tma_kernel<bf16> (bulk-copy streamed preconditioner "
+                              "smoothing step, BF16 blocks (%s) + smoother matrices, FP32 vectors)" % form,
+                              nb, t, 2.0 * N * N * (2 * m.nele + s_int)))
         ya = torch.empty_like(xs)
         nb = nblk_a * N * N * 4 + 2 * dofs * 4 + m.nele * F * 4 + ftab
         t = time_launch(lambda: s.apply_f32(xs, ya), cold=bool(nsh))
@@ -604,8 +618,9 @@ def run_ours(args):
                           "%s)" % form, nb, t, 2.0 * N * N * (m.nele + s_int)))
         # the same BF16 step with the L2 flushed before every launch (each
         # launch timed alone: nothing of the previous launch's stream is in L2)
-        t = time_launch(lambda: s.smooth_pc(xs, bs, xo), cold=True)
-        rooflines.append(("smooth_pc_cold", rooflines[0][1] + ", L2 flushed before each launch",
+        t = time_launch((lambda: s.smooth_scaled(xs, bs, xo)) if scaled else (lambda: s.smooth_pc(xs, bs, xo)),
+                        cold=True)
+        rooflines.append((rooflines[0][0] + "_cold", rooflines[0][1] + ", L2 flushed before each launch",
                           rooflines[0][2], t, rooflines[0][4]))
         # the plain FP64 path's operator apply (stored FP64 blocks)
         xa = torch.randn(dofs, dtype=torch.float64, device=dev)
@@ -618,7 +633,7 @@ def run_ours(args):
         t_pc = time_launch(lambda: s.precond_f32(bs, xo))
         it_ms = RMX["t_ms"] / args.steps / max(1, int(np.median(RMX["its"])))
         breakdown = {"iteration_ms": it_ms, "precond_f32_ms": t_pc * 1e3, "apply_f32_ms": rooflines[1][3] * 1e3,
-                     "smooth_pc_ms": rooflines[0][3] * 1e3,
+                     ("smooth_scaled_ms" if scaled else "smooth_pc_ms"): rooflines[0][3] * 1e3,
                      "rest_ms": it_ms - t_pc * 1e3 - rooflines[1][3] * 1e3}
     else:
         xa = torch.randn(dofs, dtype=torch.float64, device=dev)

@@ -69,6 +69,8 @@ _SIGNATURES = {
     "dg_apply_f32": (_I, [_P, _P, _P, _P]),
     "dg_solve_mixed_batched": (_I, [_P, _P, _P, C.c_int32, _P, C.c_int32, C.c_int32, C.c_double, _P, _P, _P]),
     "dg_smooth_pc": (_I, [_P, _P, _P, _P, _P]),
+    "dg_smooth_scaled": (_I, [_P, _P, _P, _P, _P]),
+    "dg_smooth_scaled_batched": (_I, [_P, _P, _P, _P, _P]),
     "dg_apply_batched": (_I, [_P, _P, _P, _P]),
     "dg_smooth_pc_batched": (_I, [_P, _P, _P, _P, _P]),
     "dg_set_batched_kernel": (_I, [_P, C.c_int32]),

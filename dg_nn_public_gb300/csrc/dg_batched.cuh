@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat1
                                                        const float* __restrict__ b, float* __restrict__ r,
                                                        float* __restrict__ x_out, int64_t B, int flags,
                                                        const float* __restrict__ P, float* __restrict__ r1,
-                                                       const float* __restrict__ wsp) {
+                                                       const float* __restrict__ wsp, float* __restrict__ c_out) {
   constexpr int N = 20, F = 4;
   const float ws = wsp ? *wsp : 1.0f;
   __shared__ __align__(16) unsigned char As[(F + 1) * 800];
@@ -457,9 +457,116 @@ __global__ void __launch_bounds__(NWARP * 32) bres_mma_kernel(const __nv_bfloat1
           const float2 xv = xpre[mt][hh][nt];
           *reinterpret_cast<float2*>(x_out + o) =
               make_float2(ws * c2[mt][nt][2 * hh] + xv.x, ws * c2[mt][nt][2 * hh + 1] + xv.y);
+          // W res, kept for the scaled-face steps (bsc_mma_kernel)
+          if (c_out) *reinterpret_cast<float2*>(c_out + o) = make_float2(c2[mt][nt][2 * hh], c2[mt][nt][2 * hh + 1]);
         }
       }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Batched smoothing step on the scaled face blocks S_ef = W_e A_ef (BF16,
+// chunked, four per element; the single-RHS form is smooth_scaled_tma_kernel):
+//   X_out = X + s (C - w X - sum_f S_ef X_nb(f)),   C = W B,
+// C formed by the zero-start step (c_out of bres_mma_kernel).  The face
+// products run on the tensor cores as in bres_mma_kernel (x split into BF16
+// hi + lo, mma.sync m16n8k16 + m16n8k8), but per element there are four
+// block products instead of five, no smoother product and no second
+// shared-memory round: the epilogue works on the accumulators directly.
+template <int NWARP>
+__global__ void __launch_bounds__(NWARP * 32) bsc_mma_kernel(const __nv_bfloat16* __restrict__ sblk,
+                                                      const int* __restrict__ nbe, const float* __restrict__ x,
+                                                      const float* __restrict__ cv, float* __restrict__ x_out,
+                                                      int64_t B, float w, const float* __restrict__ wsp) {
+  constexpr int N = 20, F = 4;
+  const float ws = wsp ? *wsp : 1.0f;
+  __shared__ __align__(16) unsigned char As[F * 800];
+  __shared__ __align__(16) unsigned char Xhi[F * 24 * kXRow];
+  __shared__ __align__(16) unsigned char Xlo[F * 24 * kXRow];
+  __shared__ int nbs[F];
+  const int64_t e = blockIdx.x;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, t = lane & 3;
+  if (tid < F) nbs[tid] = nbe[e * F + tid];
+  for (int i = tid; i < F * 800 / 16; i += NWARP * 32)
+    reinterpret_cast<uint4*>(As)[i] = reinterpret_cast<const uint4*>(sblk + e * F * 400)[i];
+  for (int i = tid; i < F * 4 * (kNR / 4); i += NWARP * 32) {   // zero pad slots (nodes 20..23)
+    const int bb = i / (4 * (kNR / 4)), rem = i % (4 * (kNR / 4));
+    const int row = bb * 24 + 20 + rem / (kNR / 4), q4 = rem % (kNR / 4);
+    *reinterpret_cast<uint2*>(Xhi + row * kXRow + q4 * 8) = make_uint2(0u, 0u);
+    *reinterpret_cast<uint2*>(Xlo + row * kXRow + q4 * 8) = make_uint2(0u, 0u);
+  }
+  constexpr int NT = 8 / NWARP;
+  const int rbase = warp * 8 * NT;
+  float acc[2][NT][4];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[mt][nt][i] = 0.0f;
+  // the epilogue's c and x values of this thread, loaded with the gather
+  float2 cpre[2][2][NT], xpre[2][2][NT];
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const int row = mt * 16 + g + 8 * hh;
+        const int64_t o = (e * N + row) * kNR + rbase + nt * 8 + 2 * t;
+        const bool ok = row < N;
+        cpre[mt][hh][nt] = ok ? *reinterpret_cast<const float2*>(cv + o) : make_float2(0.f, 0.f);
+        xpre[mt][hh][nt] = ok ? *reinterpret_cast<const float2*>(x + o) : make_float2(0.f, 0.f);
+      }
+  __syncthreads();   // nbs
+  {
+    constexpr int kItems = F * N * (kNR / 4);   // 1280 float4
+    constexpr int kPer = (kItems + NWARP * 32 - 1) / (NWARP * 32);
+    float4 v[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int i = tid + u * NWARP * 32;
+      v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i < kItems) {
+        const int bb = i / (N * (kNR / 4)), rem = i % (N * (kNR / 4));
+        const int64_t src_e = nbs[bb];
+        if (src_e >= 0) v[u] = reinterpret_cast<const float4*>(x + src_e * N * kNR)[rem];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int i = tid + u * NWARP * 32;
+      if (i < kItems) {
+        const int bb = i / (N * (kNR / 4)), rem = i % (N * (kNR / 4));
+        const int n = rem / (kNR / 4), q4 = rem % (kNR / 4);
+        const int row = bb * 24 + n;
+        store_split4(Xhi + row * kXRow + q4 * 8, Xlo + row * kXRow + q4 * 8, v[u]);
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int bb = 0; bb < F; ++bb) {
+    if (nbs[bb] < 0) continue;
+    mma_block_t<NT>(acc, As + bb * 800, Xhi, bb * 24, rbase, lane);
+    mma_block_t<NT>(acc, As + bb * 800, Xlo, bb * 24, rbase, lane);
+  }
+#pragma unroll
+  for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+      const int row = mt * 16 + g + 8 * hh;
+      if (row >= N) continue;
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const int64_t o = (e * N + row) * kNR + rbase + nt * 8 + 2 * t;
+        const float2 xv = xpre[mt][hh][nt], cc = cpre[mt][hh][nt];
+        *reinterpret_cast<float2*>(x_out + o) =
+            make_float2(xv.x + ws * (cc.x - fmaf(w, xv.x, acc[mt][nt][2 * hh])),
+                        xv.y + ws * (cc.y - fmaf(w, xv.y, acc[mt][nt][2 * hh + 1])));
+      }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1275,6 +1382,7 @@ struct BatchState {
   double *H = nullptr, *part = nullptr, *h = nullptr, *nrm = nullptr, *scl = nullptr, *y = nullptr;
   float* inv = nullptr;
   double* r64 = nullptr;                    // (kNR, nonods) FP64 residuals, RHS-major
+  float* chat = nullptr;                    // C = W R of the scaled-face steps (nonods, kNR)
   int nblk = 0;
   // BF16 blocks + smoother matrices in the padded tensor-core layout of
   // bres_tc05_kernel (5,760 bytes per element), rebuilt per mixed build
@@ -1410,10 +1518,10 @@ int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, co
       if (c->B > 0) {
         if (variant == 2)
           bres_mma_kernel<8><<<(unsigned)c->B, 256, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, b, nullptr, xo, c->B,
-                                                             flags, c->d_P32, rr1, ws);
+                                                             flags, c->d_P32, rr1, ws, nullptr);
         else
           bres_mma_kernel<4><<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, xx, b, nullptr, xo, c->B,
-                                                             flags, c->d_P32, rr1, ws);
+                                                             flags, c->d_P32, rr1, ws, nullptr);
       }
       bump();
       CKL(c);
@@ -1451,6 +1559,36 @@ int bsmooth(dg_ctx* c, Mixed& M, BatchState& S, int variant, const float* xx, co
       return btcs(c, S, xx ? S.xs1 : nullptr, b, xo, flags & ~RF_OUT_SPLIT, rr1, ws, st);
     }
   }
+}
+
+// The batched preconditioner's smoothing steps on the scaled face blocks
+// (bsc_mma_kernel) need the single-RHS scaled copy and the mma.sync forms
+// for the zero-start step (which forms C) and the restriction.
+bool batched_scaled(dg_ctx* c, const Mixed& M) {
+  return M.sc && c->precond_bf16 && c->batched_kernel >= 1 && c->batched_kernel <= 4;
+}
+
+// zero-start step X_out = s W B that also keeps C = W B
+int bzero_start_scaled(dg_ctx* c, Mixed& M, BatchState& S, const float* b, float* xo, const float* ws,
+                       cudaStream_t st) {
+  int rc;
+  if (!S.chat && (rc = dalloc(c, &S.chat, (size_t)c->nonods * kNR))) return rc;
+  if (c->B > 0)
+    bres_mma_kernel<4><<<(unsigned)c->B, 128, 0, st>>>(M.blk16, M.W16, c->d_nbe, nullptr, b, nullptr, xo, c->B,
+                                                       RF_ZEROX | RF_SMOOTH, c->d_P32, nullptr, ws, S.chat);
+  bump();
+  CKL(c);
+  return DG_OK;
+}
+
+int bsmooth_scaled(dg_ctx* c, Mixed& M, const float* xx, const float* cv, float* xo, const float* ws,
+                   cudaStream_t st) {
+  if (c->B > 0)
+    bsc_mma_kernel<4><<<(unsigned)c->B, 128, 0, st>>>(M.scblk16, c->d_nbe, xx, cv, xo, c->B, (float)c->mixed_smooth_w,
+                                                      ws);
+  bump();
+  CKL(c);
+  return DG_OK;
 }
 
 // Smoothing-kernel autotuner of the batched solve: times every variant of
@@ -1532,6 +1670,8 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   // split-x pipeline: the iterate stays in the tensor-core operand layout
   // from the first smoothing step to the last, which writes z in FP32
   const bool split = bf && c->batched_kernel >= 5;
+  // scaled face blocks for the smoothing steps after the zero-start one
+  const bool sc = !split && batched_scaled(c, M);
   unsigned char* scur = nullptr;
   unsigned char* soth = nullptr;
   if (split) {
@@ -1544,6 +1684,13 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
       std::swap(scur, soth);
     }
     if ((rc = btcs(c, S, scur, r, nullptr, RF_RESTRICT, S.r1, nullptr, st))) return rc;
+  } else if (sc) {
+    if ((rc = bzero_start_scaled(c, M, S, r, cur, wsk(0), st))) return rc;
+    for (int it = 1; it < nsm; ++it) {
+      if ((rc = bsmooth_scaled(c, M, cur, S.chat, other, wsk(it), st))) return rc;
+      std::swap(cur, other);
+    }
+    if ((rc = pc(cur, nullptr, RF_RESTRICT, S.r1, nullptr))) return rc;
   } else {
     if ((rc = pc(nullptr, cur, RF_ZEROX | RF_SMOOTH, nullptr, wsk(0)))) return rc;
     for (int it = 1; it < nsm; ++it) {
@@ -1603,7 +1750,9 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   bump();
   for (int it = 0; it < nsm; ++it) {
     float* out = (it == nsm - 1) ? z : other;
-    if ((rc = pc(cur, out, RF_SMOOTH, nullptr, wsk(nsm - 1 - it)))) return rc;
+    if ((rc = sc ? bsmooth_scaled(c, M, cur, S.chat, out, wsk(nsm - 1 - it), st)
+                 : pc(cur, out, RF_SMOOTH, nullptr, wsk(nsm - 1 - it))))
+      return rc;
     other = cur;
     cur = out;
   }
@@ -1677,6 +1826,8 @@ int run_bstep(dg_ctx* c, int j, int m, cudaStream_t st) {
       M.blk,
       M.blk16,
       M.dense_inv,
+      tag(batched_scaled(c, M)),
+      M.scblk16,
   };
   if (key != S.step_key) {
     for (auto& g : S.step_graph)
@@ -1689,6 +1840,7 @@ int run_bstep(dg_ctx* c, int j, int m, cudaStream_t st) {
     int rc;
     if (c->precond_bf16 && c->batched_kernel >= 4 && (rc = ensure_tc_layout(c, M, S, st))) return rc;
     if (c->precond_bf16 && c->batched_kernel >= 5 && (rc = ensure_split(c, S))) return rc;
+    if (batched_scaled(c, M) && !S.chat && (rc = dalloc(c, &S.chat, (size_t)c->nonods * kNR))) return rc;
     if (!c->cap_stream) CK(c, cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking));
     CK(c, cudaStreamBeginCapture(c->cap_stream, cudaStreamCaptureModeThreadLocal));
     const long long k0 = g_launches.load();
@@ -1982,6 +2134,21 @@ extern "C" int dg_smooth_pc_batched(dg_ctx* c, const float* x, const float* b, f
   CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
   return bsmooth(c, M, batch_of(M), c->batched_kernel, x, b, x_out, x ? RF_SMOOTH : (RF_SMOOTH | RF_ZEROX), nullptr,
                  nullptr, st);
+}
+
+// X_out = X + (C - w X - sum_f S_ef X_nb(f)) for 64 right-hand sides on the
+// scaled face blocks (the batched preconditioner's steps after its zero-start
+// one, bsc_mma_kernel); DG_ERR_STATE when the scaled form is not in use.
+extern "C" int dg_smooth_scaled_batched(dg_ctx* c, const float* x, const float* cv, float* x_out, void* stream) {
+  if (!c || !x || !cv || !x_out) return set_thread_error(DG_ERR_ARG, "dg_smooth_scaled_batched: null argument");
+  if (x_out == x) return fail(c, DG_ERR_ARG, "dg_smooth_scaled_batched: x_out must not alias x");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int rc;
+  if ((rc = batched_prep(c, "dg_smooth_scaled_batched", st))) return rc;
+  Mixed& M = mixed_of(c);
+  if (!M.sc || !c->precond_bf16)
+    return fail(c, DG_ERR_STATE, "dg_smooth_scaled_batched: the scaled face blocks are not in use");
+  return bsmooth_scaled(c, M, x, cv, x_out, nullptr, st);
 }
 
 // Batched smoothing kernel variant: -1 = timed choice at the next batched

@@ -3121,6 +3121,22 @@ extern "C" int dg_smooth_pc(dg_ctx* c, const float* x, const float* b, float* x_
   return residual_pc(c, x, b, nullptr, x_out, RF_SMOOTH, st);
 }
 
+extern "C" int dg_smooth_scaled(dg_ctx* c, const float* x, const float* cv, float* x_out, void* stream) {
+  if (!c || !x || !cv || !x_out) return set_thread_error(DG_ERR_ARG, "dg_smooth_scaled: null argument");
+  if (x_out == x) return fail(c, DG_ERR_ARG, "dg_smooth_scaled: x_out must not alias x");
+  if (!c->built) return fail(c, DG_ERR_STATE, "dg_smooth_scaled: operator not built");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  CK(c, cudaSetDevice(c->dev));
+  Mixed& M = mixed_of(c);
+  int rc;
+  if (!M.built || c->mixed_version != c->build_version) {
+    if ((rc = build_mixed(c, st))) return rc;
+    c->mixed_version = c->build_version;
+  }
+  if (!M.sc) return fail(c, DG_ERR_STATE, "dg_smooth_scaled: the scaled face blocks are not in use");
+  return launch_scaled(c, M.scblk16, x, cv, x_out, st, nullptr);
+}
+
 // Options of the mixed-precision preconditioner (take effect at the next
 // mixed solve): smoother 0 = three point-Jacobi sweeps as the reference,
 // 1 = damped block inverse smooth_w * A_ee^{-1}; precond_bf16 != 0 stores

@@ -883,10 +883,13 @@ int dg_info(const dg_ctx* ctx, int64_t* out, int32_t nout) {
   if (!ctx || !out) return set_thread_error(DG_ERR_ARG, "dg_info: null argument");
   const bool sf = ctx->D == 3 && ctx->shared_faces && ctx->d_fref5 && ctx->f32_tma && ctx->bf16_tma &&
                   ctx->precond_bf16;
-  int64_t v[16] = {ctx->D, ctx->N, ctx->B, ctx->nonods, ctx->ncg, (int64_t)ctx->cola.size(), ctx->ncolor,
+  const bool sc = ctx->scaled_faces && ctx->D == 3 && ctx->precond_bf16 && ctx->bf16_tma && !sf &&
+                  ctx->mixed_smoother == 1;
+  int64_t v[18] = {ctx->D, ctx->N, ctx->B, ctx->nonods, ctx->ncg, (int64_t)ctx->cola.size(), ctx->ncolor,
                    (int64_t)ctx->lev.size(), ctx->nbf, ctx->built ? 1 : 0, ctx->VG, ctx->SG, ctx->tma_variant,
-                   ctx->batched_kernel == 3 ? 1 : 0, sf ? ctx->nface_sh : 0, ctx->batched_kernel};
-  for (int i = 0; i < nout && i < 16; ++i) out[i] = v[i];
+                   ctx->batched_kernel == 3 ? 1 : 0, sf ? ctx->nface_sh : 0, ctx->batched_kernel, sc ? 1 : 0,
+                   ctx->sc_variant};
+  for (int i = 0; i < nout && i < 18; ++i) out[i] = v[i];
   return DG_OK;
 }
 

@@ -114,10 +114,11 @@ class DGSolver:
         return t.data_ptr()
 
     def info(self):
-        out = np.zeros(15, dtype=np.int64)
-        self._chk(self._lib.dg_info(self._ctx, out.ctypes.data, 15))
+        out = np.zeros(18, dtype=np.int64)
+        self._chk(self._lib.dg_info(self._ctx, out.ctypes.data, 18))
         keys = ["ndim", "nloc", "nele", "nonods", "cg_nonods", "ncola", "ncolor", "nlevel", "nbface",
-                "built", "ngi", "sngi", "tma_variant", "batched_tma", "shared_faces"]
+                "built", "ngi", "sngi", "tma_variant", "batched_tma", "shared_faces", "batched_kernel",
+                "scaled_faces", "sc_variant"]
         return dict(zip(keys, out.tolist()))
 
     def close(self):
@@ -328,6 +329,27 @@ class DGSolver:
         self._chk(self._lib.dg_apply_batched(self._ctx, self._check_batched(x), self._check_batched(y),
                                              self._stream()))
         return y
+
+    def smooth_scaled(self, x, cv, x_out=None):
+        """x_out = x + (cv - w x - sum_f S_f x_f) on the scaled face blocks
+        S_f = W A_f, with cv = W b (the preconditioner's steps after its
+        zero-start one; FP32 CUDA tensors, x_out distinct from x)."""
+        torch = _torch()
+        for t in (x, cv):
+            if not (t.is_cuda and t.dtype == torch.float32 and t.is_contiguous() and t.numel() == self.nonods):
+                raise ValueError("expected a contiguous FP32 CUDA tensor with %d entries" % self.nonods)
+        x_out = torch.empty_like(x) if x_out is None else x_out
+        self._chk(self._lib.dg_smooth_scaled(self._ctx, x.data_ptr(), cv.data_ptr(), x_out.data_ptr(),
+                                             self._stream()))
+        return x_out
+
+    def smooth_scaled_batched(self, x, cv, x_out=None):
+        """smooth_scaled for 64 right-hand sides (RHS-interleaved FP32
+        vectors, the layout of apply_batched)."""
+        x_out = _torch().empty_like(cv) if x_out is None else x_out
+        self._chk(self._lib.dg_smooth_scaled_batched(self._ctx, self._check_batched(x), self._check_batched(cv),
+                                                     self._check_batched(x_out), self._stream()))
+        return x_out
 
     def smooth_pc_batched(self, x, b, x_out=None):
         """X_out = X + W (B - A X) with the batched preconditioner's BF16

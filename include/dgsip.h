@@ -88,10 +88,12 @@ void dg_destroy(dg_ctx* ctx);
 /* Message of the last failed call on ctx; ctx = NULL gives the last failed
  * dg_create / host-only helper on this thread. */
 const char* dg_last_error(const dg_ctx* ctx);
-/* out[0..14]: ndim, nloc, nele, nonods, cg_nonods, ncola, ncolor, nlevel,
+/* out[0..17]: ndim, nloc, nele, nonods, cg_nonods, ncola, ncolor, nlevel,
  * nbface, built, ngi, sngi, chosen bulk-copy launch shape, batched
  * bulk-copy form on/off, interior faces stored once in the reduced-precision
- * copies (0 = five blocks per element). */
+ * copies (0 = five blocks per element), batched smoothing kernel variant,
+ * preconditioner smoothing on scaled face blocks (see dg_smooth_scaled),
+ * launch shape of that kernel. */
 int  dg_info(const dg_ctx* ctx, int64_t* out, int32_t nout);
 /* Number of CUDA kernels this library has launched in this process (all
  * contexts); used to account for device work in benchmarks. */
@@ -227,6 +229,20 @@ int dg_precond_f32(dg_ctx* ctx, const float* r, float* z, void* stream);
  * get_residual_or_smooth(do_smooth=True), z06/volume_mf_diff.py:403.
  * x_out must not alias x. */
 int dg_smooth_pc(dg_ctx* ctx, const float* x, const float* b, float* x_out, void* stream);
+/* The same step as the mixed preconditioner runs it after its zero-start
+ * step, on the scaled face blocks S_ef = W_e A_ef (BF16; W_e = smooth_w *
+ * A_ee^{-1}): x_out = x + (cv - smooth_w x - sum_f S_ef x_nb(f)), where cv =
+ * W b.  Available when the scaled form is in use (3D, BF16 bulk-copy
+ * preconditioner, damped block-inverse smoother; dg_info out[16]); otherwise
+ * DG_ERR_STATE.  dg_smooth_pc runs the zero-start step for cv and then this
+ * one.  x_out must not alias x. */
+int dg_smooth_scaled(dg_ctx* ctx, const float* x, const float* cv, float* x_out, void* stream);
+/* dg_smooth_scaled for 64 right-hand sides on RHS-interleaved vectors (the
+ * layout of dg_apply_batched): the batched preconditioner's steps after its
+ * zero-start one (tensor cores, x split into BF16 hi + lo).  The batched
+ * preconditioner uses them with the mma.sync / tcgen05 gathered-x kernel
+ * variants 1-4. */
+int dg_smooth_scaled_batched(dg_ctx* ctx, const float* x, const float* cv, float* x_out, void* stream);
 /* Options of the mixed preconditioner, applied at the next mixed solve:
  * smoother 0 = three point-Jacobi sweeps per element block (as the
  * reference), 1 = damped exact block inverse smooth_w * A_ee^{-1};

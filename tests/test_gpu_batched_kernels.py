@@ -169,3 +169,52 @@ def test_batched_step_graphs_match_direct_launches(kernel):
     assert float(torch.abs(Xo - Xod).max() / torch.abs(Xod).max()) < 1e-12
     s.set_launch_options(use_graph=True)
     s.close()
+
+
+def test_scaled_batched_step_matches_single_rhs(tet5):
+    """The batched smoothing step on the scaled face blocks (X + C - w X -
+    sum_f S_f X_f, tensor cores with x split into BF16 hi + lo) against the
+    single-RHS step on the same blocks (FP32 x, CUDA cores), column by
+    column: the split keeps ~16 bits of x, so max-abs <= 1e-4 of max |y|."""
+    m, s = tet5
+    assert s.info()["scaled_faces"] == 1
+    g = torch.Generator(device="cuda:0").manual_seed(12)
+    X = torch.randn(s.nonods, 64, dtype=torch.float32, device="cuda:0", generator=g)
+    C = torch.randn(s.nonods, 64, dtype=torch.float32, device="cuda:0", generator=g)
+    Y = s.smooth_scaled_batched(X.reshape(-1).contiguous(), C.reshape(-1).contiguous()).reshape(s.nonods, 64)
+    again = s.smooth_scaled_batched(X.reshape(-1).contiguous(), C.reshape(-1).contiguous()).reshape(s.nonods, 64)
+    assert torch.equal(Y, again)
+    for q in (0, 31, 63):
+        y1 = s.smooth_scaled(X[:, q].contiguous(), C[:, q].contiguous())
+        err = _rel(Y[:, q], y1)
+        print("scaled batched step vs single RHS, column %d: %.3e" % (q, err))
+        assert err < 1e-4, (q, err)
+
+
+def test_batched_solve_scaled_faces_on_off(monkeypatch):
+    """The batched solve with its smoothing steps on the scaled face blocks
+    and on the unscaled blocks (DG_SCALED_FACES=0): both meet every FP64
+    tolerance, their solutions agree within 1e-7 and the iteration counts
+    stay within 10%."""
+    m = mesh.build_mesh("tet", 6, seed=2)
+    F = _modes(m, 8, seed=7)
+    out = {}
+    for scaled in ("0", "1"):
+        monkeypatch.setenv("DG_SCALED_FACES", scaled)
+        s = DGSolver(m, sfc.hilbert_sfc_order(m.cg_coords), SolverConfig(pre_smooth_its=2, post_smooth_its=2),
+                     element.p3_element(3))
+        s.build_operator()
+        s.set_batched_kernel("mma_sync4")
+        assert s.info()["scaled_faces"] == int(scaled)
+        Bm = torch.stack([s.rhs(torch.tensor(F[q], device="cuda:0")) for q in range(len(F))]).contiguous()
+        tol = 1e-10 * torch.linalg.norm(Bm, dim=1).cpu().numpy()
+        X = torch.zeros_like(Bm)
+        its, res = s.solve_mixed_batched(X, Bm, tol, raise_noconv=True)
+        assert (res <= tol).all()
+        out[scaled] = (int(max(its)), X.clone())
+        s.close()
+    (i0, x0), (i1, x1) = out["0"], out["1"]
+    d = float(torch.abs(x1 - x0).max() / torch.abs(x0).max())
+    print("batched solve scaled vs unscaled: its %d / %d, max rel diff %.3e" % (i0, i1, d))
+    assert d < 1e-7
+    assert abs(i1 - i0) <= max(2, 0.1 * i0)
