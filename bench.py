@@ -384,8 +384,30 @@ def batched_leg(args, s, m, dofs, dev, stream, ws, R64=None, RMX=None):
                 for q in range(args.nrhs))
     err_b = float(np.abs(Xb.cpu().numpy() - Ub).max() / np.abs(Ub).max())
     kern, tune_us = s.batched_tuning()
+    scaled = bool(s.info().get("scaled_faces", 0)) and kern in ("mma_sync4", "mma_sync8", "mma_sync_bulk",
+                                                                 "tcgen05_bulk")
+    sc_us = None
+    if scaled:
+        # the steps after the zero-start one (3 of the 5 BF16 launches of a
+        # preconditioner application): bsc_mma_kernel alone, CUDA events
+        g = torch.Generator(device=dev).manual_seed(1)
+        xs = torch.randn(dofs * 64, dtype=torch.float32, device=dev, generator=g)
+        cs = torch.randn(dofs * 64, dtype=torch.float32, device=dev, generator=g)
+        xo = torch.empty_like(xs)
+        for _ in range(3):
+            s.smooth_scaled_batched(xs, cs, xo)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(10):
+            s.smooth_scaled_batched(xs, cs, xo)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        sc_us = a0.elapsed_time(a1) * 1e3 / 10
+        del xs, cs, xo
     return {
         "smoothing_kernel": kern, "smoothing_kernel_us": tune_us,
+        "scaled_face_steps": scaled, "scaled_step_us": sc_us,
         "workload": "c4: the %s mesh with %d Fourier right-hand sides (8 modes each, wavenumbers 1..4, "
                     "N(0,1) amplitudes, seed %d), solved together" % (
                         "c2" if args.n == 20 else "n=%d" % args.n, args.nrhs, args.seed + 2),
@@ -396,9 +418,10 @@ def batched_leg(args, s, m, dofs, dev, stream, ws, R64=None, RMX=None):
         "speedup_vs_single_mixed": (ws * args.nrhs * dofs * args.steps / tb) / RMX["value"] if RMX else None,
         "speedup_vs_fp64": (ws * args.nrhs * dofs * args.steps / tb) / R64["value"] if R64 else None,
         "method": "lockstep flexible GMRES(%d) on RHS-interleaved FP32 vectors; BF16 block smoothing on "
-                  "tensor cores (x split into BF16 hi+lo; kernel chosen by the autotuner among CUDA cores, "
-                  "mma.sync tiles, mma.sync bulk-copy and tcgen05 bulk-copy), FP32 apply on CUDA cores; "
-                  "per-RHS FP64 refinement" % args.batched_m}
+                  "tensor cores (x split into BF16 hi+lo; zero-start step and restriction by the kernel the "
+                  "autotuner chose among CUDA cores, mma.sync tiles, mma.sync bulk-copy and tcgen05 forms; the "
+                  "other smoothing steps on the scaled face blocks W_e A_ef with mma.sync), FP32 apply on CUDA "
+                  "cores; per-RHS FP64 refinement" % args.batched_m}
 
 
 def run_ours(args):
