@@ -275,10 +275,11 @@ def config_block(args, m, extra=None):
 # DRAM bytes (read + write) per launch of the roofline kernels on the
 # 20^3 Kuhn-cube workload (48,000 tets): dram__bytes_read.sum +
 # dram__bytes_write.sum of a capture on the 18^3 mesh (34,992 tets) scaled
-# by the element count (BF16 step, FP32 apply, FP64 residual;
-# profiles/residual_tma_kernel_c2.md); other workloads report null.
+# by the element count (scaled-face step: profiles/smooth_scaled_tma_kernel_n18.md;
+# BF16 step, FP32 apply, FP64 residual: profiles/residual_tma_kernel_c2.md);
+# other workloads report null.
 TRAFFIC_C2 = {
-    "smooth_scaled": {"bytes_per_launch": None},
+    "smooth_scaled": {"bytes_per_launch": 166.7e6},
     "smooth_pc": {"bytes_per_launch": 240.2e6},
     "apply_f32": {"bytes_per_launch": 393.4e6},
     "apply_f64": {"bytes_per_launch": 773.9e6},
