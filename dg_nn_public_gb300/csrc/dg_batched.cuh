@@ -1656,13 +1656,15 @@ int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   Mixed& M = mixed_of(c);
   BatchState& S = batch_of(M);
   int rc;
-  const int nsm = c->cfg.pre_smooth_its;
+  const int nsm = mixed_steps(c);
   const float w = (float)c->cfg.jac_wei;
   float* cur = S.t3;
   float* other = S.t4;
   const bool bf = c->precond_bf16;
   // DG-level smoothing step k damped like the single-RHS preconditioner
-  auto wsk = [&](int k) -> const float* { return (nsm == 2 || c->omegas_set) && k < 4 ? M.d_ws + k : nullptr; };
+  auto wsk = [&](int k) -> const float* {
+    return ((nsm >= 2 && nsm <= kMaxSmoothSteps) || c->omegas_set) && k < kMaxSmoothSteps ? M.d_ws + k : nullptr;
+  };
   auto pc = [&](const float* xx, float* xo, int flags, float* rr1, const float* ws) -> int {
     if (bf) return bsmooth(c, M, S, c->batched_kernel, xx, r, xo, flags, rr1, ws, st);
     return bres<float>(c, M.blk, M.W, xx, r, nullptr, xo, flags, rr1, st, ws);

@@ -1797,6 +1797,14 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
   return DG_OK;
 }
 
+// DG-level smoothing steps of the mixed preconditioner (pre and post each):
+// DG_MIXED_SWEEPS when set, else kMixedChebSteps with the damped block
+// inverse (a Chebyshev polynomial of that degree), else the configured V(s,s)
+int mixed_steps(const dg_ctx* c) {
+  if (c->mixed_sweeps >= 0) return c->mixed_sweeps;
+  return c->mixed_smoother == 1 ? kMixedChebSteps : c->cfg.pre_smooth_its;
+}
+
 // one smoothing step of the preconditioner with x != 0: x_out = x + s W (b -
 // A x), s = *ws.  On the scaled face blocks, rhs is c = W b (formed by the
 // zero-start step); otherwise it is b.
@@ -1810,12 +1818,14 @@ int smooth_step(dg_ctx* c, const float* x, const float* rhs, float* x_out, cudaS
 int precond32(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   Mixed& M = mixed_of(c);
   int rc;
-  const int nsm = c->mixed_sweeps >= 0 ? c->mixed_sweeps : c->cfg.pre_smooth_its;
+  const int nsm = mixed_steps(c);
   float* cur = M.t3;
   float* other = M.t4;
   // per-step damping: pre-smoothing steps k = 0, 1, ... use ws[k], the
   // post-smoothing steps the same factors in reverse order
-  auto ws = [&](int k) -> const float* { return (nsm == 2 || c->omegas_set) && k < 4 ? M.d_ws + k : nullptr; };
+  auto ws = [&](int k) -> const float* {
+    return ((nsm >= 2 && nsm <= kMaxSmoothSteps) || c->omegas_set) && k < kMaxSmoothSteps ? M.d_ws + k : nullptr;
+  };
   // scaled-face steps: the zero-start step also keeps c = W r, which every
   // later step reads in place of r
   const float* rs = M.sc ? M.chat : r;
@@ -1957,15 +1967,20 @@ int set_smoother_schedule(dg_ctx* c, cudaStream_t st) {
   }
   CKL(c);
   const double lmax = lam / c->mixed_smooth_w;   // of A_ee^-1 A
-  const double beta = c->cheb_margin * lmax, alpha = beta / 8.0;
-  const double mid = 0.5 * (beta + alpha), half = 0.5 * (beta - alpha) * std::sqrt(0.5);
-  const double om0 = 1.0 / (mid + half), om1 = 1.0 / (mid - half);
-  c->mixed_wscale[0] = (float)(om0 / c->mixed_smooth_w);
-  c->mixed_wscale[1] = (float)(om1 / c->mixed_smooth_w);
+  const double beta = c->cheb_margin * lmax, alpha = beta / c->cheb_ratio;
+  const double mid = 0.5 * (beta + alpha), hw = 0.5 * (beta - alpha);
+  // roots of the degree-d Chebyshev polynomial on [alpha, beta], smallest
+  // factor first: 1 / (mid + hw cos(pi (2k + 1) / (2d)))
+  const int deg = std::min(kMaxSmoothSteps, std::max(2, mixed_steps(c)));
+  const double pi = 3.14159265358979323846;
+  for (int k = 0; k < deg; ++k) {
+    const double om = 1.0 / (mid + hw * std::cos(pi * (2 * k + 1) / (2.0 * deg)));
+    c->mixed_wscale[k] = (float)(om / c->mixed_smooth_w);
+  }
   c->smoother_lmax = lmax;
   if (c->verbose)
-    std::fprintf(stderr, "[build_mixed] smoother: lambda_max(A_ee^-1 A) ~ %.4f, damping %.4f, %.4f\n", lmax, om0,
-                 om1);
+    std::fprintf(stderr, "[build_mixed] smoother: lambda_max(A_ee^-1 A) ~ %.4f, degree %d, damping %.4f .. %.4f\n",
+                 lmax, deg, c->mixed_wscale[0] * c->mixed_smooth_w, c->mixed_wscale[deg - 1] * c->mixed_smooth_w);
   return DG_OK;
 }
 
@@ -2207,13 +2222,13 @@ int build_mixed(dg_ctx* c, cudaStream_t st) {
   CKL(c);
   if ((rc = setup_vcycle_cluster(c, st))) return rc;
   M.built = true;
-  if (!M.d_ws && (rc = dalloc(c, &M.d_ws, 4))) return rc;
+  if (!M.d_ws && (rc = dalloc(c, &M.d_ws, kMaxSmoothSteps))) return rc;
   if (!c->omegas_set && c->mixed_smoother == 1) {
     if ((rc = set_smoother_schedule(c, st))) return rc;
   } else if (!c->omegas_set) {
     for (float& f : c->mixed_wscale) f = 1.0f;
   }
-  CK(c, cudaMemcpyAsync(M.d_ws, c->mixed_wscale, sizeof(float) * 4, cudaMemcpyHostToDevice, st));
+  CK(c, cudaMemcpyAsync(M.d_ws, c->mixed_wscale, sizeof(float) * kMaxSmoothSteps, cudaMemcpyHostToDevice, st));
   CK(c, cudaStreamSynchronize(st));
   if (c->verbose)
     std::fprintf(stderr, "[build_mixed] ms: copies + smoother blocks + levels %.2f, dense coarse inverse (%d rows) %.2f\n",

@@ -54,6 +54,15 @@ struct DevLevel {
 
 }  // namespace
 
+// most DG-level smoothing steps per leg of the mixed preconditioner with
+// their own damping factor (Chebyshev roots or DG_MIXED_OMEGAS)
+constexpr int kMaxSmoothSteps = 8;
+// default smoothing steps per leg of the mixed preconditioner (c2: 2 / 3 / 4
+// / 5 / 6 / 8 steps with their best Chebyshev interval took 20.6 / 17.0 /
+// 14.0 / 13.8 / 14.1 / 15.3 ms at 78 / 54 / 38 / 33 / 30 / 27 inner steps;
+// c3: 2 / 4 / 5 / 6 steps 161 / 114 / 107 / 115 ms)
+constexpr int kMixedChebSteps = 5;
+
 struct dg_ctx {
   int dev = 0;
   int D = 0, N = 0, F = 0, NC = 0, VG = 0, SG = 0;
@@ -169,17 +178,22 @@ struct dg_ctx {
   // the launch chain of that V-cycle without launches of its own for the
   // transfers between levels (vcycle32_fused; DG_MIXED_VC_FUSED=0: off)
   bool vc32_fused = true;
-  // mixed preconditioner with two DG-level smoothing steps: step k damped by
-  // mixed_smooth_w * mixed_wscale[k] (pre-smoothing k = 0, 1; post-smoothing
-  // in reverse), a degree-2 Chebyshev polynomial smoother whose factors are
-  // set at each mixed build from an estimate of lambda_max(A_ee^-1 A)
-  // (set_smoother_schedule); other step counts take the uniform damping w
-  float mixed_wscale[4] = {1.0f, 1.0f, 1.0f, 1.0f};
+  // mixed preconditioner with 2 to 4 DG-level smoothing steps: step k damped
+  // by mixed_smooth_w * mixed_wscale[k] (pre-smoothing k = 0, 1, ...;
+  // post-smoothing in reverse), a Chebyshev polynomial smoother of that
+  // degree whose factors are set at each mixed build from an estimate of
+  // lambda_max(A_ee^-1 A) (set_smoother_schedule); one step takes the
+  // uniform damping w
+  float mixed_wscale[kMaxSmoothSteps] = {1.0f, 1.0f, 1.0f, 1.0f, 1.0f, 1.0f, 1.0f, 1.0f};
   double smoother_lmax = 0.0;
   // beta = margin x the estimated lambda_max (c2: margin 1.05 / 1.1 / 1.2
   // -> 80 / 84 / 88 inner steps; c3: 94 / 94 / 106); a larger margin keeps
   // the polynomial below 1 further past an underestimated lambda_max
   double cheb_margin = 1.05;
+  // the Chebyshev interval is [beta / cheb_ratio, beta] (c2 / c3 with 5 steps:
+  // ratio 32 / 64 / 128 -> 37 / 34 / 33 and - / 36 / - inner steps; with 2
+  // steps the ratio 8 of the first schedule)
+  double cheb_ratio = 64.0;
   bool omegas_set = false;   // DG_MIXED_OMEGAS given: its factors, for any step count
   // mixed inner FGMRES: per-step convergence test on the device, chunk
   // graphs with one conditional node per step (c2: 100 -> 98 inner steps,
@@ -966,6 +980,8 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (gb && gb[0]) c->general_build = gb[0] != '0';
     const char* cmg = std::getenv("DG_CHEB_MARGIN");
     if (cmg && cmg[0]) c->cheb_margin = std::max(1.0, std::atof(cmg));
+    const char* crt = std::getenv("DG_CHEB_RATIO");
+    if (crt && crt[0]) c->cheb_ratio = std::max(1.5, std::atof(crt));
     const char* mch = std::getenv("DG_MIXED_CHUNK");
     if (mch && mch[0]) c->mixed_chunk = std::max(1, std::atoi(mch));
     const char* cg = std::getenv("DG_COND_GRAPH");
@@ -975,7 +991,7 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
       c->omegas_set = true;
       for (float& v : c->mixed_wscale) v = 1.0f;
       const char* q = om;
-      for (int k = 0; k < 4 && *q; ++k) {
+      for (int k = 0; k < kMaxSmoothSteps && *q; ++k) {
         char* end = nullptr;
         const double v = std::strtod(q, &end);
         if (end == q) break;

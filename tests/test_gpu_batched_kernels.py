@@ -194,8 +194,9 @@ def test_scaled_batched_step_matches_single_rhs(tet5):
 def test_batched_solve_scaled_faces_on_off(monkeypatch):
     """The batched solve with its smoothing steps on the scaled face blocks
     and on the unscaled blocks (DG_SCALED_FACES=0): both meet every FP64
-    tolerance, their solutions agree within 1e-7 and the iteration counts
-    stay within 10%."""
+    tolerance, their solutions agree within 1e-7 and the scaled form needs
+    at most 10% more iterations (with the default 5-step Chebyshev smoothing
+    it needs fewer: 27 against 33 here)."""
     m = mesh.build_mesh("tet", 6, seed=2)
     F = _modes(m, 8, seed=7)
     out = {}
@@ -217,4 +218,4 @@ def test_batched_solve_scaled_faces_on_off(monkeypatch):
     d = float(torch.abs(x1 - x0).max() / torch.abs(x0).max())
     print("batched solve scaled vs unscaled: its %d / %d, max rel diff %.3e" % (i0, i1, d))
     assert d < 1e-7
-    assert abs(i1 - i0) <= max(2, 0.1 * i0)
+    assert i1 <= i0 + max(2, 0.1 * i0)

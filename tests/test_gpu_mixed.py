@@ -272,8 +272,8 @@ def test_scaled_face_smoothing_solve(kind, n, monkeypatch):
     """The mixed solve with the preconditioner's smoothing steps on the
     scaled face blocks (S_ef = W_e A_ef, c = W b: the self block is w I)
     against the same solve on the unscaled blocks: both meet the FP64
-    residual tolerance, the solutions agree within 1e-7 and the inner
-    iteration counts stay within 10% of each other."""
+    residual tolerance, the solutions agree within 1e-7 and the scaled form
+    needs at most 10% more inner iterations."""
     res = {}
     for scaled in ("0", "1"):
         monkeypatch.setenv("DG_SCALED_FACES", scaled)
@@ -286,4 +286,5 @@ def test_scaled_face_smoothing_solve(kind, n, monkeypatch):
         res[scaled] = (its, x.clone())
     (i0, x0), (i1, x1) = res["0"], res["1"]
     assert float(torch.abs(x1 - x0).max() / torch.abs(x0).max()) < 1e-7
-    assert abs(i1 - i0) <= max(2, 0.1 * i0), (i0, i1)
+    print("mixed solve scaled vs unscaled: its %d / %d" % (i0, i1))
+    assert i1 <= i0 + max(2, 0.1 * i0), (i0, i1)
