@@ -1383,6 +1383,10 @@ struct BatchState {
   float* inv = nullptr;
   double* r64 = nullptr;                    // (kNR, nonods) FP64 residuals, RHS-major
   float* chat = nullptr;                    // C = W R of the scaled-face steps (nonods, kNR)
+  // damping factors of the batched preconditioner's smoothing steps (its own
+  // Chebyshev degree and interval, from the mixed build's lambda_max)
+  float* d_wsb = nullptr;
+  int wsb_version = -1;
   int nblk = 0;
   // BF16 blocks + smoother matrices in the padded tensor-core layout of
   // bres_tc05_kernel (5,760 bytes per element), rebuilt per mixed build
@@ -1651,19 +1655,50 @@ int autotune_batched(dg_ctx* c, Mixed& M, BatchState& S, cudaStream_t st) {
   return DG_OK;
 }
 
+// Smoothing steps per leg of the batched preconditioner: DG_BATCHED_SWEEPS,
+// else DG_MIXED_SWEEPS, else kBatchedChebSteps with the damped block
+// inverse; with DG_MIXED_OMEGAS or without a lambda_max estimate the
+// single-RHS schedule
+bool batched_own_schedule(const dg_ctx* c) {
+  return c->batched_sweeps >= 0 || (c->mixed_sweeps < 0 && c->mixed_smoother == 1 && !c->omegas_set &&
+                                    c->smoother_lmax > 0.0);
+}
+
+int batched_steps(const dg_ctx* c) {
+  if (!batched_own_schedule(c)) return mixed_steps(c);
+  return c->batched_sweeps >= 0 ? c->batched_sweeps : kBatchedChebSteps;
+}
+
+// the batched factors on the device, once per mixed build
+int ensure_batched_schedule(dg_ctx* c, Mixed& M, BatchState& S, cudaStream_t st) {
+  if (S.d_wsb && S.wsb_version == c->mixed_version) return DG_OK;
+  int rc;
+  if (!S.d_wsb && (rc = dalloc(c, &S.d_wsb, kMaxSmoothSteps))) return rc;
+  float f[kMaxSmoothSteps];
+  for (int k = 0; k < kMaxSmoothSteps; ++k) f[k] = c->mixed_wscale[k];
+  const int nsm = batched_steps(c);
+  if (batched_own_schedule(c) && nsm >= 2 && c->smoother_lmax > 0.0)
+    cheb_factors(c, c->smoother_lmax, std::min(kMaxSmoothSteps, nsm), c->cheb_ratio_b, f);
+  CK(c, cudaMemcpyAsync(S.d_wsb, f, sizeof(f), cudaMemcpyHostToDevice, st));
+  CK(c, cudaStreamSynchronize(st));
+  S.wsb_version = c->mixed_version;
+  (void)M;
+  return DG_OK;
+}
+
 // batched preconditioner (same schedule as precond32, dense coarse level)
 int bprecond(dg_ctx* c, const float* r, float* z, cudaStream_t st) {
   Mixed& M = mixed_of(c);
   BatchState& S = batch_of(M);
   int rc;
-  const int nsm = mixed_steps(c);
+  const int nsm = batched_steps(c);
   const float w = (float)c->cfg.jac_wei;
   float* cur = S.t3;
   float* other = S.t4;
   const bool bf = c->precond_bf16;
   // DG-level smoothing step k damped like the single-RHS preconditioner
   auto wsk = [&](int k) -> const float* {
-    return ((nsm >= 2 && nsm <= kMaxSmoothSteps) || c->omegas_set) && k < kMaxSmoothSteps ? M.d_ws + k : nullptr;
+    return ((nsm >= 2 && nsm <= kMaxSmoothSteps) || c->omegas_set) && k < kMaxSmoothSteps ? S.d_wsb + k : nullptr;
   };
   auto pc = [&](const float* xx, float* xo, int flags, float* rr1, const float* ws) -> int {
     if (bf) return bsmooth(c, M, S, c->batched_kernel, xx, r, xo, flags, rr1, ws, st);
@@ -1822,6 +1857,8 @@ int run_bstep(dg_ctx* c, int j, int m, cudaStream_t st) {
       tag(c->cfg.pre_smooth_its),
       tag(c->cfg.post_smooth_its),
       tag(c->omegas_set),
+      tag(batched_steps(c)),
+      S.d_wsb,
       tag(M.dense_l),
       S.V,
       S.Z,
@@ -1902,6 +1939,7 @@ extern "C" int dg_solve_mixed_batched(dg_ctx* c, double* x, const double* b, int
   CK(c, cudaFuncSetAttribute(bres_tcw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTwDyn));
   CK(c, cudaFuncSetAttribute(bdense2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDnSmem));
   if ((rc = autotune_batched(c, M, batch_of(M), st))) return rc;
+  if ((rc = ensure_batched_schedule(c, M, batch_of(M), st))) return rc;
   CK(c, cudaMemsetAsync(c->d_err, 0, sizeof(int), st));   // bulk-copy wait time-outs land here
   BatchState& S = batch_of(M);
   const int64_t n = c->nonods;

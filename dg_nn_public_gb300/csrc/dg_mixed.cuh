@@ -1797,6 +1797,20 @@ int vcycle32(dg_ctx* c, const float* r_sfc, cudaStream_t st) {
   return DG_OK;
 }
 
+// Damping of a degree-deg Chebyshev smoother for A_ee^-1 A on [beta / ratio,
+// beta], beta = cheb_margin * lmax: the polynomial's roots, smallest factor
+// first, 1 / (mid + hw cos(pi (2k + 1) / (2 deg))), stored as factors of
+// the smoother matrices' own damping w
+void cheb_factors(const dg_ctx* c, double lmax, int deg, double ratio, float* out) {
+  const double beta = c->cheb_margin * lmax, alpha = beta / ratio;
+  const double mid = 0.5 * (beta + alpha), hw = 0.5 * (beta - alpha);
+  const double pi = 3.14159265358979323846;
+  for (int k = 0; k < deg; ++k) {
+    const double om = 1.0 / (mid + hw * std::cos(pi * (2 * k + 1) / (2.0 * deg)));
+    out[k] = (float)(om / c->mixed_smooth_w);
+  }
+}
+
 // DG-level smoothing steps of the mixed preconditioner (pre and post each):
 // DG_MIXED_SWEEPS when set, else kMixedChebSteps with the damped block
 // inverse (a Chebyshev polynomial of that degree), else the configured V(s,s)
@@ -1967,16 +1981,8 @@ int set_smoother_schedule(dg_ctx* c, cudaStream_t st) {
   }
   CKL(c);
   const double lmax = lam / c->mixed_smooth_w;   // of A_ee^-1 A
-  const double beta = c->cheb_margin * lmax, alpha = beta / c->cheb_ratio;
-  const double mid = 0.5 * (beta + alpha), hw = 0.5 * (beta - alpha);
-  // roots of the degree-d Chebyshev polynomial on [alpha, beta], smallest
-  // factor first: 1 / (mid + hw cos(pi (2k + 1) / (2d)))
   const int deg = std::min(kMaxSmoothSteps, std::max(2, mixed_steps(c)));
-  const double pi = 3.14159265358979323846;
-  for (int k = 0; k < deg; ++k) {
-    const double om = 1.0 / (mid + hw * std::cos(pi * (2 * k + 1) / (2.0 * deg)));
-    c->mixed_wscale[k] = (float)(om / c->mixed_smooth_w);
-  }
+  cheb_factors(c, lmax, deg, c->cheb_ratio, c->mixed_wscale);
   c->smoother_lmax = lmax;
   if (c->verbose)
     std::fprintf(stderr, "[build_mixed] smoother: lambda_max(A_ee^-1 A) ~ %.4f, degree %d, damping %.4f .. %.4f\n",

@@ -62,6 +62,11 @@ constexpr int kMaxSmoothSteps = 8;
 // 14.0 / 13.8 / 14.1 / 15.3 ms at 78 / 54 / 38 / 33 / 30 / 27 inner steps;
 // c3: 2 / 4 / 5 / 6 steps 161 / 114 / 107 / 115 ms)
 constexpr int kMixedChebSteps = 5;
+// ... and of the batched preconditioner, whose inner steps carry more fixed
+// work (per-RHS Gram-Schmidt, FP32 apply on CUDA cores, FP64 residuals):
+// c4 with 4 / 5 / 6 steps and ratio 32 / 64 / 128 took 213 / 196 / 166 ms
+// per 64 solves at 40 / 33 / 25 inner steps
+constexpr int kBatchedChebSteps = 6;
 
 struct dg_ctx {
   int dev = 0;
@@ -194,6 +199,10 @@ struct dg_ctx {
   // ratio 32 / 64 / 128 -> 37 / 34 / 33 and - / 36 / - inner steps; with 2
   // steps the ratio 8 of the first schedule)
   double cheb_ratio = 64.0;
+  // the batched preconditioner's schedule: steps per leg (-1 = kBatchedChebSteps,
+  // or DG_MIXED_SWEEPS when that is set) and Chebyshev interval ratio
+  int batched_sweeps = -1;
+  double cheb_ratio_b = 128.0;
   bool omegas_set = false;   // DG_MIXED_OMEGAS given: its factors, for any step count
   // mixed inner FGMRES: per-step convergence test on the device, chunk
   // graphs with one conditional node per step (c2: 100 -> 98 inner steps,
@@ -980,6 +989,10 @@ int dg_create(const dg_mesh_desc* m, const dg_config* cfg, dg_ctx** out) {
     if (gb && gb[0]) c->general_build = gb[0] != '0';
     const char* cmg = std::getenv("DG_CHEB_MARGIN");
     if (cmg && cmg[0]) c->cheb_margin = std::max(1.0, std::atof(cmg));
+    const char* bsw = std::getenv("DG_BATCHED_SWEEPS");
+    if (bsw && bsw[0]) c->batched_sweeps = std::atoi(bsw);
+    const char* bcr = std::getenv("DG_BATCHED_CHEB_RATIO");
+    if (bcr && bcr[0]) c->cheb_ratio_b = std::max(1.5, std::atof(bcr));
     const char* crt = std::getenv("DG_CHEB_RATIO");
     if (crt && crt[0]) c->cheb_ratio = std::max(1.5, std::atof(crt));
     const char* mch = std::getenv("DG_MIXED_CHUNK");
