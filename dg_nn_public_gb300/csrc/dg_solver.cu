@@ -215,8 +215,11 @@ struct dg_ctx {
   // chunk 10 / 5 / 4 / 3 -> 90 / 85 / 80 / 81 steps, 27.4 / 25.9 / 24.6 /
   // 25.0 ms; c3: chunk 10 / 5 -> 212 / 202 ms)
   // (with the adaptive cut below, c2: chunk 4 / 5 / 6 / 8 -> 24.73 / 24.61 /
-  // 24.51 / 24.78 ms at 80 / 80 / 80 / 81 steps)
-  int mixed_chunk = 6;
+  // 24.51 / 24.78 ms at 80 / 80 / 80 / 81 steps; with the 5-step Chebyshev
+  // smoothing, ~8 inner steps per refinement step: chunk 2 / 3 / 4 / 6 / 8
+  // -> 13.18 / 13.10 / 13.46 / 14.25 / 14.94 ms, c3: chunk 3 / 6 -> 103.9 /
+  // 106.6 ms)
+  int mixed_chunk = 3;
   // cut a chunk that would run past the inner target to the step count the
   // observed convergence rate predicts (its remaining steps run as direct
   // launches); DG_ADAPTIVE_CHUNK=0 keeps whole chunks.  c2: 84 -> 80 steps
