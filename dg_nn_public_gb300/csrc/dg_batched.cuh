@@ -248,18 +248,18 @@ __device__ __forceinline__ void ldm_x1_trans(uint32_t& r0, const void* p) {
 }
 
 // hi / lo BF16 parts of four consecutive values, stored at two 8-byte words
+// (lower column in the low half of each 32-bit word); two values per
+// conversion instruction, round to nearest even as a per-value conversion
 __device__ __forceinline__ void store_split4(unsigned char* hi, unsigned char* lo, float4 v) {
-  const __nv_bfloat16 h0 = __float2bfloat16_rn(v.x), h1 = __float2bfloat16_rn(v.y), h2 = __float2bfloat16_rn(v.z),
-                      h3 = __float2bfloat16_rn(v.w);
-  const __nv_bfloat16 l0 = __float2bfloat16_rn(v.x - __bfloat162float(h0)),
-                      l1 = __float2bfloat16_rn(v.y - __bfloat162float(h1)),
-                      l2 = __float2bfloat16_rn(v.z - __bfloat162float(h2)),
-                      l3 = __float2bfloat16_rn(v.w - __bfloat162float(h3));
+  const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y), h23 = __floats2bfloat162_rn(v.z, v.w);
+  const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+  const __nv_bfloat162 l01 = __floats2bfloat162_rn(v.x - f01.x, v.y - f01.y);
+  const __nv_bfloat162 l23 = __floats2bfloat162_rn(v.z - f23.x, v.w - f23.y);
   uint2 H, L;
-  H.x = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-  H.y = (uint32_t)__bfloat16_as_ushort(h2) | ((uint32_t)__bfloat16_as_ushort(h3) << 16);
-  L.x = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-  L.y = (uint32_t)__bfloat16_as_ushort(l2) | ((uint32_t)__bfloat16_as_ushort(l3) << 16);
+  H.x = *reinterpret_cast<const uint32_t*>(&h01);
+  H.y = *reinterpret_cast<const uint32_t*>(&h23);
+  L.x = *reinterpret_cast<const uint32_t*>(&l01);
+  L.y = *reinterpret_cast<const uint32_t*>(&l23);
   *reinterpret_cast<uint2*>(hi) = H;
   *reinterpret_cast<uint2*>(lo) = L;
 }
