@@ -87,7 +87,17 @@ _SIGNATURES = {
     "dg_sfc_levels": (_I, [C.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_int64, _P]),
     "dg_face_connectivity": (_I, [C.c_int32, C.c_int64, _P, _P, _P]),
     "dg_rap_contributions": (_I, [C.c_int32, C.c_int64, _P, _P, _P, _P, C.c_int64, _P, _P, C.c_int64, _P]),
+    # serving: native request queue
+    "dg_server_create": (_I, [C.c_int32, C.c_int32, C.POINTER(_P)]),
+    "dg_server_destroy": (_I, [_P]),
+    "dg_enqueue": (_I, [_P, _P, _P, _P, C.c_double, C.c_int32, C.c_int32, C.c_int32, C.c_double, _P,
+                        C.POINTER(C.c_int64)]),
+    "dg_poll": (_I, [_P, C.c_int64, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                     C.POINTER(C.c_double), _P]),
+    "dg_wait": (_I, [_P, C.c_int64, C.c_double, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                     C.POINTER(C.c_double), _P]),
 }
+DG_REQ_QUEUED, DG_REQ_RUNNING, DG_REQ_DONE = 0, 1, 2
 # entry points added by later translation units (bound when present)
 _OPTIONAL = {}
 

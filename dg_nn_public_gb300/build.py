@@ -20,7 +20,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libdgsip.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["dg_host.cpp", "dg_solver.cu"]
+SOURCES = ["dg_host.cpp", "dg_serve.cpp", "dg_solver.cu"]
 HEADERS = ["dg_internal.h", "dg_kernels.cuh", "dg_kernels2.cuh", "dg_mixed.cuh", "dg_batched.cuh", "dg_batched_tc.cuh",
            "dg_noalloc.cuh", "dg_vcycle_cluster.cuh"]
 

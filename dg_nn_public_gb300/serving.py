@@ -279,3 +279,77 @@ def latency_stats(results: List[Result]) -> dict:
             "mean_build_s": float(np.mean([r.build_s for r in results])),
             "mean_solve_s": float(np.mean([r.solve_s for r in results])),
             "mean_wait_s": float(np.mean([r.start - r.arrival for r in results]))}
+
+
+class NativeQueue:
+    """The library's own request queue (dg_server_create / dg_enqueue /
+    dg_poll / dg_wait in include/dgsip.h): ``nworkers`` native threads with
+    one CUDA stream each run queued solves on ``DGSolver`` contexts, one
+    request per context at a time, in arrival order per context.  A request
+    may carry a new per-element kappa: the worker rebuilds the context's
+    operator with it before solving.  x and b (FP64 CUDA tensors) are kept
+    referenced here until the request is reported done; the caller must not
+    use the solver in the meantime, and must have finished writing x and b
+    (e.g. torch.cuda.synchronize()) before enqueueing: the workers' streams
+    do not wait for the caller's."""
+
+    def __init__(self, nworkers: int = 2, device: int = 0):
+        import ctypes as C
+        from . import _capi
+        self._C = C
+        self._capi = _capi
+        self._lib = _capi.lib()
+        h = C.c_void_p()
+        _capi.check(self._lib.dg_server_create(int(device), int(nworkers), C.byref(h)))
+        self._h = h
+        self._keep: Dict[int, tuple] = {}
+
+    def enqueue(self, solver: DGSolver, x, b, tol: float, mode: str = "mixed", m: Optional[int] = None,
+                max_its: Optional[int] = None, inner_rtol: float = 1e-3, kappa: Optional[np.ndarray] = None) -> int:
+        C = self._C
+        if mode not in ("mixed", "fp64"):
+            raise ValueError("mode must be 'mixed' or 'fp64'")
+        k = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        if k is not None and k.size != solver.mesh.nele:
+            raise ValueError("kappa needs one value per element")
+        rid = C.c_int64(0)
+        self._capi.check(self._lib.dg_enqueue(
+            self._h, solver._ctx, solver._check_t(x, solver.nonods), solver._check_t(b, solver.nonods), float(tol),
+            0 if mode == "mixed" else 1, int(m if m is not None else solver.cfg.gmres_m),
+            int(max_its if max_its is not None else solver.cfg.gmres_its), float(inner_rtol),
+            None if k is None else k.ctypes.data, C.byref(rid)))
+        self._keep[rid.value] = (x, b, k, solver)
+        return rid.value
+
+    def _report(self, fn, rid, *args):
+        C = self._C
+        st, status, its = C.c_int32(0), C.c_int32(0), C.c_int32(0)
+        res = C.c_double(0.0)
+        secs = (C.c_double * 2)()
+        self._capi.check(fn(self._h, C.c_int64(rid), *args, C.byref(st), C.byref(status), C.byref(its),
+                            C.byref(res), C.cast(secs, C.c_void_p)))
+        if st.value != self._capi.DG_REQ_DONE:
+            return None
+        self._keep.pop(rid, None)
+        return {"status": status.value, "its": its.value, "res": res.value, "wait_s": secs[0], "run_s": secs[1]}
+
+    def poll(self, rid: int):
+        """None while queued or running; once done, a dict with the solve's
+        return code ("status"), its, res, wait_s and run_s (reported once)."""
+        return self._report(self._lib.dg_poll, rid)
+
+    def wait(self, rid: int, timeout: float = -1.0):
+        """poll() after waiting up to ``timeout`` seconds (< 0: no limit)."""
+        return self._report(self._lib.dg_wait, rid, self._C.c_double(float(timeout)))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.dg_server_destroy(self._h)
+            self._h = self._C.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -338,6 +338,43 @@ int dg_rap_contributions(int32_t ndim, int64_t nele, const int64_t* p1cg, const 
 int dg_face_connectivity(int32_t ndim, int64_t nele, const int64_t* corners /* (nele, ndim+1) */,
                          int64_t* nbf, int64_t* alnmt);
 
+/* ---- serving: native request queue (dg_enqueue / dg_poll) ----
+ * The reference serves one solve at a time from one Python thread on the
+ * default stream (z06/main.py:205-206 -> solve_for_diff); here nworkers host
+ * threads, each with its own non-blocking CUDA stream on `device`, take the
+ * queued requests in arrival order.  A request runs, on its context, the
+ * optional operator rebuild for new diffusivities (dg_set_kappa with a copy
+ * of kappa taken at enqueue time, then dg_build_operator) and the solve:
+ * mode 0 dg_solve_mixed(tol, m, max_its, inner_rtol), mode 1 dg_gmres(tol,
+ * m, max_its).  A context serves one request at a time; requests on one
+ * context run in their order, requests on other contexts may pass a request
+ * that waits for its context.  x and b are device pointers of the context's
+ * size that must stay valid, and the context must not be used by the caller,
+ * until the request is reported done; the workers' streams do not wait for
+ * the caller's streams, so x and b must be ready when dg_enqueue is called.
+ * Results are those of the same calls made directly. */
+typedef struct dg_server dg_server;
+enum { DG_REQ_QUEUED = 0, DG_REQ_RUNNING = 1, DG_REQ_DONE = 2 };
+/* 1 <= nworkers <= 64; DG_ERR_CUDA without such a device. */
+int dg_server_create(int32_t device, int32_t nworkers, dg_server** out);
+/* Runs the queued requests to the end, then stops the workers. */
+int dg_server_destroy(dg_server* srv);
+/* *id receives the request's id (> 0). kappa [host] (nele) or NULL = keep
+ * the context's operator. */
+int dg_enqueue(dg_server* srv, dg_ctx* ctx, double* x, const double* b, double tol, int32_t mode, int32_t m,
+               int32_t max_its, double inner_rtol, const double* kappa, int64_t* id);
+/* *state = DG_REQ_QUEUED / RUNNING / DONE (may be NULL).  Once DONE:
+ * status = the solve's return code (DG_OK, DG_ERR_NOCONV, ...; the message
+ * is dg_last_error(ctx)), its, res_norm and seconds[2] = {queued, running}
+ * (each may be NULL), and the request is forgotten: a later poll of its id
+ * returns DG_ERR_ARG. */
+int dg_poll(dg_server* srv, int64_t id, int32_t* state, int32_t* status, int32_t* its, double* res_norm,
+            double* seconds);
+/* dg_poll after waiting until the request is done or timeout_s has passed
+ * (timeout_s < 0: no limit). */
+int dg_wait(dg_server* srv, int64_t id, double timeout_s, int32_t* state, int32_t* status, int32_t* its,
+            double* res_norm, double* seconds);
+
 #ifdef __cplusplus
 }
 #endif

@@ -157,3 +157,20 @@ def test_sfc_order_in_validates_reference_curve(lib):
     with pytest.raises(_capi.DGError) as e:
         _capi.sfc_order(order=bad)
     assert e.value.code == _capi.DG_ERR_ARG
+
+
+def test_server_argument_checks(lib):
+    """The native request queue rejects bad arguments before it touches a
+    device: worker counts out of range, a missing server or context, an
+    unknown mode, and polls of unknown servers; destroying NULL is a no-op."""
+    h = ctypes.c_void_p()
+    assert lib.dg_server_create(0, 0, ctypes.byref(h)) == _capi.DG_ERR_ARG
+    assert lib.dg_server_create(0, 65, ctypes.byref(h)) == _capi.DG_ERR_ARG
+    assert b"nworkers" in lib.dg_last_error(None)
+    rid = ctypes.c_int64(0)
+    rc = lib.dg_enqueue(None, None, None, None, 1e-10, 0, 30, 100, 1e-3, None, ctypes.byref(rid))
+    assert rc == _capi.DG_ERR_ARG
+    st = ctypes.c_int32(0)
+    assert lib.dg_poll(None, 1, ctypes.byref(st), None, None, None, None) == _capi.DG_ERR_ARG
+    assert lib.dg_wait(None, 1, 0.0, ctypes.byref(st), None, None, None, None) == _capi.DG_ERR_ARG
+    assert lib.dg_server_destroy(None) == _capi.DG_OK

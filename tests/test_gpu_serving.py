@@ -49,3 +49,61 @@ def test_admission_respects_budget():
     stats = serving.latency_stats(res)
     assert stats["p99_s"] >= stats["p50_s"] > 0
     srv.close()
+
+
+def test_native_queue_matches_direct_solves():
+    """The library's request queue (dg_enqueue / dg_poll, two worker threads
+    with a stream each) on two contexts with interleaved requests, some with
+    a new kappa (the worker rebuilds the operator first): every result equals
+    the same sequence of calls made directly on twin contexts (<= 1e-12
+    relative, deterministic kernels), meets its tolerance, and requests on
+    one context run in their order."""
+    from dg_nn_public_gb300 import element, mesh, sfc
+    from dg_nn_public_gb300.solver import DGSolver, SolverConfig
+
+    def solver(m):
+        s = DGSolver(m, sfc.hilbert_sfc_order(m.cg_coords), SolverConfig(pre_smooth_its=2, post_smooth_its=2),
+                     element.p3_element(3))
+        s.set_build_mode("affine")
+        s.build_operator()
+        return s
+
+    meshes = [mesh.build_mesh("tet", n, seed=0) for n in (4, 5)]
+    queued = [solver(m) for m in meshes]
+    direct = [solver(m) for m in meshes]
+    rng = np.random.default_rng(11)
+    plan = []   # (context index, kappa or None, mode)
+    for k in range(7):
+        c = k % 2
+        kap = np.exp(0.5 * rng.standard_normal(meshes[c].nele)) if k in (0, 1, 2, 5) else None
+        plan.append((c, kap, "fp64" if k == 3 else "mixed"))
+    # right-hand sides formed before the queue runs: a context with requests
+    # in flight belongs to the queue
+    rhs = []
+    for c, kap, mode in plan:
+        b = direct[c].rhs(torch.ones(direct[c].nonods, dtype=torch.float64, device="cuda:0"))
+        rhs.append((b, 1e-10 * float(torch.linalg.norm(b))))
+    xs = [torch.zeros_like(b) for b, _ in rhs]
+    torch.cuda.synchronize()   # the workers' streams do not wait for this thread's stream
+    q = serving.NativeQueue(nworkers=2)
+    jobs = []
+    for (c, kap, mode), (b, tol), x in zip(plan, rhs, xs):
+        jobs.append((q.enqueue(queued[c], x, b, tol, mode=mode, kappa=kap), x, b, tol))
+    outs = [q.wait(rid, timeout=120.0) for rid, _, _, _ in jobs]
+    q.close()
+    assert all(o is not None and o["status"] == 0 for o in outs), outs
+    for (c, kap, mode), (rid, x, b, tol), o in zip(plan, jobs, outs):
+        s = direct[c]
+        if kap is not None:
+            s.set_kappa(kap)
+            s.build_operator()
+        xd = torch.zeros_like(b)
+        if mode == "mixed":
+            s.solve_mixed(xd, b, tol)
+        else:
+            s.gmres(xd, b, tol)
+        d = float(torch.abs(x - xd).max() / torch.abs(xd).max())
+        assert d <= 1e-12, (rid, mode, d)
+        assert o["res"] <= tol
+    for s in queued + direct:
+        s.close()
