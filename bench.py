@@ -690,6 +690,9 @@ def run_ours(args):
         "mixed": None if RMX is None else {
             "value": RMX["value"], "ms_per_step": RMX["t_ms"] / args.steps, "its": RMX["its"],
             "final_residual": RMX["res"], "tol": RMX["tol"], "gpu_launches": RMX["launches"],
+            "preconditioner": ("DG->CG SFC-MG V-cycle in FP32 / BF16: 5 Chebyshev smoothing steps per leg on "
+                               "[beta/64, beta] of A_ee^-1 A with the damped block inverse, the steps after the "
+                               "zero-start one on scaled face blocks W_e A_ef; dense FP32 coarse inverse"),
             "speedup_vs_fp64": (RMX["value"] / R64["value"]) if R64 else None},
         "its": its_list, "rel_residual": rel_res, "max_nodal_error_vs_exact": err_inf,
         "mixed_vs_fp64_max_rel": mixed_vs_fp64,
