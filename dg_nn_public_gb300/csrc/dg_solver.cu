@@ -197,7 +197,11 @@ struct dg_ctx {
   double cheb_margin = 1.05;
   // the Chebyshev interval is [beta / cheb_ratio, beta] (c2 / c3 with 5 steps:
   // ratio 32 / 64 / 128 -> 37 / 34 / 33 and - / 36 / - inner steps; with 2
-  // steps the ratio 8 of the first schedule)
+  // steps the ratio 8 of the first schedule).  With host checks every 3
+  // steps, ratio 128 gave c2 12.88 ms (30 steps) and c3 99.3 ms (33) against
+  // 13.26 / 104.9 ms, but on a 2D case (64^2 x 2 triangles) the inner steps
+  // then moved from 64 to 81 with a rounding-level change of the coarse
+  // inverse; 64 keeps them within 2
   double cheb_ratio = 64.0;
   // the batched preconditioner's schedule: steps per leg (-1 = kBatchedChebSteps,
   // or DG_MIXED_SWEEPS when that is set) and Chebyshev interval ratio
