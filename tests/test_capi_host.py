@@ -174,3 +174,15 @@ def test_server_argument_checks(lib):
     assert lib.dg_poll(None, 1, ctypes.byref(st), None, None, None, None) == _capi.DG_ERR_ARG
     assert lib.dg_wait(None, 1, 0.0, ctypes.byref(st), None, None, None, None) == _capi.DG_ERR_ARG
     assert lib.dg_server_destroy(None) == _capi.DG_OK
+
+
+def test_native_queue_needs_a_device():
+    """Without a CUDA device the queue reports DG_ERR_CUDA at creation
+    instead of starting workers that could not run anything."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from dg_nn_public_gb300 import serving
+    with pytest.raises(_capi.DGError) as ei:
+        serving.NativeQueue(nworkers=1)
+    assert ei.value.code == _capi.DG_ERR_CUDA
