@@ -82,6 +82,7 @@ struct dg_ctx {
   std::vector<int> bf_elem, bf_face, bf_type;
   // device allocations (released in dg_destroy)
   std::vector<void*> allocs;
+  int64_t dev_bytes = 0;   // sum of the allocations in allocs (freed only by dg_destroy)
   double* d_x = nullptr;
   int *d_nbe = nullptr, *d_nbface = nullptr, *d_aln = nullptr, *d_bct = nullptr;
   // shared-face tables of the reduced-precision copies (3D): d_fref5[e][j]
@@ -327,6 +328,7 @@ int dalloc(dg_ctx* c, T** p, size_t count) {
   cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
   if (e != cudaSuccess) return fail(c, DG_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   c->allocs.push_back((void*)*p);
+  c->dev_bytes += (int64_t)(count * sizeof(T));
   return DG_OK;
 }
 
@@ -915,11 +917,11 @@ int dg_info(const dg_ctx* ctx, int64_t* out, int32_t nout) {
                   ctx->precond_bf16;
   const bool sc = ctx->scaled_faces && ctx->D == 3 && ctx->precond_bf16 && ctx->bf16_tma && !sf &&
                   ctx->mixed_smoother == 1;
-  int64_t v[18] = {ctx->D, ctx->N, ctx->B, ctx->nonods, ctx->ncg, (int64_t)ctx->cola.size(), ctx->ncolor,
+  int64_t v[19] = {ctx->D, ctx->N, ctx->B, ctx->nonods, ctx->ncg, (int64_t)ctx->cola.size(), ctx->ncolor,
                    (int64_t)ctx->lev.size(), ctx->nbf, ctx->built ? 1 : 0, ctx->VG, ctx->SG, ctx->tma_variant,
                    ctx->batched_kernel == 3 ? 1 : 0, sf ? ctx->nface_sh : 0, ctx->batched_kernel, sc ? 1 : 0,
-                   ctx->sc_variant};
-  for (int i = 0; i < nout && i < 18; ++i) out[i] = v[i];
+                   ctx->sc_variant, ctx->dev_bytes};
+  for (int i = 0; i < nout && i < 19; ++i) out[i] = v[i];
   return DG_OK;
 }
 

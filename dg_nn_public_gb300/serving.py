@@ -11,11 +11,12 @@ level values and the mixed-precision copies in its slot before solving.
 * Resident state: per mesh size the host mesh, its SFC ordering and a pool
   of slots; a slot is one library context (``DGSolver``) with every device
   buffer of a solve on that mesh, created once and reused.
-* Admission by HBM footprint: the footprint of a slot is measured when its
-  first slot is set up (device memory in use before / after set-up, build
-  and one warm solve); a new slot is created only while the sum of the
-  slots' footprints stays within ``hbm_budget``; a request waits (FIFO) until
-  a slot of its mesh is free or can be created.
+* Admission by HBM footprint: the footprint of a mesh's slot is taken when
+  its first slot is set up (the device bytes the library allocated for the
+  context through set-up, build and one warm solve, plus the request's
+  vectors and an allowance for streams and graphs); a new slot is created
+  only while the sum of the slots' footprints stays within ``hbm_budget``; a
+  request waits (FIFO) until a slot of its mesh is free or can be created.
 * Continuous batching: requests that arrive while others run are admitted
   as soon as a slot frees up or fits; every admitted request runs on its own
   CUDA stream from its own host thread (the library releases the GIL inside
@@ -111,11 +112,12 @@ class SolveServer:
         self._lock = threading.Condition()
 
     # -- slots ------------------------------------------------------------
+    # device memory of a slot beyond what its library context allocates: the
+    # context's streams and captured CUDA graphs
+    GRAPH_ALLOWANCE = 64 << 20
+
     def _new_slot(self, n: int) -> _Slot:
         torch = _torch()
-        # no device-wide synchronize: other slots may be capturing CUDA graphs
-        # on their streams, and a device synchronize during a capture fails
-        free0, _ = torch.cuda.mem_get_info(self.device)
         s = DGSolver(self.meshes[n], self.orders[n], self.cfg, self.el)
         s.set_mixed_options(dense_max=self.dense_max)
         # every request rebuilds the operator: the affine block build (equal
@@ -131,8 +133,10 @@ class SolveServer:
                 x = torch.zeros_like(b)
                 s.solve_mixed(x, b, 1e-6 * float(torch.linalg.norm(b)))
             slot.stream.synchronize()
-            free1, _ = torch.cuda.mem_get_info(self.device)
-            self.footprint[n] = float(max(free0 - free1, 1))
+            # the library reports its own allocations for the context, so
+            # slots of other meshes allocating at the same time do not enter
+            # the figure; add the request's vectors (f, b, x) and the graphs
+            self.footprint[n] = float(s.info()["device_bytes"] + 3 * 8 * s.nonods + self.GRAPH_ALLOWANCE)
         self.used += self.footprint[n]
         self.slots[n].append(slot)
         return slot

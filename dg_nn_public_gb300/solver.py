@@ -114,11 +114,11 @@ class DGSolver:
         return t.data_ptr()
 
     def info(self):
-        out = np.zeros(18, dtype=np.int64)
-        self._chk(self._lib.dg_info(self._ctx, out.ctypes.data, 18))
+        out = np.zeros(19, dtype=np.int64)
+        self._chk(self._lib.dg_info(self._ctx, out.ctypes.data, 19))
         keys = ["ndim", "nloc", "nele", "nonods", "cg_nonods", "ncola", "ncolor", "nlevel", "nbface",
                 "built", "ngi", "sngi", "tma_variant", "batched_tma", "shared_faces", "batched_kernel",
-                "scaled_faces", "sc_variant"]
+                "scaled_faces", "sc_variant", "device_bytes"]
         return dict(zip(keys, out.tolist()))
 
     def close(self):

@@ -88,12 +88,13 @@ void dg_destroy(dg_ctx* ctx);
 /* Message of the last failed call on ctx; ctx = NULL gives the last failed
  * dg_create / host-only helper on this thread. */
 const char* dg_last_error(const dg_ctx* ctx);
-/* out[0..17]: ndim, nloc, nele, nonods, cg_nonods, ncola, ncolor, nlevel,
+/* out[0..18]: ndim, nloc, nele, nonods, cg_nonods, ncola, ncolor, nlevel,
  * nbface, built, ngi, sngi, chosen bulk-copy launch shape, batched
  * bulk-copy form on/off, interior faces stored once in the reduced-precision
  * copies (0 = five blocks per element), batched smoothing kernel variant,
  * preconditioner smoothing on scaled face blocks (see dg_smooth_scaled),
- * launch shape of that kernel. */
+ * launch shape of that kernel, bytes of device memory the context has
+ * allocated (held until dg_destroy). */
 int  dg_info(const dg_ctx* ctx, int64_t* out, int32_t nout);
 /* Number of CUDA kernels this library has launched in this process (all
  * contexts); used to account for device work in benchmarks. */
